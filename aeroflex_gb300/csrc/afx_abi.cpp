@@ -1,0 +1,871 @@
+// C ABI of the GB300 rans library (include/afx_rans.h) and the host
+// orchestration of the device path: buffers, CUDA-graph capture of iteration
+// chunks, the run_solver loop with a device-resident convergence test, and
+// the reference-order <-> device-order state exchange.
+#include "../../include/afx_rans.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "afx_host.hpp"
+#include "afx_launch.hpp"
+
+namespace afx {
+void enqueue_permute_in(int n, const int* cell_old, const void* src, void* dst, cudaStream_t s);
+void enqueue_permute_out(int n, const int* cell_old, const void* src, void* dst, cudaStream_t s);
+void enqueue_to_f32(int n, const void* src, void* dst, cudaStream_t s);
+}  // namespace afx
+
+using namespace afx;
+
+static thread_local std::string g_err;
+
+#define AFX_CUDA(x)                                                                                      \
+    do {                                                                                                 \
+        cudaError_t e_ = (x);                                                                            \
+        if (e_ != cudaSuccess) throw Error(AFX_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+template <class F>
+static int guarded(F&& f) {
+    try {
+        f();
+        return AFX_OK;
+    } catch (const Error& e) {
+        g_err = e.what();
+        return e.code;
+    } catch (const std::out_of_range& e) {
+        g_err = std::string("unknown name: ") + e.what();
+        return AFX_ERR_ARG;
+    } catch (const std::exception& e) {
+        g_err = e.what();
+        return AFX_ERR_ARG;
+    }
+}
+
+struct afx_mesh_s {
+    HostMesh m;
+    DeviceLayout L;
+    bool has_layout = false;
+    const DeviceLayout& layout() {
+        if (!has_layout) {
+            L = build_layout(m);
+            has_layout = true;
+        }
+        return L;
+    }
+};
+
+struct afx_config_s {
+    Settings s;
+};
+
+namespace {
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    void alloc(size_t n) {
+        if (n == 0) n = 16;
+        AFX_CUDA(cudaMalloc(&p, n));
+        bytes = n;
+    }
+    void upload(const void* src, size_t n, cudaStream_t s) {
+        alloc(n);
+        AFX_CUDA(cudaMemcpyAsync(p, src, n, cudaMemcpyHostToDevice, s));
+    }
+    ~DevBuf() {
+        if (p) cudaFree(p);
+    }
+};
+
+template <class T>
+std::vector<T> cast_vec(const std::vector<double>& v) {
+    return std::vector<T>(v.begin(), v.end());
+}
+
+}  // namespace
+
+struct afx_solver_s {
+    Settings st;
+    // per boundary edge (reference order): patch, owner cell, edge centre, normal, length
+    struct BoundaryEdge {
+        std::string patch;
+        int owner_dev;
+        double ex, ey, nx, ny, L;
+    };
+    std::vector<BoundaryEdge> bedges;
+    std::vector<int> cell_old;  // device cell -> reference cell
+    bool fp64 = true;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    StepArgs a;
+    std::vector<std::unique_ptr<DevBuf>> bufs;
+    Ctrl* h_ctrl = nullptr;  // pinned
+    double* h_stage = nullptr;  // pinned staging for state exchange
+    size_t h_stage_bytes = 0;
+    DevBuf d_stage, d_cell_old;
+    int parity = 0;
+    int pending_last = -1;  // parity read by the last iteration whose qW is not materialised
+    std::map<std::pair<int, int>, cudaGraphExec_t> graphs;
+    std::atomic<int> stop{0};
+    std::vector<double> hist;
+    double last_sec = 0;
+    std::vector<int> boundary_type;           // per boundary edge
+    std::vector<FarfieldVars> boundary_vars;  // solver.h:214-230
+    struct PatchForces {
+        DevBuf cell, geo, cp, sums;
+        int n = 0;
+        double xmin = 0, xmax = 0, x_moment = 0, y_moment = 0;
+    };
+    std::map<std::string, std::unique_ptr<PatchForces>> patches;
+
+    void* dalloc(size_t n) {
+        bufs.emplace_back(new DevBuf());
+        bufs.back()->alloc(n);
+        AFX_CUDA(cudaMemsetAsync(bufs.back()->p, 0, bufs.back()->bytes, stream));
+        return bufs.back()->p;
+    }
+    template <class T>
+    const void* dupload(const std::vector<T>& v) {
+        bufs.emplace_back(new DevBuf());
+        bufs.back()->upload(v.data(), v.size() * sizeof(T), stream);
+        return bufs.back()->p;
+    }
+
+    ~afx_solver_s() {
+        if (stream) cudaStreamSynchronize(stream);
+        for (auto& g : graphs) cudaGraphExecDestroy(g.second);
+        if (h_ctrl) cudaFreeHost(h_ctrl);
+        if (h_stage) cudaFreeHost(h_stage);
+        bufs.clear();
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    // get_boundary_variables, solver.h:597-611
+    FarfieldVars freestream() const {
+        for (size_t b = 0; b < boundary_type.size(); ++b)
+            if (boundary_type[b] == BC_FARFIELD || boundary_type[b] == BC_INLET_OUTLET) return boundary_vars[b];
+        return FarfieldVars();
+    }
+
+    // set_bcs (solver.h:200-247): per-boundary type and variables
+    void set_bcs() {
+        const size_t B = bedges.size();
+        boundary_type.assign(B, BC_INTERNAL);
+        boundary_vars.assign(B, FarfieldVars());
+        for (size_t b = 0; b < B; ++b) {
+            auto it = st.bcs.find(bedges[b].patch);
+            if (it == st.bcs.end())
+                throw Error(AFX_ERR_CONFIG, "no boundary condition for patch '" + bedges[b].patch + "'");
+            boundary_type[b] = Settings::bc_code(it->second.type);
+            if (boundary_type[b] == BC_FARFIELD) boundary_vars[b] = it->second.vars;
+        }
+    }
+
+    // refill_bcs (solver.h:259-274): ghost states from the boundary variables
+    void refill_bcs() {
+        const size_t B = boundary_type.size();
+        std::vector<double> bq(4 * B);
+        for (size_t b = 0; b < B; ++b) conservative(st, boundary_vars[b], &bq[4 * b]);
+        std::vector<int> bt(boundary_type.begin(), boundary_type.end());
+        AFX_CUDA(cudaMemcpyAsync((void*)a.btype, bt.data(), B * sizeof(int), cudaMemcpyHostToDevice, stream));
+        if (fp64) {
+            AFX_CUDA(cudaMemcpyAsync((void*)a.bq, bq.data(), bq.size() * 8, cudaMemcpyHostToDevice, stream));
+        } else {
+            std::vector<float> f(bq.begin(), bq.end());
+            AFX_CUDA(cudaMemcpyAsync((void*)a.bq, f.data(), f.size() * 4, cudaMemcpyHostToDevice, stream));
+        }
+        AFX_CUDA(cudaStreamSynchronize(stream));
+    }
+
+    void sync_shadow(int p) {
+        if (!fp64) enqueue_to_f32(a.n_cells, a.qm[p], a.qsh[p], stream);
+    }
+
+    void enqueue_iteration(int p) {
+        if (fp64) enqueue_iteration_f64(a, p, stream);
+        else enqueue_iteration_f32(a, p, stream);
+    }
+
+    cudaGraphExec_t graph(int k, int p) {
+        auto key = std::make_pair(k, p);
+        auto it = graphs.find(key);
+        if (it != graphs.end()) return it->second;
+        cudaGraph_t g;
+        AFX_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        int q = p;
+        for (int i = 0; i < k; ++i) {
+            enqueue_iteration(q);
+            q ^= 1;
+        }
+        AFX_CUDA(cudaStreamEndCapture(stream, &g));
+        cudaGraphExec_t ex;
+        AFX_CUDA(cudaGraphInstantiate(&ex, g, 0));
+        cudaGraphDestroy(g);
+        graphs[key] = ex;
+        return ex;
+    }
+
+    int chunk() const {
+        if (a.n_cells >= 1000000) return 2;
+        if (a.n_cells >= 100000) return 8;
+        return 32;
+    }
+
+    void set_ctrl(int run_mode, int max_it, double tol) {
+        std::memset(h_ctrl, 0, sizeof(Ctrl));
+        h_ctrl->run_mode = run_mode;
+        h_ctrl->max_it = max_it;
+        h_ctrl->tol = tol;
+        AFX_CUDA(cudaMemcpyAsync(a.ctrl, h_ctrl, sizeof(Ctrl), cudaMemcpyHostToDevice, stream));
+    }
+
+    void read_ctrl() {
+        AFX_CUDA(cudaMemcpyAsync(h_ctrl, a.ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, stream));
+        AFX_CUDA(cudaStreamSynchronize(stream));
+    }
+
+    void materialize_qW() {
+        if (pending_last < 0) return;
+        if (fp64) enqueue_last_stage_residual_f64(a, pending_last, stream);
+        else enqueue_last_stage_residual_f32(a, pending_last, stream);
+        pending_last = -1;
+    }
+
+    // Runs n iterations (run_mode 0) or the run_solver loop (run_mode 1).
+    // Returns the number of iterations executed.
+    int run(int n, int run_mode, double tol) {
+        const int p0 = parity;
+        AFX_CUDA(cudaEventRecord(ev0, stream));
+        const int K = chunk();
+        int launched = 0;
+        bool stopped = false;
+        while (launched < n) {
+            const int k = (n - launched >= K) ? K : 1;
+            AFX_CUDA(cudaGraphLaunch(graph(k, (p0 + launched) & 1), stream));
+            launched += k;
+            if (run_mode == 1 || launched >= n || stop.load()) {
+                read_ctrl();
+                if (h_ctrl->done) break;
+                if (stop.load()) {
+                    stopped = true;
+                    break;
+                }
+            }
+        }
+        AFX_CUDA(cudaEventRecord(ev1, stream));
+        read_ctrl();
+        float ms = 0;
+        AFX_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+        last_sec = ms * 1e-3;
+        const int done = h_ctrl->iter;
+        parity = p0 ^ (done & 1);
+        if (done > 0) pending_last = parity ^ 1;
+        (void)tol;
+        if (stopped) stop.store(0);
+        return stopped ? -done - 1 : done;
+    }
+};
+
+extern "C" {
+
+const char* afx_last_error(void) { return g_err.c_str(); }
+const char* afx_version(void) { return "afx-gb300 0.1 (sm_103a)"; }
+
+// ------------------------------------------------------------------ mesh
+int afx_mesh_load(const char* path, afx_mesh* out) {
+    return guarded([&] {
+        if (!path || !out) throw Error(AFX_ERR_ARG, "null argument");
+        auto* m = new afx_mesh_s();
+        try {
+            m->m = load_gmsh(path);
+        } catch (...) {
+            delete m;
+            throw;
+        }
+        *out = m;
+    });
+}
+
+int afx_mesh_from_arrays(int n_nodes, const double* x, const double* y, int n_cells, const int* cell_nodes,
+                         int n_bedges, const int* bedge_nodes, const int* bedge_patch, const char* patch_names,
+                         afx_mesh* out) {
+    return guarded([&] {
+        if (!x || !y || !cell_nodes || !out || n_nodes <= 0 || n_cells <= 0 || n_bedges < 0)
+            throw Error(AFX_ERR_ARG, "bad mesh arrays");
+        std::vector<std::string> names;
+        {
+            std::string all(patch_names ? patch_names : "");
+            size_t pos = 0;
+            while (pos <= all.size()) {
+                size_t nl = all.find('\n', pos);
+                if (nl == std::string::npos) nl = all.size();
+                if (nl > pos) names.push_back(all.substr(pos, nl - pos));
+                pos = nl + 1;
+            }
+        }
+        auto m = std::make_unique<afx_mesh_s>();
+        HostMesh& h = m->m;
+        h.nodesX.assign(x, x + n_nodes);
+        h.nodesY.assign(y, y + n_nodes);
+        h.cellsNodes.resize(n_cells);
+        h.cellsIsTriangle.resize(n_cells);
+        for (int c = 0; c < n_cells; ++c) {
+            const int* cn = cell_nodes + 4 * (size_t)c;
+            const bool tri = cn[3] < 0;
+            for (int j = 0; j < (tri ? 3 : 4); ++j)
+                if (cn[j] < 0 || cn[j] >= n_nodes) throw Error(AFX_ERR_MESH, "cell node index out of range");
+            h.cellsNodes[c] = {(uint32_t)cn[0], (uint32_t)cn[1], (uint32_t)cn[2], tri ? 0u : (uint32_t)cn[3]};
+            h.cellsIsTriangle[c] = tri;
+        }
+        for (int b = 0; b < n_bedges; ++b) {
+            const int p = bedge_patch[b];
+            if (p < 0 || p >= (int)names.size()) throw Error(AFX_ERR_MESH, "boundary patch index out of range");
+            if (bedge_nodes[2 * b] < 0 || bedge_nodes[2 * b] >= n_nodes || bedge_nodes[2 * b + 1] < 0 ||
+                bedge_nodes[2 * b + 1] >= n_nodes)
+                throw Error(AFX_ERR_MESH, "boundary node index out of range");
+            h.bnd0.push_back((uint32_t)bedge_nodes[2 * b]);
+            h.bnd1.push_back((uint32_t)bedge_nodes[2 * b + 1]);
+            h.bndName.push_back(names[p]);
+        }
+        h.finalize();
+        *out = m.release();
+    });
+}
+
+int afx_mesh_counts(afx_mesh m, long long counts[5]) {
+    return guarded([&] {
+        if (!m || !counts) throw Error(AFX_ERR_ARG, "null argument");
+        counts[0] = m->m.nRealCells;
+        counts[1] = (long long)m->m.cellsAreas.size();
+        counts[2] = (long long)m->m.edgesCells.size();
+        counts[3] = (long long)m->m.boundaryEdges.size();
+        counts[4] = (long long)m->m.nodesX.size();
+    });
+}
+
+int afx_mesh_get(afx_mesh mp, const char* what, double* out, long long cap, long long* n) {
+    return guarded([&] {
+        if (!mp || !what) throw Error(AFX_ERR_ARG, "null argument");
+        HostMesh& m = mp->m;
+        std::string w(what);
+        const std::vector<double>* v = nullptr;
+        if (w == "cx") v = &m.cellsCentersX;
+        else if (w == "cy") v = &m.cellsCentersY;
+        else if (w == "area") v = &m.cellsAreas;
+        else if (w == "ex") v = &m.edgesCentersX;
+        else if (w == "ey") v = &m.edgesCentersY;
+        else if (w == "nx") v = &m.edgesNormalsX;
+        else if (w == "ny") v = &m.edgesNormalsY;
+        else if (w == "L") v = &m.edgesLengths;
+        else if (w == "wall_dist") v = &m.wall_dist;
+        if (!v) throw Error(AFX_ERR_ARG, "unknown mesh array '" + w + "'");
+        if (n) *n = (long long)v->size();
+        if (out) std::memcpy(out, v->data(), std::min<long long>(cap, (long long)v->size()) * sizeof(double));
+    });
+}
+
+int afx_mesh_get_int(afx_mesh mp, const char* what, long long* out, long long cap, long long* n) {
+    return guarded([&] {
+        if (!mp || !what) throw Error(AFX_ERR_ARG, "null argument");
+        HostMesh& m = mp->m;
+        std::string w(what);
+        std::vector<long long> v;
+        if (w == "edges_cells") {
+            for (auto& e : m.edgesCells) { v.push_back(e[0]); v.push_back(e[1]); }
+        } else if (w == "edges_nodes") {
+            for (auto& e : m.edgesNodes) { v.push_back(e[0]); v.push_back(e[1]); }
+        } else if (w == "boundary_edges") {
+            for (auto e : m.boundaryEdges) v.push_back(e);
+        } else if (w == "cell_order") {
+            for (auto c : mp->layout().cell_old) v.push_back(c);
+        } else {
+            throw Error(AFX_ERR_ARG, "unknown mesh array '" + w + "'");
+        }
+        if (n) *n = (long long)v.size();
+        if (out) std::memcpy(out, v.data(), std::min<long long>(cap, (long long)v.size()) * sizeof(long long));
+    });
+}
+
+int afx_mesh_boundary_name(afx_mesh mp, int b, char* out, int cap) {
+    return guarded([&] {
+        if (!mp || !out || cap <= 0) throw Error(AFX_ERR_ARG, "null argument");
+        const std::string& s = mp->m.boundaryEdgesPhysicals.at(b);
+        std::snprintf(out, cap, "%s", s.c_str());
+    });
+}
+
+void afx_mesh_free(afx_mesh m) { delete m; }
+
+// ---------------------------------------------------------------- config
+int afx_config_create(afx_config* out) {
+    return guarded([&] {
+        if (!out) throw Error(AFX_ERR_ARG, "null argument");
+        *out = new afx_config_s();
+    });
+}
+
+int afx_config_from_ini_string(const char* text, afx_config* out) {
+    return guarded([&] {
+        if (!text || !out) throw Error(AFX_ERR_ARG, "null argument");
+        auto c = std::make_unique<afx_config_s>();
+        import_ini(c->s, text);
+        *out = c.release();
+    });
+}
+
+int afx_config_from_ini(const char* path, afx_config* out) {
+    return guarded([&] {
+        if (!path || !out) throw Error(AFX_ERR_ARG, "null argument");
+        std::ifstream f(path);
+        if (!f) throw Error(AFX_ERR_IO, std::string("Config file: ") + path + " not found");
+        std::stringstream ss;
+        ss << f.rdbuf();
+        auto c = std::make_unique<afx_config_s>();
+        import_ini(c->s, ss.str());
+        *out = c.release();
+    });
+}
+
+static double* dfield(Settings& s, const std::string& k) {
+    if (k == "gamma") return &s.gamma;
+    if (k == "R") return &s.R;
+    if (k == "mu_L") return &s.mu_L;
+    if (k == "Pr_L") return &s.Pr_L;
+    if (k == "Pr_T") return &s.Pr_T;
+    if (k == "start_cfl") return &s.start_cfl;
+    if (k == "slope_cfl") return &s.slope_cfl;
+    if (k == "max_cfl") return &s.max_cfl;
+    if (k == "relaxation") return &s.relaxation;
+    if (k == "tolerance") return &s.tolerance;
+    if (k == "limiter_k") return &s.limiter_k;
+    if (k == "alpha_start") return &s.alpha_start;
+    if (k == "alpha_end") return &s.alpha_end;
+    if (k == "alpha_step") return &s.alpha_step;
+    return nullptr;
+}
+
+int afx_config_set_double(afx_config c, const char* key, double v) {
+    return guarded([&] {
+        if (!c || !key) throw Error(AFX_ERR_ARG, "null argument");
+        std::string k(key);
+        if (k == "rhs_iterations") c->s.rhs_iterations = (int)v;
+        else if (k == "max_iterations") c->s.max_iterations = (int)v;
+        else if (k == "second_order") c->s.second_order = v != 0;
+        else if (double* p = dfield(c->s, k)) *p = v;
+        else throw Error(AFX_ERR_ARG, "unknown numeric setting '" + k + "'");
+    });
+}
+
+int afx_config_get_double(afx_config c, const char* key, double* v) {
+    return guarded([&] {
+        if (!c || !key || !v) throw Error(AFX_ERR_ARG, "null argument");
+        std::string k(key);
+        if (k == "rhs_iterations") *v = c->s.rhs_iterations;
+        else if (k == "max_iterations") *v = c->s.max_iterations;
+        else if (k == "second_order") *v = c->s.second_order ? 1 : 0;
+        else if (double* p = dfield(c->s, k)) *v = *p;
+        else throw Error(AFX_ERR_ARG, "unknown numeric setting '" + k + "'");
+    });
+}
+
+int afx_config_set_string(afx_config c, const char* key, const char* v) {
+    return guarded([&] {
+        if (!c || !key || !v) throw Error(AFX_ERR_ARG, "null argument");
+        std::string k(key), s(v);
+        auto check = [&](std::initializer_list<const char*> ok) {
+            for (auto o : ok)
+                if (s == o) return;
+            throw Error(AFX_ERR_CONFIG, "invalid value '" + s + "' for " + k);
+        };
+        if (k == "solver") { check({"explicit", "implicit"}); c->s.solver = s; }
+        else if (k == "gradient") { check({"green-gauss", "least-squares"}); c->s.gradient = s; }
+        else if (k == "viscosity") {
+            check({"inviscid", "laminar", "spalart-allmaras", "spallart-allmaras"});
+            c->s.viscosity = s;
+        } else if (k == "limiter") { check({"venkatakrishnan", "michalak"}); c->s.limiter = s; }
+        else if (k == "precision") { check({"fp64", "fp32-mixed"}); c->s.precision = s; }
+        else if (k == "airfoil_name") c->s.airfoil_name = s;
+        else throw Error(AFX_ERR_ARG, "unknown string setting '" + k + "'");
+    });
+}
+
+int afx_config_get_string(afx_config c, const char* key, char* out, int cap) {
+    return guarded([&] {
+        if (!c || !key || !out || cap <= 0) throw Error(AFX_ERR_ARG, "null argument");
+        std::string k(key), v;
+        if (k == "solver") v = c->s.solver;
+        else if (k == "gradient") v = c->s.gradient;
+        else if (k == "viscosity") v = c->s.viscosity;
+        else if (k == "limiter") v = c->s.limiter;
+        else if (k == "precision") v = c->s.precision;
+        else if (k == "airfoil_name") v = c->s.airfoil_name;
+        else throw Error(AFX_ERR_ARG, "unknown string setting '" + k + "'");
+        std::snprintf(out, cap, "%s", v.c_str());
+    });
+}
+
+int afx_config_set_bc(afx_config c, const char* name, const char* type, double T, double mach, double angle,
+                      double p) {
+    return guarded([&] {
+        if (!c || !name || !type) throw Error(AFX_ERR_ARG, "null argument");
+        if (!c->s.bcs.count(name)) c->s.bc_order.push_back(name);
+        auto& bc = c->s.bcs[name];
+        bc.type = type;
+        bc.vars = FarfieldVars();
+        if (bc.type == "farfield") bc.vars = FarfieldVars{mach, angle, T, p};
+    });
+}
+
+int afx_config_bc_count(afx_config c, int* n) {
+    return guarded([&] {
+        if (!c || !n) throw Error(AFX_ERR_ARG, "null argument");
+        *n = (int)c->s.bcs.size();
+    });
+}
+
+void afx_config_free(afx_config c) { delete c; }
+
+// ---------------------------------------------------------------- solver
+int afx_solver_create(afx_mesh mp, afx_config cp, afx_solver* out) {
+    return guarded([&] {
+        if (!mp || !cp || !out) throw Error(AFX_ERR_ARG, "null argument");
+        int ndev = 0;
+        if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+            throw Error(AFX_ERR_CUDA, "no CUDA device available");
+        auto s = std::make_unique<afx_solver_s>();
+        s->st = cp->s;
+        if (s->st.viscosity_code() == VISC_SA)
+            throw Error(AFX_ERR_CONFIG, "spalart-allmaras is not available in this build");
+        const DeviceLayout& L = mp->layout();
+        {
+            const HostMesh& m = mp->m;
+            for (size_t b = 0; b < m.boundaryEdges.size(); ++b) {
+                const uint32_t e = m.boundaryEdges[b];
+                s->bedges.push_back({m.boundaryEdgesPhysicals[b], L.cell_new[m.edgesCells[e][0]], m.edgesCentersX[e],
+                                     m.edgesCentersY[e], m.edgesNormalsX[e], m.edgesNormalsY[e], m.edgesLengths[e]});
+            }
+            s->cell_old = L.cell_old;
+        }
+        s->fp64 = s->st.precision != "fp32-mixed";
+        AFX_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+        AFX_CUDA(cudaEventCreate(&s->ev0));
+        AFX_CUDA(cudaEventCreate(&s->ev1));
+        AFX_CUDA(cudaHostAlloc((void**)&s->h_ctrl, sizeof(Ctrl), cudaHostAllocDefault));
+        s->set_bcs();
+        StepArgs& a = s->a;
+        a.n_cells = L.n_cells;
+        a.n_faces = L.n_faces;
+        a.n_bnd = L.n_bnd;
+        const size_t N = L.n_cells, F = L.n_faces, B = L.n_bnd;
+        a.cslot = s->dupload(L.cslot);
+        a.fcell = s->dupload(L.fcell);
+        if (s->fp64) {
+            a.area = s->dupload(L.area);
+            a.fn = s->dupload(L.fn);
+            a.fLg = s->dupload(L.fLg);
+            a.fd0 = s->dupload(L.fd0);
+            a.fd1 = s->dupload(L.fd1);
+            a.ft = s->dupload(L.ft);
+        } else {
+            a.area = s->dupload(cast_vec<float>(L.area));
+            a.fn = s->dupload(cast_vec<float>(L.fn));
+            a.fLg = s->dupload(cast_vec<float>(L.fLg));
+            a.fd0 = s->dupload(cast_vec<float>(L.fd0));
+            a.fd1 = s->dupload(cast_vec<float>(L.fd1));
+            a.ft = s->dupload(cast_vec<float>(L.ft));
+        }
+        const size_t w = s->fp64 ? 8 : 4;
+        a.btype = s->dalloc(std::max<size_t>(B, 1) * sizeof(int));
+        a.bq = s->dalloc(std::max<size_t>(B, 1) * 4 * w);
+        const Settings& st = s->st;
+        a.gamma = st.gamma;
+        a.R = st.R;
+        a.mu = st.mu_L;
+        a.kheat = 1. * st.mu_L / st.Pr_L;  // gas::k(), core.h:43-45
+        a.limiter_k = st.limiter_k;
+        a.cfl = st.start_cfl;
+        a.relax = st.relaxation;
+        const int vc = st.viscosity_code();
+        a.visc = vc == VISC_LAMINAR ? 1 : 0;
+        a.second = st.second_order ? 1 : 0;
+        a.need_grad = (st.second_order || vc != VISC_INVISCID) ? 1 : 0;
+        a.limiter = st.limiter == "michalak" ? 1 : 0;
+        if (st.gradient == "least-squares")
+            throw Error(AFX_ERR_CONFIG, "least-squares gradients are not available in this build");
+        a.face_mode = s->fp64 ? 1 : 0;
+        a.block = N >= 600 * 256 ? 256 : (N >= 300 * 128 ? 128 : 64);
+        for (int p = 0; p < 2; ++p) {
+            a.qm[p] = s->dalloc(N * 32);
+            a.qsh[p] = s->fp64 ? a.qm[p] : s->dalloc(N * 16);
+            a.qs[p] = s->dalloc(N * 4 * w);
+        }
+        a.gx = s->dalloc(N * 4 * w);
+        a.gy = s->dalloc(N * 4 * w);
+        a.phi = s->dalloc(N * 4 * w);
+        a.dt = s->dalloc(N * w);
+        a.Rq = s->dalloc(N * 32);
+        a.fflux = a.face_mode ? s->dalloc(F * 4 * w) : nullptr;
+        a.n_partials = (int)((N + a.block - 1) / a.block);
+        a.partials = (double*)s->dalloc(a.n_partials * sizeof(double));
+        a.ctrl = (Ctrl*)s->dalloc(sizeof(Ctrl));
+        a.hist = (double*)s->dalloc(HIST_CAP * sizeof(double));
+        s->d_cell_old.upload(L.cell_old.data(), N * sizeof(int), s->stream);
+        s->d_stage.alloc(N * 32);
+        AFX_CUDA(cudaHostAlloc((void**)&s->h_stage, N * 32, cudaHostAllocDefault));
+        s->h_stage_bytes = N * 32;
+        s->refill_bcs();
+        AFX_CUDA(cudaStreamSynchronize(s->stream));
+        *out = s.release();
+    });
+}
+
+void afx_solver_free(afx_solver s) { delete s; }
+
+int afx_init_freestream(afx_solver s) {
+    return guarded([&] {
+        if (!s) throw Error(AFX_ERR_ARG, "null argument");
+        double q[4];
+        conservative(s->st, s->freestream(), q);  // init(), solver.h:615-631
+        const size_t N = s->a.n_cells;
+        for (size_t i = 0; i < N; ++i) std::memcpy(s->h_stage + 4 * i, q, 32);
+        AFX_CUDA(cudaMemcpyAsync(s->a.qm[s->parity], s->h_stage, N * 32, cudaMemcpyHostToDevice, s->stream));
+        s->sync_shadow(s->parity);
+        s->refill_bcs();
+    });
+}
+
+int afx_set_state(afx_solver s, const double* q, long long n) {
+    return guarded([&] {
+        if (!s || !q) throw Error(AFX_ERR_ARG, "null argument");
+        const size_t N = s->a.n_cells;
+        if (n != (long long)(4 * N)) throw Error(AFX_ERR_ARG, "state size must be 4*n_real_cells");
+        AFX_CUDA(cudaMemcpyAsync(s->d_stage.p, q, N * 32, cudaMemcpyDefault, s->stream));
+        enqueue_permute_in((int)N, (const int*)s->d_cell_old.p, s->d_stage.p, s->a.qm[s->parity], s->stream);
+        s->sync_shadow(s->parity);
+        AFX_CUDA(cudaStreamSynchronize(s->stream));
+    });
+}
+
+int afx_get_state(afx_solver s, double* q, long long n) {
+    return guarded([&] {
+        if (!s || !q) throw Error(AFX_ERR_ARG, "null argument");
+        const size_t N = s->a.n_cells;
+        if (n != (long long)(4 * N)) throw Error(AFX_ERR_ARG, "state size must be 4*n_real_cells");
+        enqueue_permute_out((int)N, (const int*)s->d_cell_old.p, s->a.qm[s->parity], s->d_stage.p, s->stream);
+        AFX_CUDA(cudaMemcpyAsync(q, s->d_stage.p, N * 32, cudaMemcpyDefault, s->stream));
+        AFX_CUDA(cudaStreamSynchronize(s->stream));
+    });
+}
+
+int afx_residual(afx_solver s, double* R, long long n) {
+    return guarded([&] {
+        if (!s) throw Error(AFX_ERR_ARG, "null argument");
+        const size_t N = s->a.n_cells;
+        if (R && n != (long long)(4 * N)) throw Error(AFX_ERR_ARG, "residual size must be 4*n_real_cells");
+        s->set_ctrl(0, 0, 0);
+        if (s->fp64) enqueue_residual_f64(s->a, s->parity, s->stream);
+        else enqueue_residual_f32(s->a, s->parity, s->stream);
+        s->pending_last = -1;
+        if (R) {
+            enqueue_permute_out((int)N, (const int*)s->d_cell_old.p, s->a.Rq, s->d_stage.p, s->stream);
+            AFX_CUDA(cudaMemcpyAsync(R, s->d_stage.p, N * 32, cudaMemcpyDefault, s->stream));
+        }
+        AFX_CUDA(cudaStreamSynchronize(s->stream));
+        AFX_CUDA(cudaGetLastError());
+    });
+}
+
+int afx_iterate(afx_solver s, int n_iters, double* res_norm) {
+    return guarded([&] {
+        if (!s || n_iters < 0) throw Error(AFX_ERR_ARG, "bad argument");
+        s->set_ctrl(0, n_iters, 0);
+        const int done = s->run(n_iters, 0, 0);
+        AFX_CUDA(cudaGetLastError());
+        if (res_norm) *res_norm = s->h_ctrl->last_norm;
+        if (s->h_ctrl->status == 4) throw Error(AFX_ERR_NONFINITE, "residual norm is not finite");
+        if (done < 0) throw Error(AFX_ERR_STOPPED, "stopped by request");
+    });
+}
+
+int afx_run_to_convergence(afx_solver s, double tol, int max_it, int* iters, double* err) {
+    return guarded([&] {
+        if (!s) throw Error(AFX_ERR_ARG, "null argument");
+        if (tol <= 0) tol = s->st.tolerance;
+        if (max_it <= 0) max_it = s->st.max_iterations;
+        s->materialize_qW();
+        s->set_ctrl(1, max_it, tol);
+        double qf[4];
+        conservative(s->st, s->freestream(), qf);
+        if (s->fp64) enqueue_uniform_f64(s->a, s->parity, qf, s->stream);
+        else enqueue_uniform_f32(s->a, s->parity, qf, s->stream);
+        const int done = s->run(max_it, 1, tol);
+        AFX_CUDA(cudaGetLastError());
+        if (iters) *iters = s->h_ctrl->iter;
+        if (err) *err = s->h_ctrl->err;
+        s->hist.resize(s->h_ctrl->hist_n);
+        if (!s->hist.empty())
+            AFX_CUDA(cudaMemcpy(s->hist.data(), s->a.hist, s->hist.size() * 8, cudaMemcpyDeviceToHost));
+        if (s->h_ctrl->status == 4) throw Error(AFX_ERR_NONFINITE, "residual norm is not finite");
+        if (done < 0) throw Error(AFX_ERR_STOPPED, "stopped by request");
+    });
+}
+
+int afx_residual_history(afx_solver s, double* out, int cap, int* n) {
+    return guarded([&] {
+        if (!s || !n) throw Error(AFX_ERR_ARG, "null argument");
+        *n = (int)s->hist.size();
+        if (out)
+            for (int i = 0; i < *n && i < cap; ++i) out[i] = s->hist[i];
+    });
+}
+
+int afx_forces(afx_solver s, const char* patch, double* cl, double* cd, double* cm, double* cp, int cap, int* n_cp) {
+    return guarded([&] {
+        if (!s || !patch) throw Error(AFX_ERR_ARG, "null argument");
+        auto& pf = s->patches[patch];
+        if (!pf) {
+            pf.reset(new afx_solver_s::PatchForces());
+            std::vector<int> cells;
+            std::vector<double> geo;
+            bool first = true;
+            unsigned n_added = 0;
+            for (const auto& be : s->bedges) {  // post.h:320-338
+                if (be.patch != patch) continue;
+                if (first) {
+                    pf->xmin = pf->xmax = be.ex;
+                    pf->y_moment = be.ey;
+                    first = false;
+                } else {
+                    pf->xmin = std::min(pf->xmin, be.ex);
+                    pf->xmax = std::max(pf->xmax, be.ex);
+                    pf->y_moment += be.ey;
+                }
+                n_added += 1;
+                cells.push_back(be.owner_dev);
+                geo.insert(geo.end(), {be.ex, be.ey, be.nx, be.ny, be.L});
+            }
+            if (n_added == 0) throw Error(AFX_ERR_ARG, std::string("no boundary edges on patch '") + patch + "'");
+            pf->y_moment /= (double)n_added;
+            pf->x_moment = (pf->xmax - pf->xmin) * 0.25 + pf->xmin;
+            pf->n = (int)n_added;
+            pf->cell.upload(cells.data(), cells.size() * sizeof(int), s->stream);
+            pf->geo.upload(geo.data(), geo.size() * 8, s->stream);
+            pf->cp.alloc(n_added * 8);
+            pf->sums.alloc(3 * 8);
+        }
+        const FarfieldVars vf = s->freestream();
+        ForceArgs f;
+        f.n = pf->n;
+        f.cell = (const int*)pf->cell.p;
+        f.geo = (const double*)pf->geo.p;
+        f.xmin = pf->xmin;
+        f.xmax = pf->xmax;
+        f.x_moment = pf->x_moment;
+        f.y_moment = pf->y_moment;
+        f.p_inf = vf.p;
+        f.mach_inf = vf.mach;
+        f.gamma = s->st.gamma;
+        f.q = (const double*)s->a.qm[s->parity];
+        f.cp = (double*)pf->cp.p;
+        f.sums = (double*)pf->sums.p;
+        enqueue_forces(f, s->stream);
+        double sums[3];
+        AFX_CUDA(cudaMemcpyAsync(sums, pf->sums.p, 24, cudaMemcpyDeviceToHost, s->stream));
+        std::vector<double> cph(pf->n);
+        AFX_CUDA(cudaMemcpyAsync(cph.data(), pf->cp.p, pf->n * 8, cudaMemcpyDeviceToHost, s->stream));
+        AFX_CUDA(cudaStreamSynchronize(s->stream));
+        const double fx = sums[0], fy = sums[1], aoa = vf.angle;  // post.h:379-384
+        if (cd) *cd = fx * std::cos(aoa) + fy * std::sin(aoa);
+        if (cl) *cl = -fx * std::sin(aoa) + fy * std::cos(aoa);
+        if (cm) *cm = sums[2];
+        if (n_cp) *n_cp = pf->n;
+        if (cp)
+            for (int i = 0; i < pf->n && i < cap; ++i) cp[i] = cph[i];
+    });
+}
+
+int afx_set_farfield(afx_solver s, const char* patch, double mach, double angle, double T, double p) {
+    return guarded([&] {
+        if (!s || !patch) throw Error(AFX_ERR_ARG, "null argument");
+        auto it = s->st.bcs.find(patch);
+        if (it == s->st.bcs.end() || it->second.type != "farfield")
+            throw Error(AFX_ERR_ARG, std::string("no farfield patch '") + patch + "'");
+        s->materialize_qW();
+        it->second.vars = FarfieldVars{mach, angle, T, p};
+        s->set_bcs();
+        s->refill_bcs();
+    });
+}
+
+int afx_profile_iterations(afx_solver s, int n_iters, double* ms, int* launches, int n_kinds) {
+    return guarded([&] {
+        if (!s || !ms || !launches || n_iters <= 0) throw Error(AFX_ERR_ARG, "bad argument");
+        Prof prof;
+        for (int i = 0; i <= Prof::CAP; ++i) AFX_CUDA(cudaEventCreate(&prof.ev[i]));
+        for (int k = 0; k < n_kinds; ++k) {
+            ms[k] = 0;
+            launches[k] = 0;
+        }
+        s->set_ctrl(0, n_iters, 0);
+        s->a.prof = &prof;
+        try {
+            for (int it = 0; it < n_iters; ++it) {
+                prof.start(s->stream);
+                s->enqueue_iteration(s->parity);
+                AFX_CUDA(cudaStreamSynchronize(s->stream));
+                for (int j = 0; j < prof.n; ++j) {
+                    float t = 0;
+                    AFX_CUDA(cudaEventElapsedTime(&t, prof.ev[j], prof.ev[j + 1]));
+                    if (prof.kid[j] < n_kinds) {
+                        ms[prof.kid[j]] += t;
+                        launches[prof.kid[j]] += 1;
+                    }
+                }
+                s->parity ^= 1;
+            }
+        } catch (...) {
+            s->a.prof = nullptr;
+            throw;
+        }
+        s->a.prof = nullptr;
+        s->pending_last = s->parity ^ 1;
+        for (int i = 0; i <= Prof::CAP; ++i) cudaEventDestroy(prof.ev[i]);
+        s->read_ctrl();
+        if (s->h_ctrl->status == 4) throw Error(AFX_ERR_NONFINITE, "residual norm is not finite");
+    });
+}
+
+const char* afx_kernel_name(int k) {
+    static const char* names[K_COUNT] = {"k_prep", "k_limiter", "k_face_flux", "k_cell_sum", "k_resid_gather",
+                                         "k_control"};
+    return (k >= 0 && k < K_COUNT) ? names[k] : "";
+}
+
+int afx_request_stop(afx_solver s) {
+    if (!s) return AFX_ERR_ARG;
+    s->stop.store(1);
+    return AFX_OK;
+}
+
+int afx_last_device_seconds(afx_solver s, double* sec) {
+    return guarded([&] {
+        if (!s || !sec) throw Error(AFX_ERR_ARG, "null argument");
+        *sec = s->last_sec;
+    });
+}
+
+}  // extern "C"

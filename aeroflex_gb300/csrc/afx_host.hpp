@@ -1,0 +1,100 @@
+// Host-side data of the GB300 rans library: the mesh in AeroFLEX's own
+// numbering (what the C ABI exposes), the settings, and the device layout
+// built from them.
+#pragma once
+
+#include <array>
+#include <cstdint>
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace afx {
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+enum BcType { BC_INTERNAL = 0, BC_FARFIELD = 1, BC_SLIP_WALL = 2, BC_WALL = 3, BC_INLET_OUTLET = 4 };
+enum Viscosity { VISC_INVISCID = 0, VISC_LAMINAR = 1, VISC_SA = 2, VISC_SA_MISSPELLED = 3 };
+
+// boundary_variables (src/rans/include/rans/core.h:61-84)
+struct FarfieldVars {
+    double mach = 0.2, angle = 0., T = 1., p = 1.;
+};
+
+struct BoundaryCondition {
+    std::string type = "farfield";
+    FarfieldVars vars;
+};
+
+// rans::Settings (core.h:166-232) plus this library's precision switch.
+struct Settings {
+    double gamma = 1.4, R = 0.71428571428, mu_L = 1e-5, Pr_L = 0.72, Pr_T = 0.9, cp = 1.;
+    std::map<std::string, BoundaryCondition> bcs;
+    std::vector<std::string> bc_order;  // [rans-bc] order as read
+    std::string solver = "implicit";
+    std::string gradient = "green-gauss";
+    std::string viscosity = "inviscid";
+    std::string limiter = "venkatakrishnan";
+    std::string precision = "fp64";
+    std::string airfoil_name = "wall";
+    bool second_order = true;
+    double start_cfl = 40., slope_cfl = 50., max_cfl = 100.;
+    double relaxation = 0.9, tolerance = 1e-4;
+    int rhs_iterations = 5, max_iterations = 300;
+    double alpha_start = 1.0, alpha_end = 7.0, alpha_step = 3.0;
+    double limiter_k = 5.;
+
+    int viscosity_code() const;
+    static int bc_code(const std::string& t);
+};
+
+void import_ini(Settings& s, const std::string& text);  // core.h:238-272 over tinyconfig
+
+// Conservative freestream state, core.h:73-83.
+void conservative(const Settings& s, const FarfieldVars& v, double out[4]);
+
+// Mesh in the reference's numbering (mesh.h:198-273).  Ghost cells follow
+// the real cells, one per boundary edge.
+struct HostMesh {
+    std::vector<double> nodesX, nodesY;
+    std::vector<std::array<uint32_t, 4>> cellsNodes;
+    std::vector<uint8_t> cellsIsTriangle;
+    std::vector<std::array<uint32_t, 2>> edgesNodes, edgesCells;
+    std::vector<double> edgesLengths, edgesNormalsX, edgesNormalsY, edgesCentersX, edgesCentersY;
+    std::vector<double> cellsAreas, cellsCentersX, cellsCentersY;
+    std::vector<uint32_t> boundaryEdges;
+    std::vector<std::string> boundaryEdgesPhysicals;
+    std::vector<double> wall_dist;
+    uint32_t nRealCells = 0;
+
+    // raw input before finalize()
+    std::vector<uint32_t> bnd0, bnd1;
+    std::vector<std::string> bndName;
+
+    void finalize();  // edges, metrics, ghosts (mesh.h:843-884)
+};
+
+HostMesh load_gmsh(const std::string& path);
+
+// Device numbering of cells and faces, with per-cell face slots sorted by the
+// reference's edge id (so a per-cell sum over its faces adds in the same
+// order as the reference's serial edge loop).
+struct DeviceLayout {
+    int n_cells = 0, n_faces = 0, n_bnd = 0;
+    std::vector<int32_t> cell_old;       // device cell -> reference cell
+    std::vector<int32_t> cell_new;       // reference cell -> device cell
+    std::vector<int32_t> face_edge;      // device face -> reference edge
+    std::vector<int32_t> cslot;          // 4 per device cell, device face ids, -1 pad
+    std::vector<int32_t> fcell;          // 2 per device face: c0, c1 (c1 < 0: boundary -(b+1))
+    std::vector<double> area;            // per device cell
+    std::vector<double> fn, fLg, fd0, fd1, ft;  // 2,2,2,2,4 per face
+    std::vector<int32_t> bface;          // boundary b -> device face
+};
+
+DeviceLayout build_layout(const HostMesh& m);
+
+}  // namespace afx

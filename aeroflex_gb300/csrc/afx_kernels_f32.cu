@@ -1,0 +1,17 @@
+// FP32-mixed path: face fluxes, gradients and limiters in FP32 (FMA allowed),
+// the RK state update, the residual norm and the forces in FP64.  The FP64
+// master state is kept with an FP32 shadow that the flux kernels read.
+#include "afx_kernels_impl.cuh"
+
+namespace afx {
+
+void enqueue_iteration_f32(const StepArgs& a, int p, cudaStream_t s) { dev::iteration<float, float, true>(a, p, s); }
+void enqueue_residual_f32(const StepArgs& a, int p, cudaStream_t s) { dev::residual<float, float>(a, p, s); }
+void enqueue_last_stage_residual_f32(const StepArgs& a, int p, cudaStream_t s) {
+    dev::last_stage_residual<float, float>(a, p, s);
+}
+void enqueue_uniform_f32(const StepArgs& a, int p, const double* qf, cudaStream_t s) {
+    dev::uniform<float, float>(a, p, qf, s);
+}
+
+}  // namespace afx

@@ -1,0 +1,173 @@
+// Launch sequences of one explicit iteration and its helpers, instantiated
+// once per precision (afx_kernels_f64.cu, afx_kernels_f32.cu).
+#pragma once
+
+#include "afx_device.cuh"
+
+namespace afx {
+namespace dev {
+
+template <class T>
+KM<T> make_km(const StepArgs& a) {
+    KM<T> m;
+    m.n_cells = a.n_cells;
+    m.cslot = (const int4*)a.cslot;
+    m.area = (const T*)a.area;
+    m.fcell = (const int2*)a.fcell;
+    m.fn = (const V2<T>*)a.fn;
+    m.fLg = (const V2<T>*)a.fLg;
+    m.fd0 = (const V2<T>*)a.fd0;
+    m.fd1 = (const V2<T>*)a.fd1;
+    m.ft = (const V4<T>*)a.ft;
+    m.btype = (const int*)a.btype;
+    m.bq = (const V4<T>*)a.bq;
+    m.gamma = (T)a.gamma;
+    m.R = (T)a.R;
+    m.mu = (T)a.mu;
+    m.kheat = (T)a.kheat;
+    m.limk = (T)a.limiter_k;
+    m.cfl = (T)a.cfl;
+    m.limiter = a.limiter;
+    return m;
+}
+
+inline int nblocks(int n, int b) { return (n + b - 1) / b; }
+
+inline void mark(const StepArgs& a, int id, cudaStream_t s) {
+    if (a.prof) a.prof->mark(id, s);
+}
+
+template <class T, class S>
+void launch_prep(const StepArgs& a, const KM<T>& m, const V4<S>* q, cudaStream_t s) {
+    const int nb = nblocks(a.n_cells, a.block);
+    V4<T>* gx = (V4<T>*)a.gx;
+    V4<T>* gy = (V4<T>*)a.gy;
+    V4<T>* ph = (V4<T>*)a.phi;
+    T* dt = (T*)a.dt;
+    if (a.second)
+        k_prep<T, S, true, true><<<nb, a.block, 0, s>>>(m, q, gx, gy, ph, dt, a.ctrl);
+    else if (a.need_grad)
+        k_prep<T, S, true, false><<<nb, a.block, 0, s>>>(m, q, gx, gy, ph, dt, a.ctrl);
+    else
+        k_prep<T, S, false, false><<<nb, a.block, 0, s>>>(m, q, gx, gy, ph, dt, a.ctrl);
+    mark(a, K_PREP, s);
+}
+
+template <class T, class S, int VISC, bool SECOND>
+void launch_stage_v(const StepArgs& a, const KM<T>& m, const V4<S>* qk, const V4<S>* qmem,
+                    const StageOut<T, S>& o, cudaStream_t s) {
+    const int nb = nblocks(a.n_cells, a.block);
+    const V4<T>* gx = (const V4<T>*)a.gx;
+    const V4<T>* gy = (const V4<T>*)a.gy;
+    const V4<T>* ph = (const V4<T>*)a.phi;
+    if (a.face_mode) {
+        const int nbf = nblocks(a.n_faces, a.block);
+        k_face_flux<T, S, VISC, SECOND>
+            <<<nbf, a.block, 0, s>>>(m, a.n_faces, qk, qmem, gx, gy, ph, (V4<T>*)a.fflux, a.ctrl);
+        mark(a, K_FACE_FLUX, s);
+        k_cell_sum<T, S><<<nb, a.block, 0, s>>>(m, (const V4<T>*)a.fflux, o, a.ctrl);
+        mark(a, K_CELL_SUM, s);
+    } else {
+        k_resid_gather<T, S, VISC, SECOND><<<nb, a.block, 0, s>>>(m, qk, qmem, gx, gy, ph, o, a.ctrl);
+        mark(a, K_RESID_GATHER, s);
+    }
+}
+
+template <class T, class S>
+void launch_stage(const StepArgs& a, const KM<T>& m, const V4<S>* qk, const V4<S>* qmem, const StageOut<T, S>& o,
+                  cudaStream_t s) {
+    if (a.visc == 1) {
+        if (a.second) launch_stage_v<T, S, 1, true>(a, m, qk, qmem, o, s);
+        else launch_stage_v<T, S, 1, false>(a, m, qk, qmem, o, s);
+    } else {
+        if (a.second) launch_stage_v<T, S, 0, true>(a, m, qk, qmem, o, s);
+        else launch_stage_v<T, S, 0, false>(a, m, qk, qmem, o, s);
+    }
+}
+
+template <class T, class S>
+StageOut<T, S> base_out(const StepArgs& a, int p) {
+    StageOut<T, S> o;
+    o.q0 = (const d4*)a.qm[p];
+    o.qnext = nullptr;
+    o.qm_next = nullptr;
+    o.qsh_next = nullptr;
+    o.Rq = (d4*)a.Rq;
+    o.dt = (const T*)a.dt;
+    o.alpha = 1.0;
+    o.relax = a.relax;
+    o.partials = a.partials;
+    o.mode = 0;
+    return o;
+}
+
+// explicitSolver::solve (solver.h:802-828): dt, gradients and first limiter
+// from q; three stages alpha = 1/4, 1/2, 1 with the limiter re-formed from
+// each stage state; the new state goes to parity p^1.
+template <class T, class S, bool SHADOW>
+void iteration(const StepArgs& a, int p, cudaStream_t s) {
+    const KM<T> m = make_km<T>(a);
+    const V4<S>* q = (const V4<S>*)a.qsh[p];
+    launch_prep<T, S>(a, m, q, s);
+    static const double alpha[3] = {0.25, 0.5, 1.0};
+    StageOut<T, S> o = base_out<T, S>(a, p);
+    for (int st = 0; st < 3; ++st) {
+        const V4<S>* qk = st == 0 ? q : (const V4<S>*)a.qs[st - 1];
+        if (st > 0 && a.second) {
+            k_limiter<T, S><<<nblocks(a.n_cells, a.block), a.block, 0, s>>>(
+                m, qk, (const V4<T>*)a.gx, (const V4<T>*)a.gy, (V4<T>*)a.phi, a.ctrl);
+            mark(a, K_LIMITER, s);
+        }
+        o.alpha = alpha[st];
+        if (st < 2) {
+            o.mode = 0;
+            o.qnext = (V4<S>*)a.qs[st];
+        } else {
+            o.mode = 1;
+            o.qnext = nullptr;
+            o.qm_next = (d4*)a.qm[p ^ 1];
+            o.qsh_next = SHADOW ? (V4<S>*)a.qsh[p ^ 1] : nullptr;
+        }
+        launch_stage<T, S>(a, m, qk, q, o, s);
+    }
+    k_control<<<1, 256, 0, s>>>(a.partials, nblocks(a.n_cells, a.block), a.ctrl, a.hist, a.norms, 0);
+    mark(a, K_CONTROL, s);
+}
+
+// Residual of state parity p as the first RK stage forms it -> Rq.
+template <class T, class S>
+void residual(const StepArgs& a, int p, cudaStream_t s) {
+    const KM<T> m = make_km<T>(a);
+    const V4<S>* q = (const V4<S>*)a.qsh[p];
+    launch_prep<T, S>(a, m, q, s);
+    StageOut<T, S> o = base_out<T, S>(a, p);
+    o.mode = 2;
+    launch_stage<T, S>(a, m, q, q, o, s);
+}
+
+// qW of the last stage of the iteration that read parity p (stage state in
+// qs[1], gradients and stage-3 limiter still in place).
+template <class T, class S>
+void last_stage_residual(const StepArgs& a, int p, cudaStream_t s) {
+    const KM<T> m = make_km<T>(a);
+    StageOut<T, S> o = base_out<T, S>(a, p);
+    o.mode = 2;
+    launch_stage<T, S>(a, m, (const V4<S>*)a.qs[1], (const V4<S>*)a.qsh[p], o, s);
+}
+
+template <class T, class S>
+void uniform(const StepArgs& a, int p, const double* qf, cudaStream_t s) {
+    const KM<T> m = make_km<T>(a);
+    const int nb = nblocks(a.n_cells, a.block);
+    const V4<S>* q = (const V4<S>*)a.qsh[p];
+    if (a.visc == 1)
+        k_uniform<T, S, 1><<<nb, a.block, 0, s>>>(m, q, (const V4<T>*)a.gx, (const V4<T>*)a.gy, qf[0], qf[1],
+                                                   qf[2], qf[3], (d4*)a.Rq, a.partials);
+    else
+        k_uniform<T, S, 0><<<nb, a.block, 0, s>>>(m, q, (const V4<T>*)a.gx, (const V4<T>*)a.gy, qf[0], qf[1],
+                                                   qf[2], qf[3], (d4*)a.Rq, a.partials);
+    k_control<<<1, 256, 0, s>>>(a.partials, nb, a.ctrl, a.hist, nullptr, 1);
+}
+
+}  // namespace dev
+}  // namespace afx

@@ -1,0 +1,118 @@
+// Interface between the host orchestrator (afx_solver.cu) and the
+// precision-specific kernel translation units (afx_kernels_f64.cu compiled
+// without FMA contraction for bit parity, afx_kernels_f32.cu for the
+// FP32-mixed path).  Plain pointers only.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace afx {
+
+// Device-resident control block of an iteration run (one per solver).
+struct Ctrl {
+    int done;       // set when the run stopped (converged / max iterations / non-finite)
+    int iter;       // iterations completed in this run
+    int status;     // 0 ok, 4 non-finite
+    int run_mode;   // 0: plain iterate (no stopping), 1: run_solver logic
+    int max_it;
+    int hist_n;
+    int nparts;     // partial sums written by the last stage kernel
+    int pad;
+    double err0;
+    double err;     // last normalised residual (run_mode 1)
+    double tol;
+    double last_norm;  // ‖qW‖₂ of the last stage of the last iteration
+};
+
+constexpr int HIST_CAP = 1 << 16;
+
+// Eager-launch profiler: an event after every kernel of an iteration, so the
+// host can time each kernel on the stream it runs on.
+enum KernelId { K_PREP = 0, K_LIMITER, K_FACE_FLUX, K_CELL_SUM, K_RESID_GATHER, K_CONTROL, K_COUNT };
+struct Prof {
+    static constexpr int CAP = 64;
+    cudaEvent_t ev[CAP + 1];
+    int kid[CAP];
+    int n = 0;
+    void start(cudaStream_t s) {
+        n = 0;
+        cudaEventRecord(ev[0], s);
+    }
+    void mark(int id, cudaStream_t s) {
+        if (n < CAP) {
+            kid[n] = id;
+            cudaEventRecord(ev[n + 1], s);
+            ++n;
+        }
+    }
+};
+
+// Everything a launch needs.  Pointers to typed arrays are passed as void*
+// and cast in the precision's translation unit (T = double or float).
+struct StepArgs {
+    int n_cells = 0, n_faces = 0, n_bnd = 0;
+    // mesh, device layout (afx_host.hpp DeviceLayout), in T
+    const void* cslot = nullptr;  // int4 [N]
+    const void* area = nullptr;   // T [N]
+    const void* fcell = nullptr;  // int2 [F]
+    const void* fn = nullptr;     // T2 [F]
+    const void* fLg = nullptr;    // T2 [F]
+    const void* fd0 = nullptr;    // T2 [F]
+    const void* fd1 = nullptr;    // T2 [F]
+    const void* ft = nullptr;     // T4 [F]
+    const void* btype = nullptr;  // int [B]
+    const void* bq = nullptr;     // T4 [B] ghost (boundary) states
+    // physics / scheme
+    double gamma = 1.4, R = 0.71428571428, mu = 1e-5, kheat = 1e-5 / 0.72;
+    double limiter_k = 5., cfl = 1., relax = 0.9;
+    int visc = 0;         // 0 inviscid, 1 laminar (gradients passed to the flux)
+    int second = 1;       // second-order reconstruction
+    int need_grad = 1;    // gradients computed (second order or viscous model)
+    int limiter = 0;      // 0 Venkatakrishnan, 1 Michalak
+    int face_mode = 1;    // 1: face-flux kernel + ordered cell sum; 0: cell gather recomputing fluxes
+    int block = 256;
+    // state
+    void* qm[2] = {nullptr, nullptr};   // FP64 master state, ping-pong (d4 [N])
+    void* qsh[2] = {nullptr, nullptr};  // state in T (== qm for FP64)
+    void* qs[2] = {nullptr, nullptr};   // RK stage states in T
+    void* gx = nullptr;
+    void* gy = nullptr;
+    void* phi = nullptr;
+    void* dt = nullptr;
+    void* Rq = nullptr;        // d4 [N]: qW mirror (real cells)
+    void* fflux = nullptr;     // d4 or T4 [F]: F*L per face (face mode)
+    double* partials = nullptr;
+    int n_partials = 0;
+    Ctrl* ctrl = nullptr;
+    double* hist = nullptr;    // [HIST_CAP] run_solver history (every 10th)
+    double* norms = nullptr;   // optional per-iteration norms
+    Prof* prof = nullptr;      // eager profiling only (never inside a graph)
+};
+
+// One explicit iteration reading parity p, writing parity p^1.
+void enqueue_iteration_f64(const StepArgs& a, int p, cudaStream_t s);
+void enqueue_iteration_f32(const StepArgs& a, int p, cudaStream_t s);
+// Residual of state parity p with stage-0 semantics -> Rq (qW mirror).
+void enqueue_residual_f64(const StepArgs& a, int p, cudaStream_t s);
+void enqueue_residual_f32(const StepArgs& a, int p, cudaStream_t s);
+// Re-form qW of the last RK stage of the iteration that read parity p.
+void enqueue_last_stage_residual_f64(const StepArgs& a, int p, cudaStream_t s);
+void enqueue_last_stage_residual_f32(const StepArgs& a, int p, cudaStream_t s);
+// get_uniform_residual: qW += freestream face fluxes, ‖qW‖₂ -> ctrl->err0.
+void enqueue_uniform_f64(const StepArgs& a, int p, const double* qfar, cudaStream_t s);
+void enqueue_uniform_f32(const StepArgs& a, int p, const double* qfar, cudaStream_t s);
+
+// Pressure forces over one boundary patch (post.h:301-387).
+struct ForceArgs {
+    int n = 0;
+    const int* cell = nullptr;     // device cell of each patch edge
+    const double* geo = nullptr;   // 5 per edge: ecx, ecy, nx, ny, L
+    double xmin = 0, xmax = 0, x_moment = 0, y_moment = 0;
+    double p_inf = 1, mach_inf = 0.2, gamma = 1.4;
+    const double* q = nullptr;     // FP64 master state (d4)
+    double* cp = nullptr;          // per edge
+    double* sums = nullptr;        // fx, fy, m
+};
+void enqueue_forces(const ForceArgs& f, cudaStream_t s);
+
+}  // namespace afx

@@ -1,0 +1,223 @@
+"""Synthetic mesh generators for the rans residual workloads, plus a gmsh 4.1
+ASCII writer whose output the library's loader (and AeroFLEX's own reader,
+src/rans/include/rans/mesh.h:457-738) parse back into the same cells.
+
+A mesh is a dict of numpy arrays:
+  x, y     node coordinates (float64)
+  cells    (N, 4) int32 node indices, -1 in slot 3 for a triangle
+  bedges   (B, 2) int32 node indices of boundary edges
+  bpatch   (B,)   int32 index into ``names``
+  names    list of boundary patch names
+"""
+import math
+
+import numpy as np
+
+
+def naca4_thickness(x, t):
+    """NACA 4-digit half thickness with the closed trailing edge (-0.1036)."""
+    return 5.0 * t * (0.2969 * np.sqrt(x) - 0.1260 * x - 0.3516 * x ** 2 + 0.2843 * x ** 3 - 0.1036 * x ** 4)
+
+
+def naca4_surface(n_surf, m=0.0, p=0.4, t=0.12):
+    """``n_surf`` distinct surface points, counter-clockwise from the trailing
+    edge over the upper surface, cosine-clustered at both edges."""
+    j = np.arange(n_surf)
+    beta = 2.0 * np.pi * j / n_surf
+    xc = 0.5 * (1.0 + np.cos(beta))
+    yt = naca4_thickness(xc, t)
+    if m > 0.0:
+        yc = np.where(xc < p, m / p ** 2 * (2 * p * xc - xc ** 2),
+                      m / (1 - p) ** 2 * ((1 - 2 * p) + 2 * p * xc - xc ** 2))
+        dyc = np.where(xc < p, 2 * m / p ** 2 * (p - xc), 2 * m / (1 - p) ** 2 * (p - xc))
+    else:
+        yc = np.zeros_like(xc)
+        dyc = np.zeros_like(xc)
+    th = np.arctan(dyc)
+    sgn = np.where(j <= n_surf // 2, 1.0, -1.0)
+    x = xc - sgn * yt * np.sin(th)
+    y = yc + sgn * yt * np.cos(th)
+    # exact closure at the trailing edge and leading edge
+    x[0], y[0] = 1.0, 0.0
+    return x, y
+
+
+def airfoil_omesh(n_surf=128, n_rad=64, r_far=20.0, growth=1.1, m=0.0, p=0.4, t=0.12, split=True):
+    """O-mesh around a NACA 4-digit airfoil of chord 1.
+
+    ``n_surf`` distinct surface nodes, ``n_rad + 1`` node layers whose
+    spacing grows geometrically by ``growth`` out to a circle of radius
+    ``r_far`` chords centred at mid-chord.  Each quad is split into two
+    triangles along a fixed diagonal when ``split``.  Patches: "wall"
+    (airfoil) and "farfield" (outer circle).
+    """
+    sx, sy = naca4_surface(n_surf, m, p, t)
+    ang = 2.0 * np.pi * np.arange(n_surf) / n_surf
+    fx = 0.5 + r_far * np.cos(ang)
+    fy = r_far * np.sin(ang)
+    k = np.arange(n_rad + 1)
+    s = (growth ** k - 1.0) / (growth ** n_rad - 1.0)
+    X = sx[None, :] + (fx - sx)[None, :] * s[:, None]
+    Y = sy[None, :] + (fy - sy)[None, :] * s[:, None]
+    x = X.reshape(-1)
+    y = Y.reshape(-1)
+
+    def nid(kk, jj):
+        return kk * n_surf + (jj % n_surf)
+
+    kk, jj = np.meshgrid(np.arange(n_rad), np.arange(n_surf), indexing="ij")
+    a = nid(kk, jj)
+    b = nid(kk, jj + 1)
+    c = nid(kk + 1, jj + 1)
+    d = nid(kk + 1, jj)
+    if split:
+        t1 = np.stack([a, b, c, np.full_like(a, -1)], -1).reshape(-1, 4)
+        t2 = np.stack([a, c, d, np.full_like(a, -1)], -1).reshape(-1, 4)
+        cells = np.stack([t1, t2], 1).reshape(-1, 4)
+    else:
+        cells = np.stack([a, b, c, d], -1).reshape(-1, 4)
+    js = np.arange(n_surf)
+    wall = np.stack([nid(0, js), nid(0, js + 1)], -1)
+    far = np.stack([nid(n_rad, js), nid(n_rad, js + 1)], -1)
+    bedges = np.concatenate([wall, far]).astype(np.int32)
+    bpatch = np.concatenate([np.zeros(n_surf), np.ones(n_surf)]).astype(np.int32)
+    return dict(x=x, y=y, cells=cells.astype(np.int32), bedges=bedges, bpatch=bpatch, names=["wall", "farfield"])
+
+
+def channel(nx=2048, ny=1024, jitter=0.2, seed=1, shuffle_seed=2):
+    """Unit-square channel triangulated from ``nx`` x ``ny`` quads (2 triangles
+    each).  Interior nodes are jittered by uniform +-``jitter``*h (seed
+    ``seed``) and the cells shuffled (seed ``shuffle_seed``; None keeps the
+    generator order).  Patches: "farfield" (left and right) and "wall"
+    (bottom and top)."""
+    xs = np.linspace(0.0, 1.0, nx + 1)
+    ys = np.linspace(0.0, 1.0, ny + 1)
+    X, Y = np.meshgrid(xs, ys, indexing="ij")  # node (i, j) -> i*(ny+1) + j
+    if jitter:
+        rng = np.random.default_rng(seed)
+        jx = rng.uniform(-jitter, jitter, X.shape) / nx
+        jy = rng.uniform(-jitter, jitter, Y.shape) / ny
+        inner = np.zeros(X.shape, bool)
+        inner[1:-1, 1:-1] = True
+        X = np.where(inner, X + jx, X)
+        Y = np.where(inner, Y + jy, Y)
+    x = X.reshape(-1)
+    y = Y.reshape(-1)
+    ii, jj = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
+    a = ii * (ny + 1) + jj
+    b = (ii + 1) * (ny + 1) + jj
+    c = (ii + 1) * (ny + 1) + jj + 1
+    d = ii * (ny + 1) + jj + 1
+    neg = np.full(a.shape, -1)
+    t1 = np.stack([a, b, c, neg], -1).reshape(-1, 4)
+    t2 = np.stack([a, c, d, neg], -1).reshape(-1, 4)
+    cells = np.stack([t1, t2], 1).reshape(-1, 4).astype(np.int32)
+    if shuffle_seed is not None:
+        perm = np.random.default_rng(shuffle_seed).permutation(len(cells))
+        cells = cells[perm]
+    i = np.arange(nx)
+    j = np.arange(ny)
+    left = np.stack([j, j + 1], -1)
+    right = np.stack([nx * (ny + 1) + j, nx * (ny + 1) + j + 1], -1)
+    bottom = np.stack([i * (ny + 1), (i + 1) * (ny + 1)], -1)
+    top = np.stack([i * (ny + 1) + ny, (i + 1) * (ny + 1) + ny], -1)
+    bedges = np.concatenate([left, right, bottom, top]).astype(np.int32)
+    bpatch = np.concatenate([np.zeros(2 * ny), np.ones(2 * nx)]).astype(np.int32)
+    return dict(x=x, y=y, cells=cells, bedges=bedges, bpatch=bpatch, names=["farfield", "wall"])
+
+
+def cell_centroids(m):
+    """Vertex-mean centroids in the order mesh.h:384-396 forms them."""
+    cells = m["cells"]
+    tri = cells[:, 3] < 0
+    n = np.where(tri, 3.0, 4.0)
+    cx = np.zeros(len(cells))
+    cy = np.zeros(len(cells))
+    for j in range(4):
+        idx = np.where(cells[:, j] >= 0, cells[:, j], 0)
+        use = (j < 3) | ~tri
+        cx = np.where(use, cx + m["x"][idx] / n, cx)
+        cy = np.where(use, cy + m["y"][idx] / n, cy)
+    return cx, cy
+
+
+def density_bump_state(m, mach=0.3, amp=0.05, width=0.1, center=(0.5, 0.5), gamma=1.4, R=0.71428571428):
+    """Uniform freestream at ``mach`` (p = 1, T = 1, angle 0) with the density
+    multiplied by 1 + amp*exp(-|x - center|^2 / width^2) at uniform p and u.
+    Returns the AoS state [rho, rhou, rhov, rhoE] per real cell (N*4)."""
+    cx, cy = cell_centroids(m)
+    c = math.sqrt(gamma * R * 1.0)
+    u = mach * c
+    rho_inf = 1.0 / (R * 1.0)
+    r2 = (cx - center[0]) ** 2 + (cy - center[1]) ** 2
+    rho = rho_inf * (1.0 + amp * np.exp(-r2 / width ** 2))
+    q = np.empty((len(cx), 4))
+    q[:, 0] = rho
+    q[:, 1] = rho * u
+    q[:, 2] = 0.0
+    q[:, 3] = 1.0 / (gamma - 1.0) + 0.5 * rho * u * u
+    return q.reshape(-1)
+
+
+def write_gmsh(path, m):
+    """Write ``m`` as gmsh 4.1 ASCII: one curve entity per boundary patch and
+    element blocks in mesh order, so reading it back reproduces the node,
+    boundary-edge and cell orders of ``m``."""
+    names = list(m["names"])
+    npatch = len(names)
+    x, y = m["x"], m["y"]
+    cells = m["cells"]
+    bedges, bpatch = m["bedges"], m["bpatch"]
+    nn = len(x)
+    out = ["$MeshFormat", "4.1 0 8", "$EndMeshFormat", "$PhysicalNames", str(npatch + 1)]
+    for p, nm in enumerate(names):
+        out.append('1 %d "%s"' % (p + 1, nm))
+    out.append('2 %d "internal"' % (npatch + 1))
+    out += ["$EndPhysicalNames", "$Entities", "0 %d 1 0" % npatch]
+    for p in range(npatch):
+        out.append("%d 0 0 0 0 0 0 1 %d 0 " % (p + 1, p + 1))
+    out.append("1 0 0 0 0 0 0 1 %d 0 " % (npatch + 1))
+    out += ["$EndEntities", "$Nodes", "1 %d 1 %d" % (nn, nn), "2 1 0 %d" % nn]
+    out += [str(i + 1) for i in range(nn)]
+    out += ["%r %r 0" % (float(a), float(b)) for a, b in zip(x, y)]
+    out.append("$EndNodes")
+    # element blocks: boundary runs (consecutive edges of one patch), then cell runs of one type
+    blocks = []
+    start = 0
+    B = len(bedges)
+    while start < B:
+        end = start
+        while end < B and bpatch[end] == bpatch[start]:
+            end += 1
+        blocks.append(("b", int(bpatch[start]), start, end))
+        start = end
+    tri = cells[:, 3] < 0
+    start = 0
+    N = len(cells)
+    while start < N:
+        end = start
+        while end < N and tri[end] == tri[start]:
+            end += 1
+        blocks.append(("c", bool(tri[start]), start, end))
+        start = end
+    total = B + N
+    out += ["$Elements", "%d %d 1 %d" % (len(blocks), total, total)]
+    eid = 1
+    for kind, key, s, e in blocks:
+        if kind == "b":
+            out.append("1 %d 1 %d" % (key + 1, e - s))
+            for k in range(s, e):
+                out.append("%d %d %d " % (eid, bedges[k, 0] + 1, bedges[k, 1] + 1))
+                eid += 1
+        else:
+            out.append("2 1 %d %d" % (2 if key else 3, e - s))
+            for k in range(s, e):
+                c = cells[k]
+                if key:
+                    out.append("%d %d %d %d " % (eid, c[0] + 1, c[1] + 1, c[2] + 1))
+                else:
+                    out.append("%d %d %d %d %d " % (eid, c[0] + 1, c[1] + 1, c[2] + 1, c[3] + 1))
+                eid += 1
+    out.append("$EndElements")
+    with open(path, "w") as f:
+        f.write("\n".join(out) + "\n")

@@ -1,0 +1,289 @@
+"""Python host mirror of AeroFLEX's `rans` interface over the C ABI.
+
+Names follow the reference (src/rans/include/rans/*.h): ``mesh`` (mesh.h),
+``Settings`` (core.h), ``Solver`` (solver.h explicitSolver + multigrid.h
+run_solver) and ``get_wall_profile`` (post.h).  Every call goes through
+libafx_rans.so; there is no Python or CPU fallback — a missing library is
+an ImportError.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libafx_rans.so")
+
+AFX_ERRORS = {1: "IO", 2: "CONFIG", 3: "MESH", 4: "NONFINITE", 5: "DIVERGED", 6: "TIMEOUT", 7: "CUDA", 8: "ARG",
+              9: "STOPPED"}
+
+# Symbols declared in include/afx_rans.h.
+ABI_SYMBOLS = [
+    "afx_last_error", "afx_version", "afx_mesh_load", "afx_mesh_from_arrays", "afx_mesh_counts", "afx_mesh_get",
+    "afx_mesh_get_int", "afx_mesh_boundary_name", "afx_mesh_free", "afx_config_create", "afx_config_from_ini",
+    "afx_config_from_ini_string", "afx_config_set_double", "afx_config_get_double", "afx_config_set_string",
+    "afx_config_get_string", "afx_config_set_bc", "afx_config_bc_count", "afx_config_free", "afx_solver_create",
+    "afx_solver_free", "afx_init_freestream", "afx_set_state", "afx_get_state", "afx_residual", "afx_iterate",
+    "afx_run_to_convergence", "afx_residual_history", "afx_forces", "afx_set_farfield", "afx_request_stop",
+    "afx_last_device_seconds", "afx_profile_iterations", "afx_kernel_name",
+]
+N_KERNEL_KINDS = 6
+
+
+class AfxError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("AFX_ERR_%s: %s" % (AFX_ERRORS.get(code, code), msg))
+        self.code = code
+
+
+_lib = None
+
+
+def lib():
+    """Load libafx_rans.so (built by __graft_entry__.build() / aeroflex_gb300.build)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("libafx_rans.so is not built (run `python -m aeroflex_gb300.build`)")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, cp, i, d, ll = ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_double, ctypes.c_longlong
+    P = ctypes.POINTER
+    sig = {
+        "afx_last_error": (cp, []),
+        "afx_version": (cp, []),
+        "afx_mesh_load": (i, [cp, P(vp)]),
+        "afx_mesh_from_arrays": (i, [i, vp, vp, i, vp, i, vp, vp, cp, P(vp)]),
+        "afx_mesh_counts": (i, [vp, vp]),
+        "afx_mesh_get": (i, [vp, cp, vp, ll, P(ll)]),
+        "afx_mesh_get_int": (i, [vp, cp, vp, ll, P(ll)]),
+        "afx_mesh_boundary_name": (i, [vp, i, ctypes.c_char_p, i]),
+        "afx_mesh_free": (None, [vp]),
+        "afx_config_create": (i, [P(vp)]),
+        "afx_config_from_ini": (i, [cp, P(vp)]),
+        "afx_config_from_ini_string": (i, [cp, P(vp)]),
+        "afx_config_set_double": (i, [vp, cp, d]),
+        "afx_config_get_double": (i, [vp, cp, P(d)]),
+        "afx_config_set_string": (i, [vp, cp, cp]),
+        "afx_config_get_string": (i, [vp, cp, ctypes.c_char_p, i]),
+        "afx_config_set_bc": (i, [vp, cp, cp, d, d, d, d]),
+        "afx_config_bc_count": (i, [vp, P(i)]),
+        "afx_config_free": (None, [vp]),
+        "afx_solver_create": (i, [vp, vp, P(vp)]),
+        "afx_solver_free": (None, [vp]),
+        "afx_init_freestream": (i, [vp]),
+        "afx_set_state": (i, [vp, vp, ll]),
+        "afx_get_state": (i, [vp, vp, ll]),
+        "afx_residual": (i, [vp, vp, ll]),
+        "afx_iterate": (i, [vp, i, P(d)]),
+        "afx_run_to_convergence": (i, [vp, d, i, P(i), P(d)]),
+        "afx_residual_history": (i, [vp, vp, i, P(i)]),
+        "afx_forces": (i, [vp, cp, P(d), P(d), P(d), vp, i, P(i)]),
+        "afx_set_farfield": (i, [vp, cp, d, d, d, d]),
+        "afx_request_stop": (i, [vp]),
+        "afx_last_device_seconds": (i, [vp, P(d)]),
+        "afx_profile_iterations": (i, [vp, i, vp, vp, i]),
+        "afx_kernel_name": (cp, [i]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != 0:
+        raise AfxError(rc, lib().afx_last_error().decode())
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class mesh:
+    """`rans::mesh` (mesh.h:198-273): gmsh 4.1 file or generator arrays."""
+
+    def __init__(self, filename=None, arrays=None):
+        h = ctypes.c_void_p()
+        if filename is not None:
+            _check(lib().afx_mesh_load(str(filename).encode(), ctypes.byref(h)))
+        else:
+            m = arrays
+            x = np.ascontiguousarray(m["x"], np.float64)
+            y = np.ascontiguousarray(m["y"], np.float64)
+            cells = np.ascontiguousarray(m["cells"], np.int32)
+            be = np.ascontiguousarray(m["bedges"], np.int32)
+            bp = np.ascontiguousarray(m["bpatch"], np.int32)
+            _check(lib().afx_mesh_from_arrays(len(x), _ptr(x), _ptr(y), len(cells), _ptr(cells), len(be), _ptr(be),
+                                              _ptr(bp), "\n".join(m["names"]).encode(), ctypes.byref(h)))
+        self.h = h
+        c = np.zeros(5, np.int64)
+        _check(lib().afx_mesh_counts(self.h, _ptr(c)))
+        self.nRealCells, self.n_tot, self.n_edges, self.n_boundary, self.n_nodes = (int(v) for v in c)
+
+    @classmethod
+    def from_arrays(cls, m):
+        return cls(arrays=m)
+
+    def get(self, what):
+        n = ctypes.c_longlong()
+        _check(lib().afx_mesh_get(self.h, what.encode(), None, 0, ctypes.byref(n)))
+        out = np.empty(n.value, np.float64)
+        _check(lib().afx_mesh_get(self.h, what.encode(), _ptr(out), n.value, ctypes.byref(n)))
+        return out
+
+    def get_int(self, what):
+        n = ctypes.c_longlong()
+        _check(lib().afx_mesh_get_int(self.h, what.encode(), None, 0, ctypes.byref(n)))
+        out = np.empty(n.value, np.int64)
+        _check(lib().afx_mesh_get_int(self.h, what.encode(), _ptr(out), n.value, ctypes.byref(n)))
+        return out
+
+    def boundary_names(self):
+        buf = ctypes.create_string_buffer(256)
+        out = []
+        for b in range(self.n_boundary):
+            _check(lib().afx_mesh_boundary_name(self.h, b, buf, 256))
+            out.append(buf.value.decode())
+        return out
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.afx_mesh_free(self.h)
+            self.h = None
+
+
+class Settings:
+    """`rans::Settings` (core.h:166-232); ``from_ini`` = import_config_file."""
+
+    def __init__(self, handle=None):
+        if handle is None:
+            handle = ctypes.c_void_p()
+            _check(lib().afx_config_create(ctypes.byref(handle)))
+        self.h = handle
+
+    @classmethod
+    def from_ini(cls, path):
+        h = ctypes.c_void_p()
+        _check(lib().afx_config_from_ini(str(path).encode(), ctypes.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def from_ini_string(cls, text):
+        h = ctypes.c_void_p()
+        _check(lib().afx_config_from_ini_string(text.encode(), ctypes.byref(h)))
+        return cls(h)
+
+    def set(self, key, value):
+        if isinstance(value, str):
+            _check(lib().afx_config_set_string(self.h, key.encode(), value.encode()))
+        else:
+            _check(lib().afx_config_set_double(self.h, key.encode(), float(value)))
+        return self
+
+    def get(self, key):
+        v = ctypes.c_double()
+        rc = lib().afx_config_get_double(self.h, key.encode(), ctypes.byref(v))
+        if rc == 0:
+            return v.value
+        buf = ctypes.create_string_buffer(256)
+        _check(lib().afx_config_get_string(self.h, key.encode(), buf, 256))
+        return buf.value.decode()
+
+    def set_bc(self, name, type, T=1.0, mach=0.2, angle=0.0, p=1.0):
+        _check(lib().afx_config_set_bc(self.h, name.encode(), type.encode(), T, mach, angle, p))
+        return self
+
+    def bc_count(self):
+        n = ctypes.c_int()
+        _check(lib().afx_config_bc_count(self.h, ctypes.byref(n)))
+        return n.value
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.afx_config_free(self.h)
+            self.h = None
+
+
+class Solver:
+    """Explicit solver on the GPU: `explicitSolver` (solver.h:721-828) +
+    `multigrid<explicitSolver>::run_solver` (multigrid.h:182-237)."""
+
+    def __init__(self, m, settings):
+        h = ctypes.c_void_p()
+        _check(lib().afx_solver_create(m.h, settings.h, ctypes.byref(h)))
+        self.h = h
+        self.n_real = m.nRealCells
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.afx_solver_free(self.h)
+            self.h = None
+
+    def init(self):
+        _check(lib().afx_init_freestream(self.h))
+
+    def set_q(self, q):
+        q = np.ascontiguousarray(q, np.float64).reshape(-1)
+        _check(lib().afx_set_state(self.h, _ptr(q), q.size))
+
+    def get_q(self, out=None):
+        if out is None:
+            out = np.empty(4 * self.n_real, np.float64)
+        _check(lib().afx_get_state(self.h, _ptr(out), out.size))
+        return out
+
+    def residual(self):
+        R = np.empty(4 * self.n_real, np.float64)
+        _check(lib().afx_residual(self.h, _ptr(R), R.size))
+        return R
+
+    def iterate(self, n):
+        r = ctypes.c_double()
+        _check(lib().afx_iterate(self.h, int(n), ctypes.byref(r)))
+        return r.value
+
+    def run_solver(self, tol=0.0, max_it=0):
+        it = ctypes.c_int()
+        err = ctypes.c_double()
+        _check(lib().afx_run_to_convergence(self.h, tol, max_it, ctypes.byref(it), ctypes.byref(err)))
+        return it.value, err.value
+
+    def history(self):
+        n = ctypes.c_int()
+        _check(lib().afx_residual_history(self.h, None, 0, ctypes.byref(n)))
+        out = np.empty(n.value, np.float64)
+        _check(lib().afx_residual_history(self.h, _ptr(out), n.value, ctypes.byref(n)))
+        return out
+
+    def set_farfield(self, patch, mach, angle, T=1.0, p=1.0):
+        _check(lib().afx_set_farfield(self.h, patch.encode(), mach, angle, T, p))
+
+    def request_stop(self):
+        _check(lib().afx_request_stop(self.h))
+
+    def last_device_seconds(self):
+        s = ctypes.c_double()
+        _check(lib().afx_last_device_seconds(self.h, ctypes.byref(s)))
+        return s.value
+
+    def profile_iterations(self, n):
+        """Per-kernel device time (CUDA events on the solver's stream) over n
+        eager iterations: {kernel name: (total ms, launches)}."""
+        ms = np.zeros(N_KERNEL_KINDS, np.float64)
+        cnt = np.zeros(N_KERNEL_KINDS, np.int32)
+        _check(lib().afx_profile_iterations(self.h, int(n), _ptr(ms), _ptr(cnt), N_KERNEL_KINDS))
+        return {lib().afx_kernel_name(k).decode(): (float(ms[k]), int(cnt[k])) for k in range(N_KERNEL_KINDS)
+                if cnt[k] > 0}
+
+
+def get_wall_profile(s, patch="wall", cap=1 << 20):
+    """`get_wall_profile` (post.h:301-387): dict(cl, cd, cm, cp)."""
+    cl, cd, cm = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    n = ctypes.c_int()
+    cp = np.empty(cap, np.float64)
+    _check(lib().afx_forces(s.h, patch.encode(), ctypes.byref(cl), ctypes.byref(cd), ctypes.byref(cm), _ptr(cp), cap,
+                            ctypes.byref(n)))
+    return dict(cl=cl.value, cd=cd.value, cm=cm.value, cp=cp[: n.value].copy())

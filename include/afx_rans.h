@@ -1,0 +1,144 @@
+/*
+ * afx_rans.h — C ABI of the GB300 rans residual library (libafx_rans.so).
+ *
+ * Drop-in boundary for AeroFLEX's `rans` module (header-only C++ in the
+ * reference: src/rans/include/rans/*.h).  Each entry point names the
+ * reference interface it replaces.  Plain C types only: opaque handles,
+ * pointers and sizes.  State arrays cross the boundary in the reference's
+ * layout: AoS [rho, rhou, rhov, rhoE] per REAL cell, cells in the order the
+ * mesh file (or the arrays) listed them.
+ *
+ * Every function returns an afx_status (0 = ok).  On failure the message is
+ * in afx_last_error() (thread-local).  No C++ exception crosses the ABI.
+ * Handles are not thread-safe individually; distinct handles may be used
+ * from distinct threads.  afx_request_stop() may be called from any thread.
+ */
+#ifndef AFX_RANS_H
+#define AFX_RANS_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    AFX_OK = 0,
+    AFX_ERR_IO = 1,        /* file missing / unreadable */
+    AFX_ERR_CONFIG = 2,    /* bad INI content or setting (tinyconfig/Settings throws) */
+    AFX_ERR_MESH = 3,      /* malformed mesh (mesh.h throws std::invalid_argument) */
+    AFX_ERR_NONFINITE = 4, /* residual norm became NaN/Inf */
+    AFX_ERR_DIVERGED = 5,  /* residual grew past the divergence guard */
+    AFX_ERR_TIMEOUT = 6,   /* a bounded device wait ran out */
+    AFX_ERR_CUDA = 7,      /* CUDA runtime error or no usable GPU */
+    AFX_ERR_ARG = 8,       /* null handle / bad size / unknown name */
+    AFX_ERR_STOPPED = 9    /* afx_request_stop() ended a run early (results are valid) */
+} afx_status;
+
+typedef struct afx_mesh_s* afx_mesh;
+typedef struct afx_config_s* afx_config;
+typedef struct afx_solver_s* afx_solver;
+
+/* Thread-local text of the last error. */
+const char* afx_last_error(void);
+/* Library version string. */
+const char* afx_version(void);
+
+/* ------------------------------------------------------------- mesh ---- */
+/* Replaces rans::mesh::mesh(std::string filename) / read_file
+ * (src/rans/include/rans/mesh.h:250, 834-884): gmsh 4.1 ASCII. */
+int afx_mesh_load(const char* path, afx_mesh* out);
+/* Same mesh built from arrays (the generators' path).  cell_nodes holds 4
+ * node indices per cell, -1 in slot 3 for a triangle; boundary edges are
+ * node pairs with a patch index into patch_names ('\n'-separated). */
+int afx_mesh_from_arrays(int n_nodes, const double* x, const double* y, int n_cells, const int* cell_nodes,
+                         int n_bedges, const int* bedge_nodes, const int* bedge_patch, const char* patch_names,
+                         afx_mesh* out);
+/* counts[0..4] = real cells, cells incl. ghosts, edges, boundary edges, nodes
+ * (mesh.h:209-246 sizes; nRealCells, mesh.h:869). */
+int afx_mesh_counts(afx_mesh m, long long counts[5]);
+/* Copies one FP64 metric in reference order: "cx","cy","area" (all cells incl.
+ * ghosts), "ex","ey","nx","ny","L" (edges), "wall_dist" (cells), mesh.h:378-453. */
+int afx_mesh_get(afx_mesh m, const char* what, double* out, long long cap, long long* n);
+/* Integer topology: "edges_cells" (2/edge), "edges_nodes" (2/edge),
+ * "boundary_edges" (edge id per boundary edge), "cell_order" (device
+ * renumbering: reference cell id of each device cell). */
+int afx_mesh_get_int(afx_mesh m, const char* what, long long* out, long long cap, long long* n);
+/* Physical name of boundary edge b (mesh.h:783-785). */
+int afx_mesh_boundary_name(afx_mesh m, int b, char* out, int cap);
+void afx_mesh_free(afx_mesh m);
+
+/* ----------------------------------------------------------- config ---- */
+/* Replaces rans::Settings defaults (src/rans/include/rans/core.h:166-199). */
+int afx_config_create(afx_config* out);
+/* Replaces Settings::import_config_file(tiny::config&) (core.h:238-272) over
+ * tiny::config::read (libs/headeronly/tinyconfig.hpp:152-221). */
+int afx_config_from_ini(const char* path, afx_config* out);
+int afx_config_from_ini_string(const char* text, afx_config* out);
+/* Numeric fields: gamma, R, mu_L, Pr_L, Pr_T, start_cfl, slope_cfl, max_cfl,
+ * relaxation, tolerance, limiter_k, alpha_start, alpha_end, alpha_step,
+ * rhs_iterations, max_iterations, second_order (0/1). */
+int afx_config_set_double(afx_config c, const char* key, double v);
+int afx_config_get_double(afx_config c, const char* key, double* v);
+/* String fields: solver ("explicit"/"implicit"), gradient ("green-gauss"/
+ * "least-squares"), viscosity ("inviscid"/"laminar"/"spalart-allmaras"/
+ * "spallart-allmaras"), limiter ("venkatakrishnan"/"michalak"),
+ * precision ("fp64"/"fp32-mixed"), airfoil_name. */
+int afx_config_set_string(afx_config c, const char* key, const char* v);
+int afx_config_get_string(afx_config c, const char* key, char* out, int cap);
+/* One [rans-bc] entry (core.h:244-255): type "farfield"/"slip-wall"/"wall". */
+int afx_config_set_bc(afx_config c, const char* name, const char* type, double T, double mach, double angle,
+                      double p);
+int afx_config_bc_count(afx_config c, int* n);
+void afx_config_free(afx_config c);
+
+/* ----------------------------------------------------------- solver ---- */
+/* Replaces explicitSolver(mesh, gas, viscosity) + set_bcs / set_second_order /
+ * set_gradient_scheme / set_limiter_k (solver.h:108, 131-162, 200-247;
+ * multigrid.h:70-77).  Uploads the mesh to the GPU in its device layout. */
+int afx_solver_create(afx_mesh m, afx_config c, afx_solver* out);
+void afx_solver_free(afx_solver s);
+/* init() + refill_bcs() (solver.h:615-631, 259-274). */
+int afx_init_freestream(afx_solver s);
+/* Overwrite the real-cell state (get_q() = ..., solver.h:255) from host
+ * AoS FP64 [4*n_real]; ghost states keep their boundary values. */
+int afx_set_state(afx_solver s, const double* q, long long n);
+int afx_get_state(afx_solver s, double* q, long long n);
+/* Residual of the current state as the first RK stage forms it: ghosts,
+ * Green-Gauss gradient, limiter, face loop, /area (solver.h:745-799).
+ * R gets AoS FP64 [4*n_real]. */
+int afx_residual(afx_solver s, double* R, long long n);
+/* n explicit iterations (explicitSolver::solve, solver.h:802-828); res_norm
+ * gets ‖qW‖₂ of the last stage of the last iteration. */
+int afx_iterate(afx_solver s, int n_iters, double* res_norm);
+/* multigrid<explicitSolver>::run_solver (multigrid.h:182-237): err_0 from
+ * get_uniform_residual (solver.h:636-690), iterate until err <= tolerance,
+ * max_iterations, or afx_request_stop.  tol/max_it <= 0 take the config's. */
+int afx_run_to_convergence(afx_solver s, double tol, int max_it, int* iters, double* err);
+/* Residual history as run_solver stores it (every 10th iteration). */
+int afx_residual_history(afx_solver s, double* out, int cap, int* n);
+/* get_wall_profile(solver&, patch) (src/rans/include/rans/post.h:301-387):
+ * pressure C_L, C_D, C_M and cp per patch edge (cap entries at most). */
+int afx_forces(afx_solver s, const char* patch, double* cl, double* cd, double* cm, double* cp, int cap,
+               int* n_cp);
+/* settings.bcs[patch].vars_far = {...}; set_bcs(...) (rans.h:92-97). */
+int afx_set_farfield(afx_solver s, const char* patch, double mach, double angle, double T, double p);
+/* Atomic stop flag polled between device launch groups (GUIHandler::signal.stop,
+ * src/common/common_aeroflex.hpp:11-19; multigrid.h:234). */
+int afx_request_stop(afx_solver s);
+/* Seconds of device time spent by the last afx_iterate/afx_run_to_convergence. */
+int afx_last_device_seconds(afx_solver s, double* sec);
+
+/* Measurement hooks (no counterpart in the reference, which has no
+ * profiling): n iterations launched eagerly with a CUDA event after every
+ * kernel on the solver's stream; ms[k] and launches[k] accumulate per kernel
+ * kind k < n_kinds, named by afx_kernel_name(k).  The state advances by n
+ * iterations exactly as afx_iterate would. */
+int afx_profile_iterations(afx_solver s, int n_iters, double* ms, int* launches, int n_kinds);
+const char* afx_kernel_name(int k);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* AFX_RANS_H */

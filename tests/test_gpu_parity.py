@@ -1,0 +1,159 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU oracle on the
+same seeded inputs.
+
+FP64: bit-exact (every face flux, gradient, limiter and time step is formed
+with the reference's operand order, and per-cell sums visit faces in the
+reference's edge order).  Residual norms are sums in a different order:
+relative 1e-12.  Forces use a tree reduction: relative 1e-12.
+FP32-mixed: tolerances stated per test.
+"""
+import numpy as np
+import pytest
+
+from tests.cases import channel_case, gpu_solver, omesh_case, oracle_solver, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _warm_state(orc, m, bcs, n, **st):
+    s = oracle_solver(orc, m, bcs, **st)
+    s.init()
+    s.iterate(n)
+    return s
+
+
+@pytest.mark.parametrize("variant", [
+    dict(),
+    dict(second_order=False),
+    dict(limiter="michalak"),
+    dict(viscosity="laminar"),
+    dict(viscosity="laminar", second_order=False),
+    dict(viscosity="spallart-allmaras"),
+])
+def test_residual_bitexact_omesh(afx, orc, variant):
+    m, bcs = omesh_case(48, 24)
+    so = _warm_state(orc, m, bcs, 15, **variant)
+    q = so.q()
+    Ro = so.residual()
+    g = gpu_solver(afx, m, bcs, **variant)
+    g.init()
+    g.set_q(q)
+    Rg = g.residual()
+    assert np.isfinite(Rg).all()
+    np.testing.assert_array_equal(Rg, Ro)
+
+
+def test_residual_bitexact_shuffled_channel(afx, orc):
+    m, bcs, q = channel_case(64, 32)
+    so = oracle_solver(orc, m, bcs)
+    so.init()
+    so.set_q(q)
+    Ro = so.residual()
+    g = gpu_solver(afx, m, bcs)
+    g.init()
+    g.set_q(q)
+    np.testing.assert_array_equal(g.residual(), Ro)
+
+
+@pytest.mark.parametrize("variant", [dict(), dict(viscosity="laminar"), dict(second_order=False)])
+def test_iterations_bitexact(afx, orc, variant):
+    m, bcs = omesh_case(48, 24)
+    so = oracle_solver(orc, m, bcs, **variant)
+    so.init()
+    g = gpu_solver(afx, m, bcs, **variant)
+    g.init()
+    np.testing.assert_array_equal(g.get_q(), so.q())
+    norms = so.iterate(7)
+    r = g.iterate(7)
+    np.testing.assert_array_equal(g.get_q(), so.q())
+    assert abs(r - norms[-1]) <= 1e-12 * norms[-1]
+    # an odd count then an even count exercises both state buffers
+    so.iterate(2)
+    g.iterate(2)
+    np.testing.assert_array_equal(g.get_q(), so.q())
+
+
+def test_large_channel_iterations_bitexact(afx, orc):
+    m, bcs, q = channel_case(256, 128)
+    so = oracle_solver(orc, m, bcs)
+    so.init()
+    so.set_q(q)
+    g = gpu_solver(afx, m, bcs)
+    g.init()
+    g.set_q(q)
+    so.iterate(3)
+    g.iterate(3)
+    np.testing.assert_array_equal(g.get_q(), so.q())
+
+
+def test_run_solver_matches(afx, orc):
+    m, bcs = omesh_case(32, 16)
+    st = dict(tolerance=1e-3, max_iterations=400)
+    so = oracle_solver(orc, m, bcs, **st)
+    so.init()
+    it_o, err_o, hist_o = so.run_solver()
+    g = gpu_solver(afx, m, bcs, **st)
+    g.init()
+    it_g, err_g = g.run_solver()
+    assert it_g == it_o
+    assert abs(err_g - err_o) <= 1e-10 * abs(err_o)
+    np.testing.assert_allclose(g.history(), hist_o, rtol=1e-10)
+    np.testing.assert_array_equal(g.get_q(), so.q())
+    # warm restart at a new angle (rans.h:92-98): err_0 of the second run
+    # includes the previous run's qW (solver.h:643-649)
+    so.set_farfield("farfield", 0.5, 3.0 * 0.01745)
+    g.set_farfield("farfield", 0.5, 3.0 * 0.01745)
+    it_o2, err_o2, _ = so.run_solver()
+    it_g2, err_g2 = g.run_solver()
+    assert it_g2 == it_o2
+    assert abs(err_g2 - err_o2) <= 1e-10 * abs(err_o2)
+    np.testing.assert_array_equal(g.get_q(), so.q())
+
+
+def test_forces_match(afx, orc):
+    m, bcs = omesh_case(48, 24)
+    so = _warm_state(orc, m, bcs, 30)
+    g = gpu_solver(afx, m, bcs)
+    g.init()
+    g.set_q(so.q())
+    wo = so.wall_profile("wall")
+    from aeroflex_gb300.rans import get_wall_profile
+    wg = get_wall_profile(g, "wall")
+    np.testing.assert_array_equal(wg["cp"], wo["cp"])
+    for k in ("cl", "cd", "cm"):
+        assert abs(wg[k] - wo[k]) <= 1e-12 * max(abs(wo[k]), 1e-12), (k, wg[k], wo[k])
+
+
+def test_fp32_mixed_residual_close(afx, orc):
+    m, bcs = omesh_case(48, 24)
+    so = _warm_state(orc, m, bcs, 15)
+    q = so.q()
+    Ro = so.residual()
+    g = gpu_solver(afx, m, bcs, precision="fp32-mixed")
+    g.init()
+    g.set_q(q)
+    Rg = g.residual()
+    # FP32 face fluxes: the residual is a sum of O(1) fluxes cancelling to
+    # O(1e-2), so its relative error is ~1e-7 * |F|/|R|.
+    assert rel_l2(Rg, Ro) < 2e-3
+
+
+def test_fp32_mixed_iterations_track_fp64(afx, orc):
+    m, bcs = omesh_case(48, 24)
+    so = oracle_solver(orc, m, bcs)
+    so.init()
+    so.iterate(50)
+    g = gpu_solver(afx, m, bcs, precision="fp32-mixed")
+    g.init()
+    g.iterate(50)
+    assert rel_l2(g.get_q(), so.q()) < 1e-5
+
+
+def test_nonfinite_flagged(afx):
+    m, bcs = omesh_case(32, 16)
+    g = gpu_solver(afx, m, bcs, cfl=1e6)
+    g.init()
+    from aeroflex_gb300.rans import AfxError
+    with pytest.raises(AfxError) as ei:
+        g.iterate(50)
+    assert ei.value.code == 4
