@@ -106,7 +106,79 @@ struct afx_solver_s {
     };
     std::vector<BoundaryEdge> bedges;
     std::vector<int> cell_old;  // device cell -> reference cell
+    std::vector<int32_t> h_fcell, h_cslot;  // device layout topology, for the tile lists
+    struct TileData {
+        DevBuf hstart, xptr, xlist, ctile;
+        int maxnf = 0;
+    };
+    std::map<int, std::unique_ptr<TileData>> tiles;  // per block size
     bool fp64 = true;
+
+    // Tile lists for `B` cells per tile: faces sorted by their first device
+    // cell make each tile's own faces one contiguous range; a face whose two
+    // cells lie in different tiles is also listed by the later tile.
+    void use_tiles(int B) {
+        auto& td = tiles[B];
+        if (!td) {
+            td.reset(new TileData());
+            const int N = a.n_cells, F = a.n_faces;
+            const int nt = (N + B - 1) / B;
+            std::vector<int> hstart(nt + 1, F), xcount(nt, 0), xidx(F, -1), home(F);
+            for (int f = F - 1; f >= 0; --f) {
+                const int c0 = h_fcell[2 * f], c1 = h_fcell[2 * f + 1];
+                const int hc = c1 >= 0 ? std::min(c0, c1) : c0;
+                home[f] = hc / B;
+                hstart[home[f]] = f;
+            }
+            for (int t = nt - 1; t >= 0; --t)
+                if (hstart[t] > hstart[t + 1]) hstart[t] = hstart[t + 1];
+            for (int f = 0; f < F; ++f) {
+                const int c0 = h_fcell[2 * f], c1 = h_fcell[2 * f + 1];
+                if (c1 < 0) continue;
+                const int t0 = c0 / B, t1 = c1 / B;
+                if (t0 != t1) xidx[f] = xcount[std::max(t0, t1)]++;
+            }
+            std::vector<int> xptr(nt + 1, 0);
+            for (int t = 0; t < nt; ++t) xptr[t + 1] = xptr[t] + xcount[t];
+            std::vector<int> xlist(std::max(xptr[nt], 1));
+            for (int f = 0; f < F; ++f) {
+                if (xidx[f] < 0) continue;
+                const int t = std::max(h_fcell[2 * f] / B, h_fcell[2 * f + 1] / B);
+                xlist[xptr[t] + xidx[f]] = f;
+            }
+            int maxnf = 0;
+            for (int t = 0; t < nt; ++t) maxnf = std::max(maxnf, hstart[t + 1] - hstart[t] + xcount[t]);
+            if (maxnf >= 32767) throw Error(AFX_ERR_MESH, "tile face list too long");
+            std::vector<short> ctile(4 * (size_t)N, 0);
+            for (int i = 0; i < N; ++i) {
+                const int t = i / B;
+                for (int s = 0; s < 4; ++s) {
+                    const int v = h_cslot[4 * (size_t)i + s];
+                    if (v == 0) continue;
+                    const int f = (v > 0 ? v : -v) - 1;
+                    const int lf = home[f] == t ? f - hstart[t] : (hstart[t + 1] - hstart[t]) + xidx[f];
+                    ctile[4 * (size_t)i + s] = (short)(v > 0 ? lf + 1 : -(lf + 1));
+                }
+            }
+            td->hstart.upload(hstart.data(), hstart.size() * sizeof(int), stream);
+            td->xptr.upload(xptr.data(), xptr.size() * sizeof(int), stream);
+            td->xlist.upload(xlist.data(), xlist.size() * sizeof(int), stream);
+            td->ctile.upload(ctile.data(), ctile.size() * sizeof(short), stream);
+            td->maxnf = maxnf;
+            AFX_CUDA(cudaStreamSynchronize(stream));
+        }
+        a.tile_hstart = (const int*)td->hstart.p;
+        a.tile_xptr = (const int*)td->xptr.p;
+        a.tile_xlist = (const int*)td->xlist.p;
+        a.tile_ctile = td->ctile.p;
+        a.tile_maxnf = td->maxnf;
+    }
+
+    void set_launch(int variant, int block) {
+        a.variant = variant;
+        a.block = block;
+        if (variant == 2) use_tiles(block);
+    }
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     StepArgs a;
@@ -240,6 +312,7 @@ struct afx_solver_s {
 
     void materialize_qW() {
         if (pending_last < 0) return;
+        set_ctrl(0, 0, 0);  // the kernels skip their work while ctrl->done is set
         if (fp64) enqueue_last_stage_residual_f64(a, pending_last, stream);
         else enqueue_last_stage_residual_f32(a, pending_last, stream);
         pending_last = -1;
@@ -464,6 +537,12 @@ int afx_config_set_double(afx_config c, const char* key, double v) {
         std::string k(key);
         if (k == "rhs_iterations") c->s.rhs_iterations = (int)v;
         else if (k == "max_iterations") c->s.max_iterations = (int)v;
+        else if (k == "block_size") {
+            const int b = (int)v;
+            if (b != 0 && b != 32 && b != 64 && b != 128 && b != 256)
+                throw Error(AFX_ERR_CONFIG, "block_size must be 0 (auto), 32, 64, 128 or 256");
+            c->s.block_size = b;
+        }
         else if (k == "second_order") c->s.second_order = v != 0;
         else if (double* p = dfield(c->s, k)) *p = v;
         else throw Error(AFX_ERR_ARG, "unknown numeric setting '" + k + "'");
@@ -476,6 +555,7 @@ int afx_config_get_double(afx_config c, const char* key, double* v) {
         std::string k(key);
         if (k == "rhs_iterations") *v = c->s.rhs_iterations;
         else if (k == "max_iterations") *v = c->s.max_iterations;
+        else if (k == "block_size") *v = c->s.block_size;
         else if (k == "second_order") *v = c->s.second_order ? 1 : 0;
         else if (double* p = dfield(c->s, k)) *v = *p;
         else throw Error(AFX_ERR_ARG, "unknown numeric setting '" + k + "'");
@@ -498,6 +578,7 @@ int afx_config_set_string(afx_config c, const char* key, const char* v) {
             c->s.viscosity = s;
         } else if (k == "limiter") { check({"venkatakrishnan", "michalak"}); c->s.limiter = s; }
         else if (k == "precision") { check({"fp64", "fp32-mixed"}); c->s.precision = s; }
+        else if (k == "kernel_variant") { check({"auto", "gather", "face", "tile"}); c->s.kernel_variant = s; }
         else if (k == "airfoil_name") c->s.airfoil_name = s;
         else throw Error(AFX_ERR_ARG, "unknown string setting '" + k + "'");
     });
@@ -512,6 +593,7 @@ int afx_config_get_string(afx_config c, const char* key, char* out, int cap) {
         else if (k == "viscosity") v = c->s.viscosity;
         else if (k == "limiter") v = c->s.limiter;
         else if (k == "precision") v = c->s.precision;
+        else if (k == "kernel_variant") v = c->s.kernel_variant;
         else if (k == "airfoil_name") v = c->s.airfoil_name;
         else throw Error(AFX_ERR_ARG, "unknown string setting '" + k + "'");
         std::snprintf(out, cap, "%s", v.c_str());
@@ -559,6 +641,8 @@ int afx_solver_create(afx_mesh mp, afx_config cp, afx_solver* out) {
                                      m.edgesCentersY[e], m.edgesNormalsX[e], m.edgesNormalsY[e], m.edgesLengths[e]});
             }
             s->cell_old = L.cell_old;
+            s->h_fcell = L.fcell;
+            s->h_cslot = L.cslot;
         }
         s->fp64 = s->st.precision != "fp32-mixed";
         AFX_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
@@ -572,6 +656,7 @@ int afx_solver_create(afx_mesh mp, afx_config cp, afx_solver* out) {
         a.n_bnd = L.n_bnd;
         const size_t N = L.n_cells, F = L.n_faces, B = L.n_bnd;
         a.cslot = s->dupload(L.cslot);
+        a.cnbr = s->dupload(L.cnbr);
         a.fcell = s->dupload(L.fcell);
         if (s->fp64) {
             a.area = s->dupload(L.area);
@@ -606,8 +691,14 @@ int afx_solver_create(afx_mesh mp, afx_config cp, afx_solver* out) {
         a.limiter = st.limiter == "michalak" ? 1 : 0;
         if (st.gradient == "least-squares")
             throw Error(AFX_ERR_CONFIG, "least-squares gradients are not available in this build");
-        a.face_mode = s->fp64 ? 1 : 0;
-        a.block = N >= 600 * 256 ? 256 : (N >= 300 * 128 ? 128 : 64);
+        // defaults from measurement on GB300: the FP64 path is FP64-pipe bound,
+        // so each face flux is formed once; FP32-mixed re-forms fluxes in the
+        // gather.  afx_autotune() times both on the actual mesh.
+        const int variant = st.kernel_variant == "face" ? 1
+                            : st.kernel_variant == "gather" ? 0
+                            : st.kernel_variant == "tile" ? 2
+                                                          : (s->fp64 ? 1 : 0);
+        const int block = st.block_size ? st.block_size : (N >= 600 * 256 ? 256 : (N >= 300 * 128 ? 128 : 64));
         for (int p = 0; p < 2; ++p) {
             a.qm[p] = s->dalloc(N * 32);
             a.qsh[p] = s->fp64 ? a.qm[p] : s->dalloc(N * 16);
@@ -618,12 +709,15 @@ int afx_solver_create(afx_mesh mp, afx_config cp, afx_solver* out) {
         a.phi = s->dalloc(N * 4 * w);
         a.dt = s->dalloc(N * w);
         a.Rq = s->dalloc(N * 32);
-        a.fflux = a.face_mode ? s->dalloc(F * 4 * w) : nullptr;
-        a.n_partials = (int)((N + a.block - 1) / a.block);
+        // face buffers always exist so the autotuner may switch variants
+        a.fflux = s->dalloc(F * 4 * w);
+        a.feL = s->dalloc(F * w);
+        a.n_partials = (int)((N + 31) / 32);  // enough for the smallest block size
         a.partials = (double*)s->dalloc(a.n_partials * sizeof(double));
         a.ctrl = (Ctrl*)s->dalloc(sizeof(Ctrl));
         a.hist = (double*)s->dalloc(HIST_CAP * sizeof(double));
         s->d_cell_old.upload(L.cell_old.data(), N * sizeof(int), s->stream);
+        s->set_launch(variant, block);
         s->d_stage.alloc(N * 32);
         AFX_CUDA(cudaHostAlloc((void**)&s->h_stage, N * 32, cudaHostAllocDefault));
         s->h_stage_bytes = N * 32;
@@ -849,9 +943,70 @@ int afx_profile_iterations(afx_solver s, int n_iters, double* ms, int* launches,
     });
 }
 
+int afx_autotune(afx_solver s, int iters, char* variant, int cap, int* block, double* ms_per_iter) {
+    return guarded([&] {
+        if (!s || iters <= 0) throw Error(AFX_ERR_ARG, "bad argument");
+        StepArgs& a = s->a;
+        const size_t N = a.n_cells;
+        // qW of the last run is formed now: the timing runs overwrite its inputs
+        s->materialize_qW();
+        // keep the state: the timing runs start from it and it is put back after
+        DevBuf save;
+        save.alloc(N * 32);
+        AFX_CUDA(cudaMemcpyAsync(save.p, a.qm[s->parity], N * 32, cudaMemcpyDeviceToDevice, s->stream));
+        const int p0 = s->parity;
+        cudaEvent_t e0, e1;
+        AFX_CUDA(cudaEventCreate(&e0));
+        AFX_CUDA(cudaEventCreate(&e1));
+        double best = 1e300;
+        int best_var = a.variant, best_block = a.block;
+        const int blocks[3] = {64, 128, 256};
+        for (int var = 0; var < 3; ++var) {
+            for (int bi = 0; bi < 3; ++bi) {
+                s->set_launch(var, blocks[bi]);
+                s->set_ctrl(0, 0, 0);
+                AFX_CUDA(cudaMemcpyAsync(a.qm[p0], save.p, N * 32, cudaMemcpyDeviceToDevice, s->stream));
+                s->sync_shadow(p0);
+                int p = p0;
+                s->enqueue_iteration(p);  // warm-up
+                p ^= 1;
+                AFX_CUDA(cudaEventRecord(e0, s->stream));
+                for (int it = 0; it < iters; ++it) {
+                    s->enqueue_iteration(p);
+                    p ^= 1;
+                }
+                AFX_CUDA(cudaEventRecord(e1, s->stream));
+                AFX_CUDA(cudaEventSynchronize(e1));
+                float ms = 0;
+                AFX_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                if (ms < best) {
+                    best = ms;
+                    best_var = var;
+                    best_block = blocks[bi];
+                }
+            }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        s->set_launch(best_var, best_block);
+        for (auto& g : s->graphs) cudaGraphExecDestroy(g.second);
+        s->graphs.clear();
+        AFX_CUDA(cudaMemcpyAsync(a.qm[p0], save.p, N * 32, cudaMemcpyDeviceToDevice, s->stream));
+        s->sync_shadow(p0);
+        s->set_ctrl(0, 0, 0);
+        AFX_CUDA(cudaStreamSynchronize(s->stream));
+        s->parity = p0;
+        s->pending_last = -1;
+        static const char* vnames[3] = {"gather", "face", "tile"};
+        if (variant && cap > 0) std::snprintf(variant, cap, "%s", vnames[best_var]);
+        if (block) *block = best_block;
+        if (ms_per_iter) *ms_per_iter = best / iters;
+    });
+}
+
 const char* afx_kernel_name(int k) {
     static const char* names[K_COUNT] = {"k_prep", "k_limiter", "k_face_flux", "k_cell_sum", "k_resid_gather",
-                                         "k_control"};
+                                         "k_control", "k_resid_tile"};
     return (k >= 0 && k < K_COUNT) ? names[k] : "";
 }
 

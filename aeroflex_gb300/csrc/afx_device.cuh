@@ -92,7 +92,8 @@ template <class T> __device__ __forceinline__ T smax(T a, T b) { return (a < b) 
 template <class T>
 struct KM {
     int n_cells;
-    const int4* __restrict__ cslot;
+    const int4* __restrict__ cslot;  // +(face+1) if the cell is the face's cell 0, -(face+1) if cell 1, 0 empty
+    const int4* __restrict__ cnbr;   // the face's other cell, or -(b+1) for boundary face b
     const T* __restrict__ area;
     const int2* __restrict__ fcell;
     const V2<T>* __restrict__ fn;
@@ -314,507 +315,6 @@ __device__ __forceinline__ T limiter_value(const int kind, const T dqg, const T 
         }
     }
     return sig + (T(1) - sig) * lim;
-}
-
-// ------------------------------------------------------------------ kernels
-
-// Per cell, from the iteration's starting state q (the solver's member q):
-// local time step (solver.h:308-356), Green-Gauss gradient (solver.h:428-469)
-// and, when second order, the first stage's neighbour min/max and limiter
-// (solver.h:517-593).  One gather over the cell's faces in edge order.
-template <class T, class S, bool GRAD, bool SECOND>
-__global__ void __launch_bounds__(256) k_prep(const KM<T> m, const V4<S>* __restrict__ q, V4<T>* __restrict__ gx,
-                                              V4<T>* __restrict__ gy, V4<T>* __restrict__ phi,
-                                              T* __restrict__ dt, const Ctrl* __restrict__ ctrl) {
-    if (ctrl->done) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m.n_cells) return;
-    const int4 sl = __ldg(&m.cslot[i]);
-    const int slots[4] = {sl.x, sl.y, sl.z, sl.w};
-    T qi[4];
-    ld4s(&q[i], qi);
-    T sgx[4] = {T(0), T(0), T(0), T(0)}, sgy[4] = {T(0), T(0), T(0), T(0)};
-    T qmn[4], qmx[4];
-    for (int k = 0; k < 4; ++k) { qmn[k] = qi[k]; qmx[k] = qi[k]; }
-    T eigsum = T(0);
-    for (int s = 0; s < 4; ++s) {
-        const int f = slots[s];
-        if (f < 0) break;
-        const int2 cc = __ldg(&m.fcell[f]);
-        const bool own0 = (cc.x == i);
-        const V2<T> n = __ldg(&m.fn[f]);
-        const V2<T> Lg = __ldg(&m.fLg[f]);
-        T qo[4];
-        int bt = BT_INTERNAL;
-        if (cc.y >= 0) {
-            ld4s(&q[own0 ? cc.y : cc.x], qo);
-        } else {
-            const int b = -cc.y - 1;
-            bt = __ldg(&m.btype[b]);
-            ld4c<T>(&m.bq[b], qo);
-        }
-        const T* q0c = own0 ? qi : qo;  // state of the face's cell 0
-        const T* q1c = own0 ? qo : qi;  // state of the face's cell 1 (ghost: boundary state)
-        // time step
-        T eig;
-        if (two_sided(bt)) {
-            const T eL = face_eig(m.gamma, n.x, n.y, q0c);
-            const T eR = face_eig(m.gamma, n.x, n.y, q1c);
-            eig = smax(eL, eR);
-        } else {
-            eig = face_eig(m.gamma, n.x, n.y, q0c);
-        }
-        eigsum += eig * Lg.x;
-        if (GRAD) {
-            T qRv[4];
-            ghost_state(bt, m.gamma, n.x, n.y, q0c, q1c, qRv);
-            const T g = Lg.y;
-            for (int k = 0; k < 4; ++k) {
-                const T fk = (q0c[k] * (T(1) - g) + qRv[k] * g) * Lg.x;
-                if (own0) {
-                    sgx[k] += fk * n.x;
-                    sgy[k] += fk * n.y;
-                } else {
-                    sgx[k] -= fk * n.x;
-                    sgy[k] -= fk * n.y;
-                }
-            }
-        }
-        if (SECOND && bt != BT_SLIP && bt != BT_WALL) {
-            for (int k = 0; k < 4; ++k) {
-                qmn[k] = smin(qmn[k], qo[k]);
-                qmx[k] = smax(qmx[k], qo[k]);
-            }
-        }
-    }
-    const T A = __ldg(&m.area[i]);
-    dt[i] = m.cfl * A / eigsum;
-    if (!GRAD) return;
-    T gxi[4], gyi[4];
-    for (int k = 0; k < 4; ++k) {
-        gxi[k] = sgx[k] / A;
-        gyi[k] = sgy[k] / A;
-    }
-    V4<T> vx, vy;
-    st4(&vx, gxi);
-    st4(&vy, gyi);
-    gx[i] = vx;
-    gy[i] = vy;
-    if (!SECOND) return;
-    T lim[4] = {T(1), T(1), T(1), T(1)};
-    const T sqrt_area = dsqrt(A);
-    const T Ka = m.limk * sqrt_area;
-    const T K3a = Ka * Ka * Ka;
-    for (int s = 0; s < 4; ++s) {
-        const int f = slots[s];
-        if (f < 0) break;
-        const int2 cc = __ldg(&m.fcell[f]);
-        const V2<T> d = (cc.x == i) ? __ldg(&m.fd0[f]) : __ldg(&m.fd1[f]);
-        for (int k = 0; k < 4; ++k) {
-            const T dqg = gxi[k] * d.x + gyi[k] * d.y;
-            const T dmax = qmx[k] - qi[k];
-            const T dmin = qmn[k] - qi[k];
-            lim[k] = smin(lim[k], limiter_value(m.limiter, dqg, dmax, dmin, K3a));
-        }
-    }
-    V4<T> vp;
-    st4(&vp, lim);
-    phi[i] = vp;
-}
-
-// Limiter of a later RK stage state qk with the iteration's gradients
-// (solver.h:517-593; stages 2 and 3 of solver.h:808-816).
-template <class T, class S>
-__global__ void __launch_bounds__(256) k_limiter(const KM<T> m, const V4<S>* __restrict__ qk,
-                                                 const V4<T>* __restrict__ gx, const V4<T>* __restrict__ gy,
-                                                 V4<T>* __restrict__ phi, const Ctrl* __restrict__ ctrl) {
-    if (ctrl->done) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m.n_cells) return;
-    const int4 sl = __ldg(&m.cslot[i]);
-    const int slots[4] = {sl.x, sl.y, sl.z, sl.w};
-    T qi[4], gxi[4], gyi[4];
-    ld4s(&qk[i], qi);
-    ld4c<T>(&gx[i], gxi);
-    ld4c<T>(&gy[i], gyi);
-    T qmn[4], qmx[4];
-    for (int k = 0; k < 4; ++k) { qmn[k] = qi[k]; qmx[k] = qi[k]; }
-    for (int s = 0; s < 4; ++s) {
-        const int f = slots[s];
-        if (f < 0) break;
-        const int2 cc = __ldg(&m.fcell[f]);
-        T qo[4];
-        if (cc.y >= 0) {
-            ld4s(&qk[cc.x == i ? cc.y : cc.x], qo);
-        } else {
-            const int b = -cc.y - 1;
-            const int bt = __ldg(&m.btype[b]);
-            if (bt == BT_SLIP || bt == BT_WALL) continue;
-            ld4c<T>(&m.bq[b], qo);
-        }
-        for (int k = 0; k < 4; ++k) {
-            qmn[k] = smin(qmn[k], qo[k]);
-            qmx[k] = smax(qmx[k], qo[k]);
-        }
-    }
-    const T A = __ldg(&m.area[i]);
-    T lim[4] = {T(1), T(1), T(1), T(1)};
-    const T sqrt_area = dsqrt(A);
-    const T Ka = m.limk * sqrt_area;
-    const T K3a = Ka * Ka * Ka;
-    for (int s = 0; s < 4; ++s) {
-        const int f = slots[s];
-        if (f < 0) break;
-        const int2 cc = __ldg(&m.fcell[f]);
-        const V2<T> d = (cc.x == i) ? __ldg(&m.fd0[f]) : __ldg(&m.fd1[f]);
-        for (int k = 0; k < 4; ++k) {
-            const T dqg = gxi[k] * d.x + gyi[k] * d.y;
-            lim[k] = smin(lim[k], limiter_value(m.limiter, dqg, qmx[k] - qi[k], qmn[k] - qi[k], K3a));
-        }
-    }
-    V4<T> vp;
-    st4(&vp, lim);
-    phi[i] = vp;
-}
-
-// Second-order reconstruction of one side, solver.h:780-781:
-// q + (gx*dx + gy*dy) .* phi
-template <class T>
-__device__ __forceinline__ void reconstruct(const T* q, const T* gxc, const T* gyc, const T* ph, const V2<T> d,
-                                            T* out) {
-    for (int k = 0; k < 4; ++k) out[k] = q[k] + (gxc[k] * d.x + gyc[k] * d.y) * ph[k];
-}
-
-// average_gradients (solver.h:359-398) for the laminar face flux: member
-// state qa/qb and gradients of the face's two cells, direction from the
-// precomputed sum-of-centroids vector t = (t0, t1, lij).
-template <class T>
-__device__ __forceinline__ void face_gradient(const T* qa, const T* qb, const T* gxa, const T* gya, const T* gxb,
-                                              const T* gyb, const V4<T> t, T* fgx, T* fgy) {
-    const T t0 = t.x, t1 = t.y, lij = t.z;
-    for (int k = 0; k < 4; ++k) {
-        const T grad_dir = (qa[k] - qb[k]) / lij;
-        const T gxb_ = (gxa[k] + gxb[k]) * T(0.5);
-        const T gyb_ = (gya[k] + gyb[k]) * T(0.5);
-        const T grad_dot = gxb_ * t0 + gyb_ * t1;
-        fgx[k] = gxb_ - (grad_dot - grad_dir) * t0;
-        fgy[k] = gyb_ - (grad_dot - grad_dir) * t1;
-    }
-}
-
-// All inputs one face needs, for one side: stage state, gradient, limiter.
-template <class T, class S, bool SECOND>
-__device__ __forceinline__ void side_state(const V4<S>* __restrict__ qk, const V4<T>* __restrict__ gx,
-                                           const V4<T>* __restrict__ gy, const V4<T>* __restrict__ phi,
-                                           const int c, const V2<T> d, T* out) {
-    T qc[4];
-    ld4s(&qk[c], qc);
-    if (!SECOND) {
-        for (int k = 0; k < 4; ++k) out[k] = qc[k];
-        return;
-    }
-    T gxc[4], gyc[4], pc[4];
-    ld4c<T>(&gx[c], gxc);
-    ld4c<T>(&gy[c], gyc);
-    ld4c<T>(&phi[c], pc);
-    reconstruct(qc, gxc, gyc, pc, d, out);
-}
-
-// F*L of face f for stage state qk (solver.h:751-786), returned in fl; the
-// boundary state of a ghost side is used as is (ghost gradient is zero).
-template <class T, class S, int VISC, bool SECOND>
-__device__ __forceinline__ void face_flux_L(const KM<T>& m, const int f, const int2 cc,
-                                            const V4<S>* __restrict__ qk, const V4<S>* __restrict__ qmem,
-                                            const V4<T>* __restrict__ gx, const V4<T>* __restrict__ gy,
-                                            const V4<T>* __restrict__ phi, T* fl, int* btp) {
-    const V2<T> n = __ldg(&m.fn[f]);
-    const V2<T> Lg = __ldg(&m.fLg[f]);
-    T qL[4], qR[4];
-    side_state<T, S, SECOND>(qk, gx, gy, phi, cc.x, __ldg(&m.fd0[f]), qL);
-    int bt = BT_INTERNAL;
-    if (cc.y >= 0) {
-        side_state<T, S, SECOND>(qk, gx, gy, phi, cc.y, __ldg(&m.fd1[f]), qR);
-    } else {
-        const int b = -cc.y - 1;
-        bt = __ldg(&m.btype[b]);
-        ld4c<T>(&m.bq[b], qR);
-    }
-    T fgx[4] = {T(0), T(0), T(0), T(0)}, fgy[4] = {T(0), T(0), T(0), T(0)};
-    if (VISC == 1 && two_sided(bt)) {
-        T qa[4], qb[4], gxa[4], gya[4], gxb[4], gyb[4];
-        ld4s(&qmem[cc.x], qa);
-        ld4c<T>(&gx[cc.x], gxa);
-        ld4c<T>(&gy[cc.x], gya);
-        if (cc.y >= 0) {
-            ld4s(&qmem[cc.y], qb);
-            ld4c<T>(&gx[cc.y], gxb);
-            ld4c<T>(&gy[cc.y], gyb);
-        } else {
-            ld4c<T>(&m.bq[-cc.y - 1], qb);
-            for (int k = 0; k < 4; ++k) { gxb[k] = T(0); gyb[k] = T(0); }
-        }
-        face_gradient(qa, qb, gxa, gya, gxb, gyb, ldv4<T>(&m.ft[f]), fgx, fgy);
-    }
-    T F[4];
-    face_flux<T, VISC>(m, bt, n.x, n.y, qL, qR, fgx, fgy, F);
-    for (int k = 0; k < 4; ++k) fl[k] = F[k] * Lg.x;
-    *btp = bt;
-}
-
-// Per-stage epilogue of one cell: R = sum/area (solver.h:794-798), the RK
-// update qk = q + R*dt*alpha*relaxation (solver.h:818-821) in FP64, and the
-// squared norm of qW (solver.h:827) for the last stage.
-template <class T, class S>
-struct StageOut {
-    const d4* __restrict__ q0;   // FP64 iteration start state (member q)
-    V4<S>* __restrict__ qnext;   // next stage state in S (stages 0, 1)
-    d4* __restrict__ qm_next;    // FP64 new state (stage 2)
-    V4<S>* __restrict__ qsh_next;  // new state in S (stage 2, FP32-mixed shadow), may be null
-    d4* __restrict__ Rq;         // qW mirror (residual-only launches)
-    const T* __restrict__ dt;
-    double alpha, relax;
-    double* __restrict__ partials;
-    int mode;                    // 0 stage 0/1, 1 stage 2 (+norm), 2 residual only (write R)
-};
-
-__device__ __forceinline__ double block_sum(double v, double* sh) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (lane == 0) sh[w] = v;
-    __syncthreads();
-    double t = 0;
-    if (threadIdx.x == 0) {
-        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += sh[k];
-    }
-    return t;
-}
-
-template <class T, class S>
-__device__ __forceinline__ void stage_epilogue(const StageOut<T, S>& o, const int i, const bool active, const T* Rsum,
-                                               const T A, const double extra_sq, double* sh) {
-    double sq = extra_sq;
-    if (active) {
-        T R[4];
-        for (int k = 0; k < 4; ++k) R[k] = Rsum[k] / A;
-        if (o.mode == 2) {
-            double Rd[4] = {(double)R[0], (double)R[1], (double)R[2], (double)R[3]};
-            st4(&o.Rq[i], Rd);
-        } else {
-            double q0[4];
-            ld4(&o.q0[i], q0);
-            const double dti = (double)o.dt[i];
-            double qn[4];
-            for (int k = 0; k < 4; ++k) qn[k] = q0[k] + (double)R[k] * dti * o.alpha * o.relax;
-            if (o.mode == 0) {
-                V4<S> v;
-                st4(&v, qn);
-                o.qnext[i] = v;
-            } else {
-                st4(&o.qm_next[i], qn);
-                if (o.qsh_next) {
-                    V4<S> v;
-                    st4(&v, qn);
-                    o.qsh_next[i] = v;
-                }
-                for (int k = 0; k < 4; ++k) sq += (double)R[k] * (double)R[k];
-            }
-        }
-    }
-    if (o.mode == 1) {
-        const double t = block_sum(sq, sh);
-        if (threadIdx.x == 0) o.partials[blockIdx.x] = t;
-    }
-}
-
-// Cell gather: each cell recomputes the fluxes of its faces (interior faces
-// are evaluated twice, identically) and sums them in edge order.  No face
-// buffer; this is the HBM-lean variant.
-template <class T, class S, int VISC, bool SECOND>
-__global__ void __launch_bounds__(256) k_resid_gather(const KM<T> m, const V4<S>* __restrict__ qk,
-                                                      const V4<S>* __restrict__ qmem,
-                                                      const V4<T>* __restrict__ gx, const V4<T>* __restrict__ gy,
-                                                      const V4<T>* __restrict__ phi, const StageOut<T, S> o,
-                                                      const Ctrl* __restrict__ ctrl) {
-    __shared__ double sh[32];
-    if (ctrl->done) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool active = i < m.n_cells;
-    T Rs[4] = {T(0), T(0), T(0), T(0)};
-    double extra = 0;
-    T A = T(1);
-    if (active) {
-        const int4 sl = __ldg(&m.cslot[i]);
-        const int slots[4] = {sl.x, sl.y, sl.z, sl.w};
-        for (int s = 0; s < 4; ++s) {
-            const int f = slots[s];
-            if (f < 0) break;
-            const int2 cc = __ldg(&m.fcell[f]);
-            T fl[4];
-            int bt;
-            face_flux_L<T, S, VISC, SECOND>(m, f, cc, qk, qmem, gx, gy, phi, fl, &bt);
-            if (cc.x == i) {
-                for (int k = 0; k < 4; ++k) Rs[k] -= fl[k];
-                if (cc.y < 0 && two_sided(bt))
-                    for (int k = 0; k < 4; ++k) extra += (double)fl[k] * (double)fl[k];
-            } else {
-                for (int k = 0; k < 4; ++k) Rs[k] += fl[k];
-            }
-        }
-        A = __ldg(&m.area[i]);
-    }
-    stage_epilogue<T, S>(o, i, active, Rs, A, o.mode == 1 ? extra : 0.0, sh);
-}
-
-// Face variant, part 1: F*L of every face once (FP64 path: the flux is the
-// expensive part on GB300's FP64 pipe, so it is not evaluated twice).
-template <class T, class S, int VISC, bool SECOND>
-__global__ void __launch_bounds__(256) k_face_flux(const KM<T> m, const int n_faces, const V4<S>* __restrict__ qk,
-                                                   const V4<S>* __restrict__ qmem, const V4<T>* __restrict__ gx,
-                                                   const V4<T>* __restrict__ gy, const V4<T>* __restrict__ phi,
-                                                   V4<T>* __restrict__ fflux, const Ctrl* __restrict__ ctrl) {
-    if (ctrl->done) return;
-    const int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= n_faces) return;
-    const int2 cc = __ldg(&m.fcell[f]);
-    T fl[4];
-    int bt;
-    face_flux_L<T, S, VISC, SECOND>(m, f, cc, qk, qmem, gx, gy, phi, fl, &bt);
-    V4<T> v;
-    st4(&v, fl);
-    fflux[f] = v;
-}
-
-// Face variant, part 2: ordered per-cell sum of the face fluxes + epilogue.
-template <class T, class S>
-__global__ void __launch_bounds__(256) k_cell_sum(const KM<T> m, const V4<T>* __restrict__ fflux,
-                                                  const StageOut<T, S> o, const Ctrl* __restrict__ ctrl) {
-    __shared__ double sh[32];
-    if (ctrl->done) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool active = i < m.n_cells;
-    T Rs[4] = {T(0), T(0), T(0), T(0)};
-    double extra = 0;
-    T A = T(1);
-    if (active) {
-        const int4 sl = __ldg(&m.cslot[i]);
-        const int slots[4] = {sl.x, sl.y, sl.z, sl.w};
-        for (int s = 0; s < 4; ++s) {
-            const int f = slots[s];
-            if (f < 0) break;
-            const int2 cc = __ldg(&m.fcell[f]);
-            T fl[4];
-            ld4c<T>(&fflux[f], fl);
-            if (cc.x == i) {
-                for (int k = 0; k < 4; ++k) Rs[k] -= fl[k];
-                if (cc.y < 0 && two_sided(__ldg(&m.btype[-cc.y - 1])))
-                    for (int k = 0; k < 4; ++k) extra += (double)fl[k] * (double)fl[k];
-            } else {
-                for (int k = 0; k < 4; ++k) Rs[k] += fl[k];
-            }
-        }
-        A = __ldg(&m.area[i]);
-    }
-    stage_epilogue<T, S>(o, i, active, Rs, A, o.mode == 1 ? extra : 0.0, sh);
-}
-
-// get_uniform_residual (solver.h:636-690): qW keeps its previous real-cell
-// entries and gains the freestream fluxes (not divided by the area).
-template <class T, class S, int VISC>
-__global__ void __launch_bounds__(256) k_uniform(const KM<T> m, const V4<S>* __restrict__ qmem,
-                                                 const V4<T>* __restrict__ gx, const V4<T>* __restrict__ gy,
-                                                 const double q0, const double q1, const double q2, const double q3,
-                                                 d4* __restrict__ Rq, double* __restrict__ partials) {
-    __shared__ double sh[32];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double sq = 0;
-    if (i < m.n_cells) {
-        const T qf[4] = {(T)q0, (T)q1, (T)q2, (T)q3};
-        double acc[4];
-        ld4(&Rq[i], acc);
-        T accT[4] = {(T)acc[0], (T)acc[1], (T)acc[2], (T)acc[3]};
-        const int4 sl = __ldg(&m.cslot[i]);
-        const int slots[4] = {sl.x, sl.y, sl.z, sl.w};
-        for (int s = 0; s < 4; ++s) {
-            const int f = slots[s];
-            if (f < 0) break;
-            const int2 cc = __ldg(&m.fcell[f]);
-            const V2<T> n = __ldg(&m.fn[f]);
-            const V2<T> Lg = __ldg(&m.fLg[f]);
-            int bt = BT_INTERNAL;
-            if (cc.y < 0) bt = __ldg(&m.btype[-cc.y - 1]);
-            T fgx[4] = {T(0), T(0), T(0), T(0)}, fgy[4] = {T(0), T(0), T(0), T(0)};
-            if (VISC == 1 && two_sided(bt)) {
-                T qa[4], qb[4], gxa[4], gya[4], gxb[4], gyb[4];
-                ld4s(&qmem[cc.x], qa);
-                ld4c<T>(&gx[cc.x], gxa);
-                ld4c<T>(&gy[cc.x], gya);
-                if (cc.y >= 0) {
-                    ld4s(&qmem[cc.y], qb);
-                    ld4c<T>(&gx[cc.y], gxb);
-                    ld4c<T>(&gy[cc.y], gyb);
-                } else {
-                    ld4c<T>(&m.bq[-cc.y - 1], qb);
-                    for (int k = 0; k < 4; ++k) { gxb[k] = T(0); gyb[k] = T(0); }
-                }
-                face_gradient(qa, qb, gxa, gya, gxb, gyb, ldv4<T>(&m.ft[f]), fgx, fgy);
-            }
-            T F[4];
-            face_flux<T, VISC>(m, bt, n.x, n.y, qf, qf, fgx, fgy, F);
-            for (int k = 0; k < 4; ++k) {
-                const T fl = F[k] * Lg.x;
-                if (cc.x == i) {
-                    accT[k] -= fl;
-                    if (cc.y < 0 && two_sided(bt)) sq += (double)fl * (double)fl;
-                } else {
-                    accT[k] += fl;
-                }
-            }
-        }
-        double out[4];
-        for (int k = 0; k < 4; ++k) {
-            out[k] = (double)accT[k];
-            sq += out[k] * out[k];
-        }
-        st4(&Rq[i], out);
-    }
-    const double t = block_sum(sq, sh);
-    if (threadIdx.x == 0) partials[blockIdx.x] = t;
-}
-
-// Residual-norm finalisation and the run_solver control (multigrid.h:195-234)
-// in one block: fixed-order sum of the partials -> ‖qW‖₂, err/err_0,
-// convergence test, history every 10th iteration.
-static __global__ void k_control(const double* __restrict__ partials, int n, Ctrl* ctrl, double* hist, double* norms,
-                          int uniform) {
-    __shared__ double sh[32];
-    if (!uniform && ctrl->done) return;
-    double v = 0;
-    for (int k = threadIdx.x; k < n; k += blockDim.x) v += partials[k];
-    const double t = block_sum(v, sh);
-    if (threadIdx.x != 0) return;
-    const double norm = sqrt(t);
-    if (uniform) {
-        ctrl->err0 = norm;
-        return;
-    }
-    const int i = ctrl->iter;
-    ctrl->last_norm = norm;
-    if (norms) norms[i] = norm;
-    double err = norm;
-    if (!(norm == norm) || norm > 1.7976931348623157e308) {
-        ctrl->status = 4;
-        ctrl->done = 1;
-    }
-    if (ctrl->run_mode) {
-        if (i == 0 && err > 2 * ctrl->err0) ctrl->err0 = err;
-        if (err > 0) err /= ctrl->err0;
-        ctrl->err = err;
-        if (i % 10 == 0 && ctrl->hist_n < HIST_CAP) hist[ctrl->hist_n++] = err;
-        ctrl->iter = i + 1;
-        if (!((err > ctrl->tol) && (i + 1 < ctrl->max_it))) ctrl->done = 1;
-    } else {
-        ctrl->iter = i + 1;
-    }
 }
 
 }  // namespace dev

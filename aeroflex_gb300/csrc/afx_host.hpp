@@ -47,6 +47,10 @@ struct Settings {
     int rhs_iterations = 5, max_iterations = 300;
     double alpha_start = 1.0, alpha_end = 7.0, alpha_step = 3.0;
     double limiter_k = 5.;
+    // device launch configuration (this library only): residual kernel
+    // variant "auto" | "gather" | "face" and threads per block (0 = auto)
+    std::string kernel_variant = "auto";
+    int block_size = 0;
 
     int viscosity_code() const;
     static int bc_code(const std::string& t);
@@ -88,7 +92,8 @@ struct DeviceLayout {
     std::vector<int32_t> cell_old;       // device cell -> reference cell
     std::vector<int32_t> cell_new;       // reference cell -> device cell
     std::vector<int32_t> face_edge;      // device face -> reference edge
-    std::vector<int32_t> cslot;          // 4 per device cell, device face ids, -1 pad
+    std::vector<int32_t> cslot;          // 4 per device cell: +-(device face + 1), 0 pad
+    std::vector<int32_t> cnbr;           // 4 per device cell: other cell or -(b+1)
     std::vector<int32_t> fcell;          // 2 per device face: c0, c1 (c1 < 0: boundary -(b+1))
     std::vector<double> area;            // per device cell
     std::vector<double> fn, fLg, fd0, fd1, ft;  // 2,2,2,2,4 per face

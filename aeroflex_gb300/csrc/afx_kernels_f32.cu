@@ -1,6 +1,9 @@
-// FP32-mixed path: face fluxes, gradients and limiters in FP32 (FMA allowed),
-// the RK state update, the residual norm and the forces in FP64.  The FP64
-// master state is kept with an FP32 shadow that the flux kernels read.
+// FP32-mixed path: face fluxes, gradients and limiters in FP32, the RK state
+// update, the residual norm and the forces in FP64.  The FP64 master state is
+// kept with an FP32 shadow that the flux kernels read.  Compiled with
+// -use_fast_math: FP32 division and square root use the SFU approximations
+// (<= 2 ulp), FMA contraction is on and FP32 denormals flush to zero; the
+// FP64 update and norm in this file are unaffected by those flags.
 #include "afx_kernels_impl.cuh"
 
 namespace afx {

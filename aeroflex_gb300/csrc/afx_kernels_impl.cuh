@@ -2,7 +2,7 @@
 // once per precision (afx_kernels_f64.cu, afx_kernels_f32.cu).
 #pragma once
 
-#include "afx_device.cuh"
+#include "afx_kernels.cuh"
 
 namespace afx {
 namespace dev {
@@ -12,6 +12,7 @@ KM<T> make_km(const StepArgs& a) {
     KM<T> m;
     m.n_cells = a.n_cells;
     m.cslot = (const int4*)a.cslot;
+    m.cnbr = (const int4*)a.cnbr;
     m.area = (const T*)a.area;
     m.fcell = (const int2*)a.fcell;
     m.fn = (const V2<T>*)a.fn;
@@ -44,28 +45,64 @@ void launch_prep(const StepArgs& a, const KM<T>& m, const V4<S>* q, cudaStream_t
     V4<T>* gy = (V4<T>*)a.gy;
     V4<T>* ph = (V4<T>*)a.phi;
     T* dt = (T*)a.dt;
-    if (a.second)
-        k_prep<T, S, true, true><<<nb, a.block, 0, s>>>(m, q, gx, gy, ph, dt, a.ctrl);
-    else if (a.need_grad)
-        k_prep<T, S, true, false><<<nb, a.block, 0, s>>>(m, q, gx, gy, ph, dt, a.ctrl);
-    else
-        k_prep<T, S, false, false><<<nb, a.block, 0, s>>>(m, q, gx, gy, ph, dt, a.ctrl);
+    // the face and tile variants form dt in their first stage (EIG/DT)
+    if (a.variant != 0) {
+        if (a.second)
+            k_prep<T, S, true, true, false><<<nb, a.block, 0, s>>>(m, q, gx, gy, ph, dt, a.ctrl);
+        else if (a.need_grad)
+            k_prep<T, S, true, false, false><<<nb, a.block, 0, s>>>(m, q, gx, gy, ph, dt, a.ctrl);
+        else
+            return;
+    } else {
+        if (a.second)
+            k_prep<T, S, true, true, true><<<nb, a.block, 0, s>>>(m, q, gx, gy, ph, dt, a.ctrl);
+        else if (a.need_grad)
+            k_prep<T, S, true, false, true><<<nb, a.block, 0, s>>>(m, q, gx, gy, ph, dt, a.ctrl);
+        else
+            k_prep<T, S, false, false, true><<<nb, a.block, 0, s>>>(m, q, gx, gy, ph, dt, a.ctrl);
+    }
     mark(a, K_PREP, s);
 }
 
 template <class T, class S, int VISC, bool SECOND>
 void launch_stage_v(const StepArgs& a, const KM<T>& m, const V4<S>* qk, const V4<S>* qmem,
-                    const StageOut<T, S>& o, cudaStream_t s) {
+                    const StageOut<T, S>& o, bool first, cudaStream_t s) {
     const int nb = nblocks(a.n_cells, a.block);
     const V4<T>* gx = (const V4<T>*)a.gx;
     const V4<T>* gy = (const V4<T>*)a.gy;
     const V4<T>* ph = (const V4<T>*)a.phi;
-    if (a.face_mode) {
+    if (a.variant == 2) {
+        TileView tv;
+        tv.hstart = a.tile_hstart;
+        tv.xptr = a.tile_xptr;
+        tv.xlist = a.tile_xlist;
+        tv.ctile = (const short4*)a.tile_ctile;
+        const size_t smem = (size_t)a.tile_maxnf * 5 * sizeof(T);
+        if (first) {
+            if (smem > 48 * 1024)
+                cudaFuncSetAttribute(k_resid_tile<T, S, VISC, SECOND, true>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            k_resid_tile<T, S, VISC, SECOND, true><<<nb, a.block, smem, s>>>(m, tv, qk, qmem, gx, gy, ph, o, a.ctrl);
+        } else {
+            if (smem > 48 * 1024)
+                cudaFuncSetAttribute(k_resid_tile<T, S, VISC, SECOND, false>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            k_resid_tile<T, S, VISC, SECOND, false><<<nb, a.block, smem, s>>>(m, tv, qk, qmem, gx, gy, ph, o, a.ctrl);
+        }
+        mark(a, K_RESID_TILE, s);
+    } else if (a.variant == 1) {
         const int nbf = nblocks(a.n_faces, a.block);
-        k_face_flux<T, S, VISC, SECOND>
-            <<<nbf, a.block, 0, s>>>(m, a.n_faces, qk, qmem, gx, gy, ph, (V4<T>*)a.fflux, a.ctrl);
-        mark(a, K_FACE_FLUX, s);
-        k_cell_sum<T, S><<<nb, a.block, 0, s>>>(m, (const V4<T>*)a.fflux, o, a.ctrl);
+        if (first) {
+            k_face_flux<T, S, VISC, SECOND, true><<<nbf, a.block, 0, s>>>(
+                m, a.n_faces, qk, qmem, gx, gy, ph, (V4<T>*)a.fflux, (T*)a.feL, a.ctrl);
+            mark(a, K_FACE_FLUX, s);
+            k_cell_sum<T, S, true><<<nb, a.block, 0, s>>>(m, (const V4<T>*)a.fflux, (const T*)a.feL, o, a.ctrl);
+        } else {
+            k_face_flux<T, S, VISC, SECOND, false><<<nbf, a.block, 0, s>>>(
+                m, a.n_faces, qk, qmem, gx, gy, ph, (V4<T>*)a.fflux, (T*)a.feL, a.ctrl);
+            mark(a, K_FACE_FLUX, s);
+            k_cell_sum<T, S, false><<<nb, a.block, 0, s>>>(m, (const V4<T>*)a.fflux, (const T*)a.feL, o, a.ctrl);
+        }
         mark(a, K_CELL_SUM, s);
     } else {
         k_resid_gather<T, S, VISC, SECOND><<<nb, a.block, 0, s>>>(m, qk, qmem, gx, gy, ph, o, a.ctrl);
@@ -75,13 +112,13 @@ void launch_stage_v(const StepArgs& a, const KM<T>& m, const V4<S>* qk, const V4
 
 template <class T, class S>
 void launch_stage(const StepArgs& a, const KM<T>& m, const V4<S>* qk, const V4<S>* qmem, const StageOut<T, S>& o,
-                  cudaStream_t s) {
+                  bool first, cudaStream_t s) {
     if (a.visc == 1) {
-        if (a.second) launch_stage_v<T, S, 1, true>(a, m, qk, qmem, o, s);
-        else launch_stage_v<T, S, 1, false>(a, m, qk, qmem, o, s);
+        if (a.second) launch_stage_v<T, S, 1, true>(a, m, qk, qmem, o, first, s);
+        else launch_stage_v<T, S, 1, false>(a, m, qk, qmem, o, first, s);
     } else {
-        if (a.second) launch_stage_v<T, S, 0, true>(a, m, qk, qmem, o, s);
-        else launch_stage_v<T, S, 0, false>(a, m, qk, qmem, o, s);
+        if (a.second) launch_stage_v<T, S, 0, true>(a, m, qk, qmem, o, first, s);
+        else launch_stage_v<T, S, 0, false>(a, m, qk, qmem, o, first, s);
     }
 }
 
@@ -93,7 +130,7 @@ StageOut<T, S> base_out(const StepArgs& a, int p) {
     o.qm_next = nullptr;
     o.qsh_next = nullptr;
     o.Rq = (d4*)a.Rq;
-    o.dt = (const T*)a.dt;
+    o.dt = (T*)a.dt;
     o.alpha = 1.0;
     o.relax = a.relax;
     o.partials = a.partials;
@@ -128,9 +165,9 @@ void iteration(const StepArgs& a, int p, cudaStream_t s) {
             o.qm_next = (d4*)a.qm[p ^ 1];
             o.qsh_next = SHADOW ? (V4<S>*)a.qsh[p ^ 1] : nullptr;
         }
-        launch_stage<T, S>(a, m, qk, q, o, s);
+        launch_stage<T, S>(a, m, qk, q, o, st == 0, s);
     }
-    k_control<<<1, 256, 0, s>>>(a.partials, nblocks(a.n_cells, a.block), a.ctrl, a.hist, a.norms, 0);
+    k_control<<<1, 1024, 0, s>>>(a.partials, nblocks(a.n_cells, a.block), a.ctrl, a.hist, a.norms, 0);
     mark(a, K_CONTROL, s);
 }
 
@@ -142,7 +179,7 @@ void residual(const StepArgs& a, int p, cudaStream_t s) {
     launch_prep<T, S>(a, m, q, s);
     StageOut<T, S> o = base_out<T, S>(a, p);
     o.mode = 2;
-    launch_stage<T, S>(a, m, q, q, o, s);
+    launch_stage<T, S>(a, m, q, q, o, false, s);
 }
 
 // qW of the last stage of the iteration that read parity p (stage state in
@@ -152,7 +189,7 @@ void last_stage_residual(const StepArgs& a, int p, cudaStream_t s) {
     const KM<T> m = make_km<T>(a);
     StageOut<T, S> o = base_out<T, S>(a, p);
     o.mode = 2;
-    launch_stage<T, S>(a, m, (const V4<S>*)a.qs[1], (const V4<S>*)a.qsh[p], o, s);
+    launch_stage<T, S>(a, m, (const V4<S>*)a.qs[1], (const V4<S>*)a.qsh[p], o, false, s);
 }
 
 template <class T, class S>
@@ -166,7 +203,7 @@ void uniform(const StepArgs& a, int p, const double* qf, cudaStream_t s) {
     else
         k_uniform<T, S, 0><<<nb, a.block, 0, s>>>(m, q, (const V4<T>*)a.gx, (const V4<T>*)a.gy, qf[0], qf[1],
                                                    qf[2], qf[3], (d4*)a.Rq, a.partials);
-    k_control<<<1, 256, 0, s>>>(a.partials, nb, a.ctrl, a.hist, nullptr, 1);
+    k_control<<<1, 1024, 0, s>>>(a.partials, nb, a.ctrl, a.hist, nullptr, 1);
 }
 
 }  // namespace dev

@@ -28,7 +28,7 @@ constexpr int HIST_CAP = 1 << 16;
 
 // Eager-launch profiler: an event after every kernel of an iteration, so the
 // host can time each kernel on the stream it runs on.
-enum KernelId { K_PREP = 0, K_LIMITER, K_FACE_FLUX, K_CELL_SUM, K_RESID_GATHER, K_CONTROL, K_COUNT };
+enum KernelId { K_PREP = 0, K_LIMITER, K_FACE_FLUX, K_CELL_SUM, K_RESID_GATHER, K_CONTROL, K_RESID_TILE, K_COUNT };
 struct Prof {
     static constexpr int CAP = 64;
     cudaEvent_t ev[CAP + 1];
@@ -52,7 +52,8 @@ struct Prof {
 struct StepArgs {
     int n_cells = 0, n_faces = 0, n_bnd = 0;
     // mesh, device layout (afx_host.hpp DeviceLayout), in T
-    const void* cslot = nullptr;  // int4 [N]
+    const void* cslot = nullptr;  // int4 [N] signed face slots
+    const void* cnbr = nullptr;   // int4 [N] other cell per slot
     const void* area = nullptr;   // T [N]
     const void* fcell = nullptr;  // int2 [F]
     const void* fn = nullptr;     // T2 [F]
@@ -69,8 +70,16 @@ struct StepArgs {
     int second = 1;       // second-order reconstruction
     int need_grad = 1;    // gradients computed (second order or viscous model)
     int limiter = 0;      // 0 Venkatakrishnan, 1 Michalak
-    int face_mode = 1;    // 1: face-flux kernel + ordered cell sum; 0: cell gather recomputing fluxes
+    // residual kernel: 0 gather (cell gather re-forming fluxes), 1 face (face
+    // kernel + ordered cell sum through HBM), 2 tile (shared-memory face tile)
+    int variant = 1;
     int block = 256;
+    // tile variant data for `block` cells per tile (see TileView)
+    const int* tile_hstart = nullptr;
+    const int* tile_xptr = nullptr;
+    const int* tile_xlist = nullptr;
+    const void* tile_ctile = nullptr;  // short4 [N]
+    int tile_maxnf = 0;
     // state
     void* qm[2] = {nullptr, nullptr};   // FP64 master state, ping-pong (d4 [N])
     void* qsh[2] = {nullptr, nullptr};  // state in T (== qm for FP64)
@@ -81,6 +90,7 @@ struct StepArgs {
     void* dt = nullptr;
     void* Rq = nullptr;        // d4 [N]: qW mirror (real cells)
     void* fflux = nullptr;     // d4 or T4 [F]: F*L per face (face mode)
+    void* feL = nullptr;       // T [F]: spectral radius * length per face (face mode)
     double* partials = nullptr;
     int n_partials = 0;
     Ctrl* ctrl = nullptr;

@@ -462,18 +462,24 @@ DeviceLayout build_layout(const HostMesh& m) {
     std::vector<int> face_of_edge(E);
     for (int f = 0; f < E; ++f) face_of_edge[L.face_edge[f]] = f;
 
-    // per-cell face slots in ascending reference edge id
-    L.cslot.assign(4 * (size_t)N, -1);
+    // per-cell face slots in ascending reference edge id: +(face+1) when the
+    // cell is the face's cell 0, -(face+1) when it is cell 1; the other cell
+    // (device id, or -(b+1) for boundary b) beside it
+    L.cslot.assign(4 * (size_t)N, 0);
+    L.cnbr.assign(4 * (size_t)N, 0);
     std::vector<uint8_t> cnt(N, 0);
     for (int e = 0; e < E; ++e) {
         const uint32_t c0 = m.edgesCells[e][0], c1 = m.edgesCells[e][1];
         const uint32_t cs[2] = {c0, c1};
+        const int other_of_c0 = c1 < (uint32_t)N ? L.cell_new[c1] : -(bnd_of_edge[e] + 1);
         for (int s = 0; s < 2; ++s) {
             if (cs[s] >= (uint32_t)N) continue;
             if (s == 1 && c1 == c0) continue;
             const int nc = L.cell_new[cs[s]];
             if (cnt[nc] >= 4) throw Error(3, "cell " + std::to_string(cs[s]) + " has more than 4 faces");
-            L.cslot[4 * (size_t)nc + cnt[nc]++] = face_of_edge[e];
+            const size_t k = 4 * (size_t)nc + cnt[nc]++;
+            L.cslot[k] = s == 0 ? face_of_edge[e] + 1 : -(face_of_edge[e] + 1);
+            L.cnbr[k] = s == 0 ? other_of_c0 : L.cell_new[c0];
         }
     }
 

@@ -25,9 +25,9 @@ ABI_SYMBOLS = [
     "afx_config_get_string", "afx_config_set_bc", "afx_config_bc_count", "afx_config_free", "afx_solver_create",
     "afx_solver_free", "afx_init_freestream", "afx_set_state", "afx_get_state", "afx_residual", "afx_iterate",
     "afx_run_to_convergence", "afx_residual_history", "afx_forces", "afx_set_farfield", "afx_request_stop",
-    "afx_last_device_seconds", "afx_profile_iterations", "afx_kernel_name",
+    "afx_last_device_seconds", "afx_profile_iterations", "afx_kernel_name", "afx_autotune",
 ]
-N_KERNEL_KINDS = 6
+N_KERNEL_KINDS = 7
 
 
 class AfxError(RuntimeError):
@@ -84,6 +84,7 @@ def lib():
         "afx_last_device_seconds": (i, [vp, P(d)]),
         "afx_profile_iterations": (i, [vp, i, vp, vp, i]),
         "afx_kernel_name": (cp, [i]),
+        "afx_autotune": (i, [vp, i, ctypes.c_char_p, i, P(i), P(d)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -268,6 +269,14 @@ class Solver:
         s = ctypes.c_double()
         _check(lib().afx_last_device_seconds(self.h, ctypes.byref(s)))
         return s.value
+
+    def autotune(self, iters=5):
+        """Pick the fastest residual-kernel variant and block size on this mesh."""
+        buf = ctypes.create_string_buffer(16)
+        blk = ctypes.c_int()
+        ms = ctypes.c_double()
+        _check(lib().afx_autotune(self.h, int(iters), buf, 16, ctypes.byref(blk), ctypes.byref(ms)))
+        return dict(variant=buf.value.decode(), block=blk.value, ms_per_iter=ms.value)
 
     def profile_iterations(self, n):
         """Per-kernel device time (CUDA events on the solver's stream) over n

@@ -117,6 +117,11 @@ def algorithmic_bytes(kernel, n, f, precision):
         # (stage 2 writes the FP64 state + FP32 shadow: counted as the average over the 3 stages)
         writes = (cell_vec + cell_vec + (32 + cell_vec)) / 3.0
         return n * (16 + w + 4 * cell_vec + 32 + w + writes) + f * face_geo
+    if kernel == "k_resid_tile":
+        # faces once (40/72 B records), cell vectors q, gx, gy, phi of every cell once, per-cell tile
+        # slots (8), area, dt, FP64 q0, stage writes; tile lists are < 1% and not counted
+        writes = (cell_vec + cell_vec + (32 + cell_vec)) / 3.0
+        return n * (4 * cell_vec + 8 + w + w + 32 + writes) + f * face_geo
     if kernel == "k_face_flux":
         return n * 4 * cell_vec + f * (face_geo + 4 * w)
     if kernel == "k_cell_sum":
@@ -129,12 +134,28 @@ def algorithmic_bytes(kernel, n, f, precision):
     return 0
 
 
+def run_lean(args):
+    """Warm-up + K iterations and nothing else (the command profiled by ncu)."""
+    from aeroflex_gb300 import meshgen, rans
+
+    marr = meshgen.channel(args.nx, args.ny, jitter=0.2, seed=1, shuffle_seed=2)
+    q0 = meshgen.density_bump_state(marr, mach=MACH)
+    m = rans.mesh.from_arrays(marr)
+    for precision in args.precision.split(","):
+        g = _setup_gpu(precision, m, q0)
+        g.iterate(args.warmup)
+        g.iterate(args.steps)
+        print(json.dumps({"precision": precision, "cells": m.nRealCells, "steps": args.steps,
+                          "ms_per_step": g.last_device_seconds() / args.steps * 1e3}))
+        del g
+
+
 def run_gpu(args):
-    import torch  # device plumbing only: torch.cuda for the device handle
+    import torch  # device plumbing only: pinned host memory for the end-to-end leg
     from aeroflex_gb300 import meshgen, rans
 
     t0 = time.time()
-    marr = meshgen.channel(NX, NY, jitter=0.2, seed=1, shuffle_seed=2)
+    marr = meshgen.channel(args.nx, args.ny, jitter=0.2, seed=1, shuffle_seed=2)
     q0 = meshgen.density_bump_state(marr, mach=MACH)
     m = rans.mesh.from_arrays(marr)
     N, F = m.nRealCells, m.n_edges
@@ -143,8 +164,8 @@ def run_gpu(args):
     result = {}
     for precision in ("fp32-mixed", "fp64"):
         g = _setup_gpu(precision, m, q0)
-        K = args.steps if precision == "fp32-mixed" else max(3, min(args.steps, 20))
-        g.iterate(args.warmup)
+        tuned = g.autotune(3 if precision == "fp32-mixed" else 1)
+        K = args.steps if precision == "fp32-mixed" else max(3, min(args.steps, 50))
         clocks = Clocks()
         clocks.start() if precision == "fp32-mixed" else None
         g.set_q(q0)
@@ -162,7 +183,7 @@ def run_gpu(args):
         ab = algorithmic_bytes(kname, N, F, precision)
         achieved = ab / per_launch_s / 1e9
         launches_per_iter = sum(v[1] for v in prof.values()) / n_prof
-        entry = dict(value=evals, ms_per_step=sec / K * 1e3, steps=K,
+        entry = dict(value=evals, ms_per_step=sec / K * 1e3, steps=K, tuned=tuned,
                      kernels={k: dict(ms_total=v[0], launches=v[1], share=v[0] / tot) for k, v in prof.items()},
                      roofline=dict(kernel=kname, bound="hbm", achieved=achieved, peak=hbm_peak, unit="GB/s",
                                    frac=achieved / hbm_peak, peak_source=peak_kind, traffic=None,
@@ -240,10 +261,14 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--nx", type=int, default=NX)
+    ap.add_argument("--ny", type=int, default=NY)
+    ap.add_argument("--lean", action="store_true", help="warm-up + timed iterations only (for ncu)")
+    ap.add_argument("--precision", default="fp32-mixed", help="--lean: comma-separated precisions")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank = int(os.environ.get("RANK", "0"))
@@ -254,6 +279,9 @@ def main():
         return
     import __graft_entry__
     __graft_entry__.build()
+    if args.lean:
+        run_lean(args)
+        return
     # replicas only: each rank runs the full workload on its own GPU
     if world > 1:
         import torch
@@ -288,7 +316,9 @@ def main():
         "clocks": f32["clocks"],
         "e2e": f32["e2e"],
         "gpu_launches": f32["gpu_launches"],
+        "tuned": f32["tuned"],
         "fp64": {"value": f64["value"], "ms_per_step": f64["ms_per_step"], "steps": f64["steps"],
+                 "tuned": f64["tuned"],
                  "roofline_kernel": f64["roofline"], "kernels": f64["kernels"], "gpu_launches": f64["gpu_launches"]},
         "setup_s": r["setup_s"],
     }

@@ -136,6 +136,13 @@ int afx_last_device_seconds(afx_solver s, double* sec);
  * iterations exactly as afx_iterate would. */
 int afx_profile_iterations(afx_solver s, int n_iters, double* ms, int* launches, int n_kinds);
 const char* afx_kernel_name(int k);
+/* Launch autotuner (no counterpart in the reference): times `iters`
+ * iterations of each residual-kernel variant ("gather": per-cell flux
+ * re-formation; "face": one flux per face + ordered cell sum) at 64, 128 and
+ * 256 threads per block on this solver's mesh, keeps the fastest, and puts
+ * the state back.  Both variants give bit-identical results; the state and
+ * the stored residual qW are as before the call. */
+int afx_autotune(afx_solver s, int iters, char* variant, int cap, int* block, double* ms_per_iter);
 
 #ifdef __cplusplus
 }

@@ -43,19 +43,27 @@ def test_residual_bitexact_omesh(afx, orc, variant):
     np.testing.assert_array_equal(Rg, Ro)
 
 
-def test_residual_bitexact_shuffled_channel(afx, orc):
+@pytest.mark.parametrize("kv", ["gather", "face", "tile"])
+def test_residual_bitexact_shuffled_channel(afx, orc, kv):
     m, bcs, q = channel_case(64, 32)
     so = oracle_solver(orc, m, bcs)
     so.init()
     so.set_q(q)
     Ro = so.residual()
-    g = gpu_solver(afx, m, bcs)
+    g = gpu_solver(afx, m, bcs, kernel_variant=kv)
     g.init()
     g.set_q(q)
     np.testing.assert_array_equal(g.residual(), Ro)
 
 
-@pytest.mark.parametrize("variant", [dict(), dict(viscosity="laminar"), dict(second_order=False)])
+@pytest.mark.parametrize("variant", [
+    dict(), dict(viscosity="laminar"), dict(second_order=False),
+    dict(kernel_variant="gather"), dict(kernel_variant="gather", viscosity="laminar"),
+    dict(kernel_variant="face", block_size=64), dict(kernel_variant="gather", block_size=32),
+    dict(kernel_variant="tile"), dict(kernel_variant="tile", block_size=64),
+    dict(kernel_variant="tile", block_size=256, viscosity="laminar"),
+    dict(kernel_variant="tile", second_order=False),
+])
 def test_iterations_bitexact(afx, orc, variant):
     m, bcs = omesh_case(48, 24)
     so = oracle_solver(orc, m, bcs, **variant)
@@ -73,12 +81,13 @@ def test_iterations_bitexact(afx, orc, variant):
     np.testing.assert_array_equal(g.get_q(), so.q())
 
 
-def test_large_channel_iterations_bitexact(afx, orc):
+@pytest.mark.parametrize("kv", ["face", "tile"])
+def test_large_channel_iterations_bitexact(afx, orc, kv):
     m, bcs, q = channel_case(256, 128)
     so = oracle_solver(orc, m, bcs)
     so.init()
     so.set_q(q)
-    g = gpu_solver(afx, m, bcs)
+    g = gpu_solver(afx, m, bcs, kernel_variant=kv)
     g.init()
     g.set_q(q)
     so.iterate(3)
@@ -147,6 +156,36 @@ def test_fp32_mixed_iterations_track_fp64(afx, orc):
     g.init()
     g.iterate(50)
     assert rel_l2(g.get_q(), so.q()) < 1e-5
+
+
+def test_autotune_keeps_state_and_parity(afx, orc):
+    m, bcs, q = channel_case(128, 64)
+    so = oracle_solver(orc, m, bcs)
+    so.init()
+    so.set_q(q)
+    g = gpu_solver(afx, m, bcs)
+    g.init()
+    g.set_q(q)
+    t = g.autotune(2)
+    assert t["variant"] in ("gather", "face") and t["block"] in (64, 128, 256) and t["ms_per_iter"] > 0
+    np.testing.assert_array_equal(g.get_q(), q)
+    so.iterate(2)
+    g.iterate(2)
+    np.testing.assert_array_equal(g.get_q(), so.q())
+
+
+def test_fp32_mixed_variants_agree(afx):
+    m, bcs, q = channel_case(128, 64)
+    out = []
+    for kv in ("gather", "face", "tile"):
+        g = gpu_solver(afx, m, bcs, precision="fp32-mixed", kernel_variant=kv)
+        g.init()
+        g.set_q(q)
+        g.iterate(3)
+        out.append(g.get_q())
+    # different FP32 summation contexts (fast-math contraction) only
+    assert rel_l2(out[0], out[1]) < 1e-6
+    assert rel_l2(out[0], out[2]) < 1e-6
 
 
 def test_nonfinite_flagged(afx):
