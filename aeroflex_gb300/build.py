@@ -42,6 +42,7 @@ def _units():
         (cxx + ["-c"], "afx_config.cpp"),
         (cxx + ["-c"], "afx_abi.cpp"),
         (nv + ["-fmad=false", "-c"], "afx_kernels_f64.cu"),
+        (nv + ["-fmad=false", "-c"], "afx_noalloc.cu"),
         (nv + ["-use_fast_math", "-c"], "afx_kernels_f32.cu"),
     ], nvcc
 

@@ -24,6 +24,10 @@ namespace afx {
 void enqueue_permute_in(int n, const int* cell_old, const void* src, void* dst, cudaStream_t s);
 void enqueue_permute_out(int n, const int* cell_old, const void* src, void* dst, cudaStream_t s);
 void enqueue_to_f32(int n, const void* src, void* dst, cudaStream_t s);
+long long noalloc_max_cells();
+long long noalloc_max_faces();
+cudaError_t noalloc_residual_f64(const StepArgs& a, const int* cell_old, const double* q_ref, double* R_ref,
+                                 cudaStream_t s);
 }  // namespace afx
 
 using namespace afx;
@@ -1008,6 +1012,35 @@ const char* afx_kernel_name(int k) {
     static const char* names[K_COUNT] = {"k_prep", "k_limiter", "k_face_flux", "k_cell_sum", "k_resid_gather",
                                          "k_control", "k_resid_tile"};
     return (k >= 0 && k < K_COUNT) ? names[k] : "";
+}
+
+// For callers that cannot let the library allocate device memory (see
+// afx_noalloc.cu): the residual of a caller-owned device state, written to a
+// caller-owned device array, with all scratch in the library's fixed device
+// array.  No cudaMalloc/cudaFree or other allocating call is made here.
+int afx_residual_noalloc(afx_solver s, const double* q_dev, double* R_dev, long long n) {
+    return guarded([&] {
+        if (!s || !q_dev || !R_dev) throw Error(AFX_ERR_ARG, "null argument");
+        const long long N = s->a.n_cells;
+        if (n != 4 * N) throw Error(AFX_ERR_ARG, "state size must be 4*n_real_cells");
+        if (!s->fp64) throw Error(AFX_ERR_CONFIG, "afx_residual_noalloc needs an fp64 solver");
+        if (N > noalloc_max_cells() || s->a.n_faces > noalloc_max_faces())
+            throw Error(AFX_ERR_ARG, "mesh too large for afx_residual_noalloc: " + std::to_string(N) + " cells, " +
+                                         std::to_string(s->a.n_faces) + " faces (limits " +
+                                         std::to_string(noalloc_max_cells()) + " cells, " +
+                                         std::to_string(noalloc_max_faces()) + " faces)");
+        for (const void* ptr : {(const void*)q_dev, (const void*)R_dev}) {
+            cudaPointerAttributes at;
+            if (cudaPointerGetAttributes(&at, ptr) != cudaSuccess ||
+                (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged)) {
+                cudaGetLastError();
+                throw Error(AFX_ERR_ARG, "afx_residual_noalloc takes device pointers");
+            }
+        }
+        s->set_ctrl(0, 0, 0);
+        AFX_CUDA(noalloc_residual_f64(s->a, (const int*)s->d_cell_old.p, q_dev, R_dev, s->stream));
+        AFX_CUDA(cudaStreamSynchronize(s->stream));
+    });
 }
 
 int afx_request_stop(afx_solver s) {

@@ -26,6 +26,7 @@ ABI_SYMBOLS = [
     "afx_solver_free", "afx_init_freestream", "afx_set_state", "afx_get_state", "afx_residual", "afx_iterate",
     "afx_run_to_convergence", "afx_residual_history", "afx_forces", "afx_set_farfield", "afx_request_stop",
     "afx_last_device_seconds", "afx_profile_iterations", "afx_kernel_name", "afx_autotune",
+    "afx_residual_noalloc",
 ]
 N_KERNEL_KINDS = 7
 
@@ -85,6 +86,7 @@ def lib():
         "afx_profile_iterations": (i, [vp, i, vp, vp, i]),
         "afx_kernel_name": (cp, [i]),
         "afx_autotune": (i, [vp, i, ctypes.c_char_p, i, P(i), P(d)]),
+        "afx_residual_noalloc": (i, [vp, vp, vp, ll]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

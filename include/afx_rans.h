@@ -144,6 +144,22 @@ const char* afx_kernel_name(int k);
  * the stored residual qW are as before the call. */
 int afx_autotune(afx_solver s, int iters, char* variant, int cap, int* block, double* ms_per_iter);
 
+/* Residual without device allocation.  No counterpart in the reference.
+ * For callers that cannot let a library allocate device memory — a coupling
+ * code that owns all device memory through its own pool (a library-side
+ * cudaMalloc would synchronise the device and break its stream overlap), or
+ * code recording a CUDA stream capture, where allocating calls are not
+ * allowed.  Same result as afx_residual (bit for bit) for the state q_dev,
+ * but q_dev and R_dev are the caller's DEVICE arrays of 4*n_real doubles in
+ * reference cell order, and the scratch lives in a fixed 24 MiB device array
+ * inside the library: at most 262,144 cells and 524,288 faces (larger meshes
+ * return AFX_ERR_ARG).  FP64 solvers only.  The solver's own state is not
+ * changed; its gradient/limiter buffers are overwritten as afx_residual does.
+ * Calls share the fixed array, so calls that overlap on the GPU race: the
+ * caller serialises them.  The first call on each device looks up the
+ * array's address; make it before any stream capture. */
+int afx_residual_noalloc(afx_solver s, const double* q_dev, double* R_dev, long long n);
+
 #ifdef __cplusplus
 }
 #endif
