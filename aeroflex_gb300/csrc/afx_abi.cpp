@@ -701,7 +701,7 @@ int afx_solver_create(afx_mesh mp, afx_config cp, afx_solver* out) {
         const int variant = st.kernel_variant == "face" ? 1
                             : st.kernel_variant == "gather" ? 0
                             : st.kernel_variant == "tile" ? 2
-                                                          : (s->fp64 ? 1 : 0);
+                                                          : (s->fp64 ? 1 : 2);
         const int block = st.block_size ? st.block_size : (N >= 600 * 256 ? 256 : (N >= 300 * 128 ? 128 : 64));
         for (int p = 0; p < 2; ++p) {
             a.qm[p] = s->dalloc(N * 32);

@@ -18,6 +18,17 @@ __device__ __forceinline__ int pick(const int4 v, const int s) {
     return s == 0 ? v.x : (s == 1 ? v.y : (s == 2 ? v.z : v.w));
 }
 
+// Plain (non-__ldg) vector loads, for shared memory.
+__device__ __forceinline__ void ld4p(const d4* p, double* v) {
+    const double2* q = reinterpret_cast<const double2*>(p);
+    const double2 a = q[0], b = q[1];
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+}
+__device__ __forceinline__ void ld4p(const float4* p, float* v) {
+    const float4 a = *p;
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+}
+
 // Per cell, from the iteration's starting state q (the solver's member q):
 // local time step (solver.h:308-356; skipped when the face kernel forms it),
 // Green-Gauss gradient (solver.h:428-469) and, when second order, the first
@@ -241,6 +252,7 @@ __device__ __forceinline__ void face_gradient(const T* qa, const T* qb, const T*
 template <class T, class S>
 struct StageOut {
     const d4* __restrict__ q0;     // FP64 iteration start state (member q)
+    const V4<S>* __restrict__ q0s; // the same state in S (FP32-mixed: its FP32 shadow)
     V4<S>* __restrict__ qnext;     // next stage state in S (stages 0, 1)
     d4* __restrict__ qm_next;      // FP64 new state (stage 2)
     V4<S>* __restrict__ qsh_next;  // new state in S (stage 2, FP32-mixed shadow), may be null
@@ -264,6 +276,49 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
     return t;
 }
 
+// FP32-mixed epilogue.  GB300's FP64 pipe issues at ~1/64 of the FP32 rate,
+// so FP64 is spent only where it accumulates: the RK increment
+// R*dt*alpha*relaxation is formed in FP32; the intermediate stage states
+// (which only feed FP32 fluxes) are q_shadow + increment in FP32; the new
+// state of the last stage is q (FP64) + increment in FP64, and its FP32
+// shadow is re-rounded from the FP64 result every iteration, so FP32
+// rounding never accumulates in the state.  The norm sums per-cell FP32
+// squares in FP64.
+template <class S>
+__device__ __forceinline__ void stage_epilogue_mixed(const StageOut<float, S>& o, const int i, const float* R,
+                                                     const float dti, double& sq) {
+    const float fac = dti * (float)o.alpha * (float)o.relax;
+    float inc[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) inc[k] = R[k] * fac;
+    if (o.mode == 0) {
+        float qs[4];
+        ld4(&o.q0s[i], qs);
+        float qn[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) qn[k] = qs[k] + inc[k];
+        V4<S> v;
+        st4(&v, qn);
+        o.qnext[i] = v;
+    } else {
+        double q0[4];
+        ld4(&o.q0[i], q0);
+        double qn[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) qn[k] = q0[k] + (double)inc[k];
+        st4(&o.qm_next[i], qn);
+        if (o.qsh_next) {
+            V4<S> v;
+            st4(&v, qn);
+            o.qsh_next[i] = v;
+        }
+        sq += (double)(R[0] * R[0] + R[1] * R[1] + R[2] * R[2] + R[3] * R[3]);
+    }
+}
+template <class S>
+__device__ __forceinline__ void stage_epilogue_mixed(const StageOut<double, S>&, const int, const double*,
+                                                     const double, double&) {}
+
 template <class T, class S>
 __device__ __forceinline__ void stage_epilogue(const StageOut<T, S>& o, const int i, const bool active, const T* Rsum,
                                                const T A, const T dti, const double extra_sq, double* sh) {
@@ -275,6 +330,8 @@ __device__ __forceinline__ void stage_epilogue(const StageOut<T, S>& o, const in
         if (o.mode == 2) {
             double Rd[4] = {(double)R[0], (double)R[1], (double)R[2], (double)R[3]};
             st4(&o.Rq[i], Rd);
+        } else if (sizeof(T) == 4) {
+            stage_epilogue_mixed<S>(o, i, R, dti, sq);
         } else {
             double q0[4];
             ld4(&o.q0[i], q0);
@@ -540,16 +597,15 @@ __global__ void __launch_bounds__(256) k_resid_tile(const KM<T> m, const TileVie
     const int tile = blockIdx.x;
     const int h0 = __ldg(&tv.hstart[tile]), nh = __ldg(&tv.hstart[tile + 1]) - h0;
     const int x0 = __ldg(&tv.xptr[tile]), nf = nh + __ldg(&tv.xptr[tile + 1]) - x0;
-    T* sF = reinterpret_cast<T*>(smem_raw);  // nf x 4
-    T* sE = sF + 4 * (size_t)nf;             // nf (EIG)
+    V4<T>* sF = reinterpret_cast<V4<T>*>(smem_raw);  // nf face fluxes F*L
+    T* sE = reinterpret_cast<T*>(sF + nf);            // nf eig*L (EIG)
     double extra = 0;
     for (int j = threadIdx.x; j < nf; j += blockDim.x) {
         const int f = j < nh ? h0 + j : __ldg(&tv.xlist[x0 + j - nh]);
         T fl[4], eL = T(0);
         int bt;
         face_flux_at<T, S, VISC, SECOND, EIG>(m, f, qk, qmem, gx, gy, phi, fl, &eL, &bt);
-#pragma unroll
-        for (int k = 0; k < 4; ++k) sF[4 * j + k] = fl[k];
+        st4(&sF[j], fl);
         if (EIG) sE[j] = eL;
         if (o.mode == 1 && bt >= 0 && two_sided(bt))  // qW of a frozen ghost (solver.h:789-790)
 #pragma unroll
@@ -569,12 +625,14 @@ __global__ void __launch_bounds__(256) k_resid_tile(const KM<T> m, const TileVie
             if (v != 0) {
                 const int lf = (v > 0 ? v : -v) - 1;
                 if (EIG) eigsum += sE[lf];
+                T fl[4];
+                ld4p(&sF[lf], fl);
                 if (v > 0) {
 #pragma unroll
-                    for (int k = 0; k < 4; ++k) Rs[k] -= sF[4 * lf + k];
+                    for (int k = 0; k < 4; ++k) Rs[k] -= fl[k];
                 } else {
 #pragma unroll
-                    for (int k = 0; k < 4; ++k) Rs[k] += sF[4 * lf + k];
+                    for (int k = 0; k < 4; ++k) Rs[k] += fl[k];
                 }
             }
         }

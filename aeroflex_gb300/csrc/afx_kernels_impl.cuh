@@ -126,6 +126,7 @@ template <class T, class S>
 StageOut<T, S> base_out(const StepArgs& a, int p) {
     StageOut<T, S> o;
     o.q0 = (const d4*)a.qm[p];
+    o.q0s = (const V4<S>*)a.qsh[p];
     o.qnext = nullptr;
     o.qm_next = nullptr;
     o.qsh_next = nullptr;

@@ -95,10 +95,11 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def _setup_gpu(precision, m, q0):
+def _setup_gpu(precision, m, q0, variant="auto"):
     from aeroflex_gb300 import rans
     st = rans.Settings()
     st.set("solver", "explicit").set("precision", precision).set("start_cfl", 1.0).set("relaxation", 0.9)
+    st.set("kernel_variant", variant)
     st.set_bc("farfield", "farfield", 1.0, MACH, 0.0, 1.0).set_bc("wall", "slip-wall")
     g = rans.Solver(m, st)
     g.init()
@@ -142,7 +143,7 @@ def run_lean(args):
     q0 = meshgen.density_bump_state(marr, mach=MACH)
     m = rans.mesh.from_arrays(marr)
     for precision in args.precision.split(","):
-        g = _setup_gpu(precision, m, q0)
+        g = _setup_gpu(precision, m, q0, args.variant)
         g.iterate(args.warmup)
         g.iterate(args.steps)
         print(json.dumps({"precision": precision, "cells": m.nRealCells, "steps": args.steps,
@@ -168,6 +169,8 @@ def run_gpu(args):
         K = args.steps if precision == "fp32-mixed" else max(3, min(args.steps, 50))
         clocks = Clocks()
         clocks.start() if precision == "fp32-mixed" else None
+        g.set_q(q0)
+        g.iterate(args.warmup)
         g.set_q(q0)
         g.iterate(K)
         sec = g.last_device_seconds()
@@ -269,6 +272,7 @@ def main():
     ap.add_argument("--ny", type=int, default=NY)
     ap.add_argument("--lean", action="store_true", help="warm-up + timed iterations only (for ncu)")
     ap.add_argument("--precision", default="fp32-mixed", help="--lean: comma-separated precisions")
+    ap.add_argument("--variant", default="auto", help="--lean: residual kernel variant (auto|gather|face|tile)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank = int(os.environ.get("RANK", "0"))
