@@ -24,6 +24,7 @@ namespace afx {
 void enqueue_permute_in(int n, const int* cell_old, const void* src, void* dst, cudaStream_t s);
 void enqueue_permute_out(int n, const int* cell_old, const void* src, void* dst, cudaStream_t s);
 void enqueue_to_f32(int n, const void* src, void* dst, cudaStream_t s);
+void enqueue_correction(int n, const void* R64, const void* R32, void* corr, cudaStream_t s);
 long long noalloc_max_cells();
 long long noalloc_max_faces();
 cudaError_t noalloc_residual_f64(const StepArgs& a, const int* cell_old, const double* q_ref, double* R_ref,
@@ -117,6 +118,25 @@ struct afx_solver_s {
     };
     std::map<int, std::unique_ptr<TileData>> tiles;  // per block size
     bool fp64 = true;
+    // FP32-mixed defect correction: an FP64 residual machine on the same FP64
+    // master state (FP64 geometry and work arrays), refreshed every
+    // corr_interval iterations
+    int corr_interval = 0;
+    StepArgs a64;
+    void* R32buf = nullptr;
+
+    // corr = R64(q) - R32(q) for the state of parity p.  Both residual
+    // launches use a64's control block, which is never set to done, so a
+    // refresh inside a run leaves the run's own control block alone.  The
+    // FP32 gradient/limiter buffers are re-formed by the next iteration.
+    void refresh_correction(int p) {
+        enqueue_residual_f64(a64, p, stream);
+        StepArgs r = a;
+        r.Rq = R32buf;
+        r.ctrl = a64.ctrl;
+        enqueue_residual_f32(r, p, stream);
+        enqueue_correction(a.n_cells, a64.Rq, R32buf, (void*)a.corr, stream);
+    }
 
     // Tile lists for `B` cells per tile: faces sorted by their first device
     // cell make each tile's own faces one contiguous range; a face whose two
@@ -222,6 +242,7 @@ struct afx_solver_s {
     ~afx_solver_s() {
         if (stream) cudaStreamSynchronize(stream);
         for (auto& g : graphs) cudaGraphExecDestroy(g.second);
+        for (auto& g : graphs64) cudaGraphExecDestroy(g.second);
         if (h_ctrl) cudaFreeHost(h_ctrl);
         if (h_stage) cudaFreeHost(h_stage);
         bufs.clear();
@@ -263,6 +284,9 @@ struct afx_solver_s {
         } else {
             std::vector<float> f(bq.begin(), bq.end());
             AFX_CUDA(cudaMemcpyAsync((void*)a.bq, f.data(), f.size() * 4, cudaMemcpyHostToDevice, stream));
+            if (a64.bq)
+                AFX_CUDA(cudaMemcpyAsync((void*)a64.bq, bq.data(), bq.size() * 8, cudaMemcpyHostToDevice, stream));
+            AFX_CUDA(cudaStreamSynchronize(stream));
         }
         AFX_CUDA(cudaStreamSynchronize(stream));
     }
@@ -276,22 +300,49 @@ struct afx_solver_s {
         else enqueue_iteration_f32(a, p, stream);
     }
 
-    cudaGraphExec_t graph(int k, int p) {
+    // FP32-mixed with an FP64 finish: after the FP32 residual stops falling,
+    // the run continues with FP64 iterations on the same FP64 master state.
+    bool finish = false;
+    StepArgs a64it;              // the FP64 machine set up for iterations (main control block)
+    bool shadow_stale = false;   // FP64 iterations ran since the FP32 shadow was formed
+    bool last_fp64 = false;      // the last iteration was an FP64 one
+    // FP64-finish phase, kept across runs until the state or the boundary
+    // conditions are reset (init, set_state, set_farfield)
+    bool phase64 = false;
+    long long iters_total = 0;
+    std::vector<std::pair<long long, double>> fp32_samples;  // (iteration, norm) of the FP32 phase
+    void reset_phase() {
+        phase64 = false;
+        iters_total = 0;
+        fp32_samples.clear();
+    }
+    std::map<std::pair<int, int>, cudaGraphExec_t> graphs64;
+
+    void ensure_shadow() {
+        if (shadow_stale) {
+            sync_shadow(parity);
+            shadow_stale = false;
+        }
+    }
+
+    cudaGraphExec_t graph(int k, int p, bool g64 = false) {
+        auto& cache = g64 ? graphs64 : graphs;
         auto key = std::make_pair(k, p);
-        auto it = graphs.find(key);
-        if (it != graphs.end()) return it->second;
+        auto it = cache.find(key);
+        if (it != cache.end()) return it->second;
         cudaGraph_t g;
         AFX_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
         int q = p;
         for (int i = 0; i < k; ++i) {
-            enqueue_iteration(q);
+            if (g64) enqueue_iteration_f64(a64it, q, stream);
+            else enqueue_iteration(q);
             q ^= 1;
         }
         AFX_CUDA(cudaStreamEndCapture(stream, &g));
         cudaGraphExec_t ex;
         AFX_CUDA(cudaGraphInstantiate(&ex, g, 0));
         cudaGraphDestroy(g);
-        graphs[key] = ex;
+        cache[key] = ex;
         return ex;
     }
 
@@ -318,28 +369,51 @@ struct afx_solver_s {
         if (pending_last < 0) return;
         set_ctrl(0, 0, 0);  // the kernels skip their work while ctrl->done is set
         if (fp64) enqueue_last_stage_residual_f64(a, pending_last, stream);
+        else if (last_fp64) enqueue_last_stage_residual_f64(a64it, pending_last, stream);
         else enqueue_last_stage_residual_f32(a, pending_last, stream);
         pending_last = -1;
     }
 
     // Runs n iterations (run_mode 0) or the run_solver loop (run_mode 1).
-    // Returns the number of iterations executed.
+    // Returns the number of iterations executed.  With the FP64 finish
+    // (run_mode 1 only), the FP32 phase ends when the residual norm has not
+    // halved over the last 3000 iterations; FP64 iterations follow.
     int run(int n, int run_mode, double tol) {
         const int p0 = parity;
+        ensure_shadow();
         AFX_CUDA(cudaEventRecord(ev0, stream));
         const int K = chunk();
         int launched = 0;
         bool stopped = false;
+        last_fp64 = phase64;
+        auto& samples = fp32_samples;
+        int since = corr_interval;  // refresh the defect correction before the first chunk
         while (launched < n) {
+            if (!phase64 && corr_interval > 0 && since >= corr_interval) {
+                refresh_correction((p0 + launched) & 1);
+                since = 0;
+            }
             const int k = (n - launched >= K) ? K : 1;
-            AFX_CUDA(cudaGraphLaunch(graph(k, (p0 + launched) & 1), stream));
+            AFX_CUDA(cudaGraphLaunch(graph(k, (p0 + launched) & 1, phase64), stream));
             launched += k;
+            since += k;
             if (run_mode == 1 || launched >= n || stop.load()) {
                 read_ctrl();
                 if (h_ctrl->done) break;
                 if (stop.load()) {
                     stopped = true;
                     break;
+                }
+                const long long now = iters_total + launched;
+                if (finish && !phase64 && run_mode == 1 && (samples.empty() || now - samples.back().first >= 1000)) {
+                    samples.emplace_back(now, h_ctrl->last_norm);
+                    for (const auto& sm : samples)
+                        if (now - sm.first >= 3000 && now - sm.first < 4000 && h_ctrl->last_norm > 0.5 * sm.second) {
+                            phase64 = true;  // FP32 floor reached
+                            shadow_stale = true;
+                            last_fp64 = true;
+                            break;
+                        }
                 }
             }
         }
@@ -349,6 +423,8 @@ struct afx_solver_s {
         AFX_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
         last_sec = ms * 1e-3;
         const int done = h_ctrl->iter;
+        iters_total += done;
+        if (phase64 && done > 0) shadow_stale = true;
         parity = p0 ^ (done & 1);
         if (done > 0) pending_last = parity ^ 1;
         (void)tol;
@@ -546,6 +622,11 @@ int afx_config_set_double(afx_config c, const char* key, double v) {
             if (b != 0 && b != 32 && b != 64 && b != 128 && b != 256)
                 throw Error(AFX_ERR_CONFIG, "block_size must be 0 (auto), 32, 64, 128 or 256");
             c->s.block_size = b;
+        } else if (k == "fp64_correction_interval") {
+            if (v < 0) throw Error(AFX_ERR_CONFIG, "fp64_correction_interval must be >= 0");
+            c->s.fp64_correction_interval = (int)v;
+        } else if (k == "fp64_finish") {
+            c->s.fp64_finish = v != 0;
         }
         else if (k == "second_order") c->s.second_order = v != 0;
         else if (double* p = dfield(c->s, k)) *p = v;
@@ -560,6 +641,8 @@ int afx_config_get_double(afx_config c, const char* key, double* v) {
         if (k == "rhs_iterations") *v = c->s.rhs_iterations;
         else if (k == "max_iterations") *v = c->s.max_iterations;
         else if (k == "block_size") *v = c->s.block_size;
+        else if (k == "fp64_correction_interval") *v = c->s.fp64_correction_interval;
+        else if (k == "fp64_finish") *v = c->s.fp64_finish ? 1 : 0;
         else if (k == "second_order") *v = c->s.second_order ? 1 : 0;
         else if (double* p = dfield(c->s, k)) *v = *p;
         else throw Error(AFX_ERR_ARG, "unknown numeric setting '" + k + "'");
@@ -620,6 +703,20 @@ int afx_config_bc_count(afx_config c, int* n) {
     return guarded([&] {
         if (!c || !n) throw Error(AFX_ERR_ARG, "null argument");
         *n = (int)c->s.bcs.size();
+    });
+}
+
+int afx_config_get_bc(afx_config c, const char* name, char* type, int cap, double* T, double* mach, double* angle,
+                      double* p) {
+    return guarded([&] {
+        if (!c || !name) throw Error(AFX_ERR_ARG, "null argument");
+        auto it = c->s.bcs.find(name);
+        if (it == c->s.bcs.end()) throw Error(AFX_ERR_ARG, std::string("no boundary condition '") + name + "'");
+        if (type && cap > 0) std::snprintf(type, cap, "%s", it->second.type.c_str());
+        if (T) *T = it->second.vars.T;
+        if (mach) *mach = it->second.vars.mach;
+        if (angle) *angle = it->second.vars.angle;
+        if (p) *p = it->second.vars.p;
     });
 }
 
@@ -722,6 +819,51 @@ int afx_solver_create(afx_mesh mp, afx_config cp, afx_solver* out) {
         a.hist = (double*)s->dalloc(HIST_CAP * sizeof(double));
         s->d_cell_old.upload(L.cell_old.data(), N * sizeof(int), s->stream);
         s->set_launch(variant, block);
+        if (!s->fp64 && (st.fp64_correction_interval > 0 || st.fp64_finish)) {
+            // FP64 residual machine on the same FP64 master state
+            s->corr_interval = st.fp64_correction_interval;
+            StepArgs& b = s->a64;
+            b = a;
+            b.area = s->dupload(L.area);
+            b.fn = s->dupload(L.fn);
+            b.fLg = s->dupload(L.fLg);
+            b.fd0 = s->dupload(L.fd0);
+            b.fd1 = s->dupload(L.fd1);
+            b.ft = s->dupload(L.ft);
+            b.bq = s->dalloc(std::max<size_t>(B, 1) * 32);
+            for (int p = 0; p < 2; ++p) b.qsh[p] = b.qm[p];
+            b.qs[0] = b.qs[1] = nullptr;  // residual launches read no stage state
+            b.gx = s->dalloc(N * 32);
+            b.gy = s->dalloc(N * 32);
+            b.phi = s->dalloc(N * 32);
+            b.dt = s->dalloc(N * 8);
+            b.Rq = s->dalloc(N * 32);
+            b.variant = 0;  // gather: no FP64 face buffers needed
+            b.fflux = b.feL = nullptr;
+            b.corr = nullptr;
+            b.ctrl = (Ctrl*)s->dalloc(sizeof(Ctrl));  // zeroed, never set to done
+            s->R32buf = s->dalloc(N * 32);
+            if (s->corr_interval > 0) a.corr = s->dalloc(N * 16);
+            if (st.fp64_finish) {
+                // the same machine, set up to iterate: FP64 stage states, the
+                // face-flux variant (FP64-pipe bound: one flux per face), the
+                // run's own control block, partial sums and history
+                s->finish = true;
+                StepArgs& c = s->a64it;
+                c = b;
+                c.qs[0] = s->dalloc(N * 32);
+                c.qs[1] = s->dalloc(N * 32);
+                c.variant = 1;
+                c.fflux = s->dalloc(F * 32);
+                c.feL = s->dalloc(F * 8);
+                c.Rq = a.Rq;
+                c.ctrl = a.ctrl;
+                c.partials = a.partials;
+                c.hist = a.hist;
+                c.norms = a.norms;
+                c.block = N >= 600 * 256 ? 256 : (N >= 300 * 128 ? 128 : 64);
+            }
+        }
         s->d_stage.alloc(N * 32);
         AFX_CUDA(cudaHostAlloc((void**)&s->h_stage, N * 32, cudaHostAllocDefault));
         s->h_stage_bytes = N * 32;
@@ -742,6 +884,8 @@ int afx_init_freestream(afx_solver s) {
         for (size_t i = 0; i < N; ++i) std::memcpy(s->h_stage + 4 * i, q, 32);
         AFX_CUDA(cudaMemcpyAsync(s->a.qm[s->parity], s->h_stage, N * 32, cudaMemcpyHostToDevice, s->stream));
         s->sync_shadow(s->parity);
+        s->shadow_stale = false;
+        s->reset_phase();
         s->refill_bcs();
     });
 }
@@ -754,6 +898,8 @@ int afx_set_state(afx_solver s, const double* q, long long n) {
         AFX_CUDA(cudaMemcpyAsync(s->d_stage.p, q, N * 32, cudaMemcpyDefault, s->stream));
         enqueue_permute_in((int)N, (const int*)s->d_cell_old.p, s->d_stage.p, s->a.qm[s->parity], s->stream);
         s->sync_shadow(s->parity);
+        s->shadow_stale = false;
+        s->reset_phase();
         AFX_CUDA(cudaStreamSynchronize(s->stream));
     });
 }
@@ -774,6 +920,7 @@ int afx_residual(afx_solver s, double* R, long long n) {
         if (!s) throw Error(AFX_ERR_ARG, "null argument");
         const size_t N = s->a.n_cells;
         if (R && n != (long long)(4 * N)) throw Error(AFX_ERR_ARG, "residual size must be 4*n_real_cells");
+        s->ensure_shadow();
         s->set_ctrl(0, 0, 0);
         if (s->fp64) enqueue_residual_f64(s->a, s->parity, s->stream);
         else enqueue_residual_f32(s->a, s->parity, s->stream);
@@ -904,6 +1051,7 @@ int afx_set_farfield(afx_solver s, const char* patch, double mach, double angle,
             throw Error(AFX_ERR_ARG, std::string("no farfield patch '") + patch + "'");
         s->materialize_qW();
         it->second.vars = FarfieldVars{mach, angle, T, p};
+        s->reset_phase();
         s->set_bcs();
         s->refill_bcs();
     });
@@ -918,6 +1066,7 @@ int afx_profile_iterations(afx_solver s, int n_iters, double* ms, int* launches,
             ms[k] = 0;
             launches[k] = 0;
         }
+        s->ensure_shadow();
         s->set_ctrl(0, n_iters, 0);
         s->a.prof = &prof;
         try {
@@ -954,6 +1103,7 @@ int afx_autotune(afx_solver s, int iters, char* variant, int cap, int* block, do
         const size_t N = a.n_cells;
         // qW of the last run is formed now: the timing runs overwrite its inputs
         s->materialize_qW();
+        s->ensure_shadow();
         // keep the state: the timing runs start from it and it is put back after
         DevBuf save;
         save.alloc(N * 32);

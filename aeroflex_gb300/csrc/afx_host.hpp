@@ -51,6 +51,12 @@ struct Settings {
     // variant "auto" | "gather" | "face" and threads per block (0 = auto)
     std::string kernel_variant = "auto";
     int block_size = 0;
+    // FP32-mixed only: refresh the FP64 defect correction every this many
+    // iterations (0 = pure FP32 residual)
+    int fp64_correction_interval = 0;
+    // FP32-mixed only: run_to_convergence switches to FP64 iterations once the
+    // FP32 residual stops falling
+    bool fp64_finish = false;
 
     int viscosity_code() const;
     static int bc_code(const std::string& t);

@@ -260,8 +260,24 @@ struct StageOut {
     T* __restrict__ dt;
     double alpha, relax;
     double* __restrict__ partials;
+    const float4* __restrict__ corr;  // FP32-mixed defect correction per cell, or null
     int mode;                      // 0 stage 0/1, 1 stage 2 (+norm), 2 residual only (write R)
 };
+
+// Mixed-precision defect correction: corr = R64(q) - R32(q) at a reference
+// state q (both residuals formed with the first-stage semantics).  The FP32
+// stages then drive R32 + corr to zero, whose fixed point, once q_ref is
+// refreshed to the converged state, is R64 = 0: the FP64 solution, reached
+// with FP32 face arithmetic between refreshes.
+static __global__ void k_correction(const int n, const d4* __restrict__ R64, const d4* __restrict__ R32,
+                             float4* __restrict__ corr) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double a[4], b[4];
+    ld4(&R64[i], a);
+    ld4(&R32[i], b);
+    corr[i] = make_float4((float)(a[0] - b[0]), (float)(a[1] - b[1]), (float)(a[2] - b[2]), (float)(a[3] - b[3]));
+}
 
 __device__ __forceinline__ double block_sum(double v, double* sh) {
 #pragma unroll
@@ -285,8 +301,14 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
 // rounding never accumulates in the state.  The norm sums per-cell FP32
 // squares in FP64.
 template <class S>
-__device__ __forceinline__ void stage_epilogue_mixed(const StageOut<float, S>& o, const int i, const float* R,
+__device__ __forceinline__ void stage_epilogue_mixed(const StageOut<float, S>& o, const int i, const float* R0,
                                                      const float dti, double& sq) {
+    // defect correction: R = R32(q) + (R64 - R32)(q_ref), see k_correction
+    float R[4] = {R0[0], R0[1], R0[2], R0[3]};
+    if (o.corr) {
+        const float4 c = __ldg(&o.corr[i]);
+        R[0] += c.x; R[1] += c.y; R[2] += c.z; R[3] += c.w;
+    }
     const float fac = dti * (float)o.alpha * (float)o.relax;
     float inc[4];
 #pragma unroll

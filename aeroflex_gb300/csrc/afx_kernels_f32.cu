@@ -16,5 +16,8 @@ void enqueue_last_stage_residual_f32(const StepArgs& a, int p, cudaStream_t s) {
 void enqueue_uniform_f32(const StepArgs& a, int p, const double* qf, cudaStream_t s) {
     dev::uniform<float, float>(a, p, qf, s);
 }
+void enqueue_correction(int n, const void* R64, const void* R32, void* corr, cudaStream_t s) {
+    dev::k_correction<<<(n + 255) / 256, 256, 0, s>>>(n, (const dev::d4*)R64, (const dev::d4*)R32, (float4*)corr);
+}
 
 }  // namespace afx

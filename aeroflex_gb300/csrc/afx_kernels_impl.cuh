@@ -135,6 +135,7 @@ StageOut<T, S> base_out(const StepArgs& a, int p) {
     o.alpha = 1.0;
     o.relax = a.relax;
     o.partials = a.partials;
+    o.corr = (const float4*)a.corr;
     o.mode = 0;
     return o;
 }

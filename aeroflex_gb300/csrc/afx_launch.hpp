@@ -96,6 +96,7 @@ struct StepArgs {
     Ctrl* ctrl = nullptr;
     double* hist = nullptr;    // [HIST_CAP] run_solver history (every 10th)
     double* norms = nullptr;   // optional per-iteration norms
+    const void* corr = nullptr;  // float4 [N]: FP32-mixed defect correction (null: off)
     Prof* prof = nullptr;      // eager profiling only (never inside a graph)
 };
 

@@ -42,23 +42,40 @@ def naca4_surface(n_surf, m=0.0, p=0.4, t=0.12):
     return x, y
 
 
-def airfoil_omesh(n_surf=128, n_rad=64, r_far=20.0, growth=1.1, m=0.0, p=0.4, t=0.12, split=True):
+def airfoil_omesh(n_surf=128, n_rad=64, r_far=20.0, growth=None, first=2e-3, m=0.0, p=0.4, t=0.12, split=True):
     """O-mesh around a NACA 4-digit airfoil of chord 1.
 
     ``n_surf`` distinct surface nodes, ``n_rad + 1`` node layers whose
-    spacing grows geometrically by ``growth`` out to a circle of radius
-    ``r_far`` chords centred at mid-chord.  Each quad is split into two
-    triangles along a fixed diagonal when ``split``.  Patches: "wall"
-    (airfoil) and "farfield" (outer circle).
+    spacing grows geometrically out to a circle of radius ``r_far`` chords
+    centred at mid-chord; the ratio is ``growth`` if given, else the one that
+    makes the first layer ``first`` chords thick.  Grid lines leave the
+    surface along its normal and blend linearly (in the layer coordinate)
+    into uniformly spaced points on the far-field circle.  Each quad is split
+    into two triangles along a fixed diagonal when ``split``.  Patches:
+    "wall" (airfoil) and "farfield" (outer circle).
     """
     sx, sy = naca4_surface(n_surf, m, p, t)
     ang = 2.0 * np.pi * np.arange(n_surf) / n_surf
     fx = 0.5 + r_far * np.cos(ang)
     fy = r_far * np.sin(ang)
+    # outward normals: rotate the central-difference tangent (CCW surface -> outward = (ty, -tx))
+    tx = np.roll(sx, -1) - np.roll(sx, 1)
+    ty = np.roll(sy, -1) - np.roll(sy, 1)
+    tn = np.hypot(tx, ty)
+    nx_, ny_ = ty / tn, -tx / tn
+    if growth is None:
+        # geometric ratio r with r_far*(r - 1)/(r^n - 1) = first (bisection)
+        lo, hi = 1.0 + 1e-9, 2.0
+        for _ in range(200):
+            mid = 0.5 * (lo + hi)
+            h1 = r_far * (mid - 1.0) / (mid ** n_rad - 1.0)
+            lo, hi = (lo, mid) if h1 < first else (mid, hi)
+        growth = 0.5 * (lo + hi)
     k = np.arange(n_rad + 1)
     s = (growth ** k - 1.0) / (growth ** n_rad - 1.0)
-    X = sx[None, :] + (fx - sx)[None, :] * s[:, None]
-    Y = sy[None, :] + (fy - sy)[None, :] * s[:, None]
+    S = s[:, None]
+    X = (1.0 - S) * (sx[None, :] + r_far * S * nx_[None, :]) + S * fx[None, :]
+    Y = (1.0 - S) * (sy[None, :] + r_far * S * ny_[None, :]) + S * fy[None, :]
     x = X.reshape(-1)
     y = Y.reshape(-1)
 
@@ -71,8 +88,12 @@ def airfoil_omesh(n_surf=128, n_rad=64, r_far=20.0, growth=1.1, m=0.0, p=0.4, t=
     c = nid(kk + 1, jj + 1)
     d = nid(kk + 1, jj)
     if split:
-        t1 = np.stack([a, b, c, np.full_like(a, -1)], -1).reshape(-1, 4)
-        t2 = np.stack([a, c, d, np.full_like(a, -1)], -1).reshape(-1, 4)
+        # diagonals alternate in a checkerboard: a one-way split biases the
+        # Green-Gauss reconstruction and stalls the explicit scheme
+        neg = np.full_like(a, -1)
+        alt = ((kk + jj) % 2 == 1)[..., None]
+        t1 = np.where(alt, np.stack([a, b, d, neg], -1), np.stack([a, b, c, neg], -1)).reshape(-1, 4)
+        t2 = np.where(alt, np.stack([b, c, d, neg], -1), np.stack([a, c, d, neg], -1)).reshape(-1, 4)
         cells = np.stack([t1, t2], 1).reshape(-1, 4)
     else:
         cells = np.stack([a, b, c, d], -1).reshape(-1, 4)

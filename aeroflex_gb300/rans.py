@@ -22,7 +22,8 @@ ABI_SYMBOLS = [
     "afx_last_error", "afx_version", "afx_mesh_load", "afx_mesh_from_arrays", "afx_mesh_counts", "afx_mesh_get",
     "afx_mesh_get_int", "afx_mesh_boundary_name", "afx_mesh_free", "afx_config_create", "afx_config_from_ini",
     "afx_config_from_ini_string", "afx_config_set_double", "afx_config_get_double", "afx_config_set_string",
-    "afx_config_get_string", "afx_config_set_bc", "afx_config_bc_count", "afx_config_free", "afx_solver_create",
+    "afx_config_get_string", "afx_config_set_bc", "afx_config_bc_count", "afx_config_get_bc", "afx_config_free",
+    "afx_solver_create",
     "afx_solver_free", "afx_init_freestream", "afx_set_state", "afx_get_state", "afx_residual", "afx_iterate",
     "afx_run_to_convergence", "afx_residual_history", "afx_forces", "afx_set_farfield", "afx_request_stop",
     "afx_last_device_seconds", "afx_profile_iterations", "afx_kernel_name", "afx_autotune",
@@ -69,6 +70,7 @@ def lib():
         "afx_config_get_string": (i, [vp, cp, ctypes.c_char_p, i]),
         "afx_config_set_bc": (i, [vp, cp, cp, d, d, d, d]),
         "afx_config_bc_count": (i, [vp, P(i)]),
+        "afx_config_get_bc": (i, [vp, cp, ctypes.c_char_p, i, P(d), P(d), P(d), P(d)]),
         "afx_config_free": (None, [vp]),
         "afx_solver_create": (i, [vp, vp, P(vp)]),
         "afx_solver_free": (None, [vp]),

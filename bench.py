@@ -107,32 +107,61 @@ def _setup_gpu(precision, m, q0, variant="auto"):
     return g
 
 
-def algorithmic_bytes(kernel, n, f, precision):
-    """Compulsory HBM bytes of one launch of ``kernel`` (every array it
-    touches counted once).  w = bytes of the arithmetic type."""
+def stage_cell_bytes(precision, variant_reads):
+    """Per-cell bytes of the three RK stages' epilogues (average over the
+    stages): stage 1 reads nothing extra and writes dt + the next stage
+    state; stage 2 reads the FP32 shadow of q (FP64: q) + dt and writes the
+    next stage state; stage 3 reads the FP64 q + dt and writes q (+ the FP32
+    shadow).  ``variant_reads`` = the variant's own per-cell reads."""
     w = 8 if precision == "fp64" else 4
-    cell_vec = 4 * w
-    face_geo = 8 + 8 * w  # c0,c1 + n, (L,g), d0, d1
-    if kernel == "k_resid_gather":
-        # reads: cslot, area, qk, gx, gy, phi, q0 (FP64), dt; faces; writes next stage state
-        # (stage 2 writes the FP64 state + FP32 shadow: counted as the average over the 3 stages)
-        writes = (cell_vec + cell_vec + (32 + cell_vec)) / 3.0
-        return n * (16 + w + 4 * cell_vec + 32 + w + writes) + f * face_geo
+    cv = 4 * w
+    shadow_w = 0 if precision == "fp64" else cv
+    s0 = variant_reads + w + cv
+    s1 = variant_reads + cv + w + cv
+    s2 = variant_reads + 32 + w + 32 + shadow_w
+    return (s0 + s1 + s2) / 3.0
+
+
+def algorithmic_bytes(kernel, n, f, precision):
+    """Compulsory HBM bytes of one launch of ``kernel``: every array element
+    the launch must touch, counted once (neighbour re-reads are not counted).
+    w = bytes of the arithmetic type; a cell vector is 4w; a face record is
+    c0,c1 (8 B) + n, (L, g), d0, d1 (8w)."""
+    w = 8 if precision == "fp64" else 4
+    cv = 4 * w
+    face_geo = 8 + 8 * w
     if kernel == "k_resid_tile":
-        # faces once (40/72 B records), cell vectors q, gx, gy, phi of every cell once, per-cell tile
-        # slots (8), area, dt, FP64 q0, stage writes; tile lists are < 1% and not counted
-        writes = (cell_vec + cell_vec + (32 + cell_vec)) / 3.0
-        return n * (4 * cell_vec + 8 + w + w + 32 + writes) + f * face_geo
+        # q, gx, gy, phi of every cell, 4 x int16 tile slots, area; faces once
+        return n * stage_cell_bytes(precision, 4 * cv + 8 + w) + f * face_geo
+    if kernel == "k_resid_gather":
+        # q, gx, gy, phi, cslot + cnbr (32), area; face records without c0,c1
+        return n * stage_cell_bytes(precision, 4 * cv + 32 + w) + f * 8 * w
     if kernel == "k_face_flux":
-        return n * 4 * cell_vec + f * (face_geo + 4 * w)
+        # q, gx, gy, phi of every cell; face records; F*L written (+ eig*L in stage 1)
+        return n * 4 * cv + f * (face_geo + 4 * w + w / 3.0)
     if kernel == "k_cell_sum":
-        writes = (cell_vec + cell_vec + 32) / 3.0
-        return n * (16 + w + 32 + w + writes) + f * (8 + 4 * w)
+        # cslot + cnbr, area, F*L of every face (+ eig*L in stage 1), epilogue
+        return n * stage_cell_bytes(precision, 32 + w) + f * (4 * w + w / 3.0)
     if kernel == "k_prep":
-        return n * (16 + w + cell_vec + 3 * cell_vec + w) + f * face_geo
+        # q, cslot + cnbr, area; n, (L, g), d0, d1; writes gx, gy, phi (+dt for the gather variant)
+        return n * (cv + 32 + w + 3 * cv) + f * 8 * w
     if kernel == "k_limiter":
-        return n * (16 + w + 4 * cell_vec) + f * face_geo
+        # qk, gx, gy, cslot + cnbr, area; d0, d1; writes phi
+        return n * (4 * cv + 32 + w) + f * 4 * w
     return 0
+
+
+def measured_traffic(kernel, precision, n, f):
+    """DRAM bytes per launch of ``kernel`` from the committed ncu summary
+    (profiles/traffic.json: measured on a smaller channel, per cell and per
+    face), scaled to this launch's cells and faces; None if not recorded."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as fh:
+            t = json.load(fh)
+        e = t[precision][kernel]
+        return e["bytes_per_cell"] * n + e["bytes_per_face"] * f
+    except Exception:
+        return None
 
 
 def run_lean(args):
@@ -189,7 +218,8 @@ def run_gpu(args):
         entry = dict(value=evals, ms_per_step=sec / K * 1e3, steps=K, tuned=tuned,
                      kernels={k: dict(ms_total=v[0], launches=v[1], share=v[0] / tot) for k, v in prof.items()},
                      roofline=dict(kernel=kname, bound="hbm", achieved=achieved, peak=hbm_peak, unit="GB/s",
-                                   frac=achieved / hbm_peak, peak_source=peak_kind, traffic=None,
+                                   frac=achieved / hbm_peak, peak_source=peak_kind,
+                                   traffic=measured_traffic(kname, precision, N, F),
                                    algorithmic_bytes_per_launch=ab, launch_ms=per_launch_s * 1e3),
                      gpu_launches=int(round(launches_per_iter * K)))
         if precision == "fp32-mixed":
@@ -209,6 +239,92 @@ def run_gpu(args):
         result[precision] = entry
         del g
     return dict(N=N, F=F, setup_s=setup_s, res=result)
+
+
+def time_to_cl(budget_s=60.0):
+    """Time to C_L within 1e-6 on the 2-D airfoil case: NACA0012, M 0.5,
+    AoA 1.25 deg (0.01745 rad/deg), O-mesh 128 surface x 128 radial quads =
+    16,384 cells, far field 20 chords, explicit second-order scheme, CFL 1.5.
+    FP64 runs until C_L moves less than 1e-10 between 5000-iteration samples:
+    that C_L is the reference.  FP32-mixed C_L, once the FP32 residual floor
+    is reached, random-walks by ~1e-6, so its C_L is the mean of the last 10
+    samples taken every 1000 iterations; its time-to-C_L is the first time
+    that mean is within 1e-6 of the FP64 value and stays so to the end of
+    the run.  Times are device seconds (CUDA events) of the iterations;
+    force evaluations between samples are not counted."""
+    from aeroflex_gb300 import meshgen, rans
+
+    m = rans.mesh.from_arrays(meshgen.airfoil_omesh(128, 128, split=False))
+
+    def solver(prec):
+        st = rans.Settings().set("solver", "explicit").set("precision", prec).set("start_cfl", 1.5)
+        st.set_bc("farfield", "farfield", 1.0, 0.5, 1.25 * 0.01745, 1.0).set_bc("wall", "slip-wall")
+        s = rans.Solver(m, st)
+        s.init()
+        return s
+
+    t_start = time.time()
+    s = solver("fp64")
+    samples, dev, last, its = [], 0.0, None, 0
+    while its < 200000 and time.time() - t_start < budget_s:
+        s.iterate(5000)
+        its += 5000
+        dev += s.last_device_seconds()
+        cl = rans.get_wall_profile(s, "wall")["cl"]
+        samples.append((its, dev, cl))
+        if last is not None and abs(cl - last) < 1e-10:
+            break
+        last = cl
+    cl64 = samples[-1][2]
+    hit64 = next((x for i, x in enumerate(samples) if all(abs(y[2] - cl64) < 1e-6 for y in samples[i:])), None)
+    cd64 = rans.get_wall_profile(s, "wall")["cd"]
+    del s
+    s = solver("fp32-mixed")
+    fs, dev, its = [], 0.0, 0
+    t1 = time.time()
+    while its < 200000 and time.time() - t1 < budget_s / 2:
+        s.iterate(1000)
+        its += 1000
+        dev += s.last_device_seconds()
+        w = rans.get_wall_profile(s, "wall")
+        fs.append((its, dev, w["cl"], w["cd"]))
+    means = [(fs[i][0], fs[i][1], float(np.mean([x[2] for x in fs[max(0, i - 9):i + 1]]))) for i in range(len(fs))]
+    hit32 = next((x for i, x in enumerate(means) if i >= 9 and all(abs(y[2] - cl64) < 1e-6 for y in means[i:])), None)
+    del s
+    # FP32-mixed with the FP64 finish: run_to_convergence in 1000-iteration
+    # calls (the FP32 -> FP64 switch persists across calls)
+    st = rans.Settings().set("solver", "explicit").set("precision", "fp32-mixed").set("start_cfl", 1.5)
+    st.set("fp64_finish", 1)
+    st.set_bc("farfield", "farfield", 1.0, 0.5, 1.25 * 0.01745, 1.0).set_bc("wall", "slip-wall")
+    s = rans.Solver(m, st)
+    s.init()
+    ff, dev, its = [], 0.0, 0
+    t2 = time.time()
+    while its < 200000 and time.time() - t2 < budget_s / 2:
+        n_it, _ = s.run_solver(1e-14, 1000)
+        its += n_it
+        dev += s.last_device_seconds()
+        ff.append((its, dev, rans.get_wall_profile(s, "wall")["cl"]))
+        if its >= 20000 and abs(ff[-1][2] - cl64) < 1e-8:
+            break
+    hitf = next((x for i, x in enumerate(ff) if all(abs(y[2] - cl64) < 1e-6 for y in ff[i:])), None)
+    out = {"case": "NACA0012 O-mesh 128x128 quads (16,384 cells), M 0.5, AoA 1.25 deg, CFL 1.5",
+           "fp64": {"cl": cl64, "cd": cd64, "iterations": samples[-1][0],
+                    "time_to_cl_1e-6_s": None if hit64 is None else hit64[1],
+                    "iterations_to_cl_1e-6": None if hit64 is None else hit64[0]},
+           "fp32_mixed": {"cl_window_mean": means[-1][2], "cl_error": abs(means[-1][2] - cl64),
+                          "cl_last_sample_error": abs(fs[-1][2] - cl64), "cd_error": abs(fs[-1][3] - cd64),
+                          "iterations": fs[-1][0],
+                          "time_to_cl_1e-6_s": None if hit32 is None else hit32[1],
+                          "iterations_to_cl_1e-6": None if hit32 is None else hit32[0]}}
+    out["fp32_mixed_fp64_finish"] = {"cl": ff[-1][2], "cl_error": abs(ff[-1][2] - cl64), "iterations": ff[-1][0],
+                                     "time_to_cl_1e-6_s": None if hitf is None else hitf[1],
+                                     "iterations_to_cl_1e-6": None if hitf is None else hitf[0]}
+    if hit64 and hit32:
+        out["speedup_time_to_cl_fp32_mixed"] = hit64[1] / hit32[1]
+    if hit64 and hitf:
+        out["speedup_time_to_cl_fp32_mixed_fp64_finish"] = hit64[1] / hitf[1]
+    return out
 
 
 def cpu_baseline(budget_s=12.0):
@@ -268,6 +384,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-cl", action="store_true", help="skip the time-to-C_L leg")
     ap.add_argument("--nx", type=int, default=NX)
     ap.add_argument("--ny", type=int, default=NY)
     ap.add_argument("--lean", action="store_true", help="warm-up + timed iterations only (for ncu)")
@@ -328,6 +445,8 @@ def main():
     }
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline()
+    if not args.no_cl:
+        line["time_to_cl"] = time_to_cl()
     print(json.dumps(line))
 
 

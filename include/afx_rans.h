@@ -2,7 +2,7 @@
  * afx_rans.h — C ABI of the GB300 rans residual library (libafx_rans.so).
  *
  * Drop-in boundary for AeroFLEX's `rans` module (header-only C++ in the
- * reference: src/rans/include/rans/*.h).  Each entry point names the
+ * reference: the headers of src/rans/include/rans/).  Each entry point names the
  * reference interface it replaces.  Plain C types only: opaque handles,
  * pointers and sizes.  State arrays cross the boundary in the reference's
  * layout: AoS [rho, rhou, rhov, rhoE] per REAL cell, cells in the order the
@@ -77,19 +77,27 @@ int afx_config_from_ini(const char* path, afx_config* out);
 int afx_config_from_ini_string(const char* text, afx_config* out);
 /* Numeric fields: gamma, R, mu_L, Pr_L, Pr_T, start_cfl, slope_cfl, max_cfl,
  * relaxation, tolerance, limiter_k, alpha_start, alpha_end, alpha_step,
- * rhs_iterations, max_iterations, second_order (0/1). */
+ * rhs_iterations, max_iterations, second_order (0/1); this library's
+ * block_size (0 auto | 32 | 64 | 128 | 256), fp64_correction_interval
+ * (FP32-mixed: refresh an FP64 defect correction every n iterations, 0 off)
+ * and fp64_finish (FP32-mixed: afx_run_to_convergence continues with FP64
+ * iterations once the FP32 residual stops falling, 0/1). */
 int afx_config_set_double(afx_config c, const char* key, double v);
 int afx_config_get_double(afx_config c, const char* key, double* v);
 /* String fields: solver ("explicit"/"implicit"), gradient ("green-gauss"/
  * "least-squares"), viscosity ("inviscid"/"laminar"/"spalart-allmaras"/
  * "spallart-allmaras"), limiter ("venkatakrishnan"/"michalak"),
- * precision ("fp64"/"fp32-mixed"), airfoil_name. */
+ * precision ("fp64"/"fp32-mixed"), kernel_variant ("auto"/"gather"/"face"/
+ * "tile"), airfoil_name. */
 int afx_config_set_string(afx_config c, const char* key, const char* v);
 int afx_config_get_string(afx_config c, const char* key, char* out, int cap);
 /* One [rans-bc] entry (core.h:244-255): type "farfield"/"slip-wall"/"wall". */
 int afx_config_set_bc(afx_config c, const char* name, const char* type, double T, double mach, double angle,
                       double p);
 int afx_config_bc_count(afx_config c, int* n);
+/* Read one [rans-bc] entry back (Settings::bcs[name], core.h:171). */
+int afx_config_get_bc(afx_config c, const char* name, char* type, int cap, double* T, double* mach, double* angle,
+                      double* p);
 void afx_config_free(afx_config c);
 
 /* ----------------------------------------------------------- solver ---- */

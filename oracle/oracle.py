@@ -63,12 +63,26 @@ def lib():
         L.orc_time_iterations.argtypes = [vp, ip]
         L.orc_time_residuals.restype = ctypes.c_double
         L.orc_time_residuals.argtypes = [vp, ip]
+        d = ctypes.c_double
+        L.orc_face_flux.argtypes = [d, ip, ip, d, d, vp, vp, vp, vp, vp]
         _lib = L
     return _lib
 
 
 def _ptr(a):
     return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def face_flux(qL, qR, nx, ny, gamma=1.4, visc=0, bc="internal", gx=None, gy=None):
+    """One restated face flux F (physics.h:160-530), not multiplied by length."""
+    qL = np.ascontiguousarray(qL, np.float64)
+    qR = np.ascontiguousarray(qR, np.float64)
+    gx = np.zeros(4) if gx is None else np.ascontiguousarray(gx, np.float64)
+    gy = np.zeros(4) if gy is None else np.ascontiguousarray(gy, np.float64)
+    f = np.empty(4)
+    t = 0 if bc == "internal" else BC_TYPES[bc]
+    lib().orc_face_flux(gamma, visc, t, nx, ny, _ptr(qL), _ptr(qR), _ptr(gx), _ptr(gy), _ptr(f))
+    return f
 
 
 class Mesh:

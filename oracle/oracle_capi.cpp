@@ -291,6 +291,24 @@ int orc_wall_profile(void* sp, const char* patch, double* clcdcm, double* cp_out
     }
 }
 
+// One face flux of the restated functors (physics.h:160-530): type 0 is the
+// internal flux (with face gradients gx, gy for the laminar term), types
+// 1-3 the farfield / slip-wall / wall functors with qR the stored boundary
+// state.
+void orc_face_flux(double gamma, int visc, int type, double nx, double ny, const double* qL, const double* qR,
+                   const double* gx, const double* gy, double* f) {
+    Gas g;
+    g.gamma = gamma;
+    if (type == BC_INTERNAL) {
+        internal_flux(g, nx, ny, visc, qL, qR, gx, gy, f);
+    } else {
+        double qb[4];
+        const double zero[4] = {0, 0, 0, 0};
+        boundary_state(g, type, nx, ny, qL, qR, qb);
+        internal_flux(g, nx, ny, visc, qL, qb, zero, zero, f);
+    }
+}
+
 // Wall-clock seconds of n explicit iterations (the CPU baseline leg).
 double orc_time_iterations(void* sp, int n) {
     auto* s = (ExplicitSolver*)sp;

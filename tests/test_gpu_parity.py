@@ -188,6 +188,42 @@ def test_fp32_mixed_variants_agree(afx):
     assert rel_l2(out[0], out[2]) < 1e-6
 
 
+def test_fp32_defect_correction_tracks_fp64(afx, orc):
+    # after a refresh at the start of the run the corrected FP32 residual is
+    # R64 up to FP32 rounding of the correction: the first iteration matches
+    # the FP64 oracle to ~1e-7 of the state update, closer than pure FP32
+    m, bcs = omesh_case(48, 24)
+    so = oracle_solver(orc, m, bcs)
+    so.init()
+    so.iterate(20)
+    q = so.q()
+    so.iterate(1)
+    ref = so.q()
+    errs = []
+    for corr in (0, 50):
+        g = gpu_solver(afx, m, bcs, precision="fp32-mixed", fp64_correction_interval=corr)
+        g.init()
+        g.set_q(q)
+        g.iterate(1)
+        errs.append(rel_l2(g.get_q() - q, ref - q))
+    assert errs[1] < errs[0] and errs[1] < 1e-4, errs
+
+
+def test_fp64_finish_switches_and_converges(afx):
+    # FP32-mixed run_to_convergence with the FP64 finish ends below what the
+    # FP32 residual alone can reach, and its last iterations are FP64 ones
+    m = __import__("aeroflex_gb300.meshgen", fromlist=["x"]).airfoil_omesh(32, 32, split=False)
+    bcs = {"farfield": dict(type="farfield", T=1.0, mach=0.5, angle=1.25 * 0.01745, p=1.0),
+           "wall": dict(type="slip-wall")}
+    errs = []
+    for fin in (0, 1):
+        g = gpu_solver(afx, m, bcs, precision="fp32-mixed", cfl=1.5, fp64_finish=fin)
+        g.init()
+        it, err = g.run_solver(1e-11, 60000)
+        errs.append(err)
+    assert errs[1] < 1e-2 * errs[0], errs
+
+
 def test_nonfinite_flagged(afx):
     m, bcs = omesh_case(32, 16)
     g = gpu_solver(afx, m, bcs, cfl=1e6)
