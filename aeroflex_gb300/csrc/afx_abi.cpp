@@ -358,6 +358,10 @@ struct afx_solver_s {
         h_ctrl->max_it = max_it;
         h_ctrl->tol = tol;
         AFX_CUDA(cudaMemcpyAsync(a.ctrl, h_ctrl, sizeof(Ctrl), cudaMemcpyHostToDevice, stream));
+        if (a.n_cases > 0) {  // every case of a batch starts the run afresh
+            AFX_CUDA(cudaMemsetAsync(a.cctrl, 0, a.n_cases * sizeof(CaseCtrl), stream));
+            AFX_CUDA(cudaMemsetAsync(a.case_done, 0, a.n_cases * sizeof(int), stream));
+        }
     }
 
     void read_ctrl() {
@@ -426,7 +430,8 @@ struct afx_solver_s {
         iters_total += done;
         if (phase64 && done > 0) shadow_stale = true;
         parity = p0 ^ (done & 1);
-        if (done > 0) pending_last = parity ^ 1;
+        // a batch keeps each case's last-stage qW in Rq as it goes
+        if (done > 0 && a.n_cases == 0) pending_last = parity ^ 1;
         (void)tol;
         if (stopped) stop.store(0);
         return stopped ? -done - 1 : done;
@@ -723,19 +728,20 @@ int afx_config_get_bc(afx_config c, const char* name, char* type, int cap, doubl
 void afx_config_free(afx_config c) { delete c; }
 
 // ---------------------------------------------------------------- solver
-int afx_solver_create(afx_mesh mp, afx_config cp, afx_solver* out) {
-    return guarded([&] {
-        if (!mp || !cp || !out) throw Error(AFX_ERR_ARG, "null argument");
+}  // extern "C"
+
+// The device solver of one mesh (a single case, or the union of a batch's
+// cases) with settings `st`.
+static std::unique_ptr<afx_solver_s> make_solver(const HostMesh& m, const DeviceLayout& L, const Settings& st0) {
+    {
         int ndev = 0;
         if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
             throw Error(AFX_ERR_CUDA, "no CUDA device available");
         auto s = std::make_unique<afx_solver_s>();
-        s->st = cp->s;
+        s->st = st0;
         if (s->st.viscosity_code() == VISC_SA)
             throw Error(AFX_ERR_CONFIG, "spalart-allmaras is not available in this build");
-        const DeviceLayout& L = mp->layout();
         {
-            const HostMesh& m = mp->m;
             for (size_t b = 0; b < m.boundaryEdges.size(); ++b) {
                 const uint32_t e = m.boundaryEdges[b];
                 s->bedges.push_back({m.boundaryEdgesPhysicals[b], L.cell_new[m.edgesCells[e][0]], m.edgesCentersX[e],
@@ -869,7 +875,16 @@ int afx_solver_create(afx_mesh mp, afx_config cp, afx_solver* out) {
         s->h_stage_bytes = N * 32;
         s->refill_bcs();
         AFX_CUDA(cudaStreamSynchronize(s->stream));
-        *out = s.release();
+        return s;
+    }
+}
+
+extern "C" {
+
+int afx_solver_create(afx_mesh mp, afx_config cp, afx_solver* out) {
+    return guarded([&] {
+        if (!mp || !cp || !out) throw Error(AFX_ERR_ARG, "null argument");
+        *out = make_solver(mp->m, mp->layout(), cp->s).release();
     });
 }
 
@@ -978,9 +993,11 @@ int afx_residual_history(afx_solver s, double* out, int cap, int* n) {
     });
 }
 
-int afx_forces(afx_solver s, const char* patch, double* cl, double* cd, double* cm, double* cp, int cap, int* n_cp) {
-    return guarded([&] {
-        if (!s || !patch) throw Error(AFX_ERR_ARG, "null argument");
+// get_wall_profile (post.h:301-387) over the boundary edges named `patch`,
+// with the freestream `vf`.
+static void forces_impl(afx_solver_s* s, const std::string& patch, const FarfieldVars& vf, double* cl, double* cd,
+                        double* cm, double* cp, int cap, int* n_cp) {
+    {
         auto& pf = s->patches[patch];
         if (!pf) {
             pf.reset(new afx_solver_s::PatchForces());
@@ -1003,7 +1020,10 @@ int afx_forces(afx_solver s, const char* patch, double* cl, double* cd, double* 
                 cells.push_back(be.owner_dev);
                 geo.insert(geo.end(), {be.ex, be.ey, be.nx, be.ny, be.L});
             }
-            if (n_added == 0) throw Error(AFX_ERR_ARG, std::string("no boundary edges on patch '") + patch + "'");
+            if (n_added == 0) {
+                s->patches.erase(patch);
+                throw Error(AFX_ERR_ARG, "no boundary edges on patch '" + patch + "'");
+            }
             pf->y_moment /= (double)n_added;
             pf->x_moment = (pf->xmax - pf->xmin) * 0.25 + pf->xmin;
             pf->n = (int)n_added;
@@ -1012,7 +1032,6 @@ int afx_forces(afx_solver s, const char* patch, double* cl, double* cd, double* 
             pf->cp.alloc(n_added * 8);
             pf->sums.alloc(3 * 8);
         }
-        const FarfieldVars vf = s->freestream();
         ForceArgs f;
         f.n = pf->n;
         f.cell = (const int*)pf->cell.p;
@@ -1040,6 +1059,13 @@ int afx_forces(afx_solver s, const char* patch, double* cl, double* cd, double* 
         if (n_cp) *n_cp = pf->n;
         if (cp)
             for (int i = 0; i < pf->n && i < cap; ++i) cp[i] = cph[i];
+    }
+}
+
+int afx_forces(afx_solver s, const char* patch, double* cl, double* cd, double* cm, double* cp, int cap, int* n_cp) {
+    return guarded([&] {
+        if (!s || !patch) throw Error(AFX_ERR_ARG, "null argument");
+        forces_impl(s, patch, s->freestream(), cl, cd, cm, cp, cap, n_cp);
     });
 }
 
@@ -1096,8 +1122,11 @@ int afx_profile_iterations(afx_solver s, int n_iters, double* ms, int* launches,
     });
 }
 
-int afx_autotune(afx_solver s, int iters, char* variant, int cap, int* block, double* ms_per_iter) {
-    return guarded([&] {
+// Times every residual variant x block size over `iters` iterations from the
+// current state and keeps the fastest; the state (and a batch's qW) is put
+// back afterwards.
+static void autotune_impl(afx_solver_s* s, int iters, char* variant, int cap, int* block, double* ms_per_iter) {
+    {
         if (!s || iters <= 0) throw Error(AFX_ERR_ARG, "bad argument");
         StepArgs& a = s->a;
         const size_t N = a.n_cells;
@@ -1105,9 +1134,13 @@ int afx_autotune(afx_solver s, int iters, char* variant, int cap, int* block, do
         s->materialize_qW();
         s->ensure_shadow();
         // keep the state: the timing runs start from it and it is put back after
-        DevBuf save;
+        DevBuf save, saveR;
         save.alloc(N * 32);
         AFX_CUDA(cudaMemcpyAsync(save.p, a.qm[s->parity], N * 32, cudaMemcpyDeviceToDevice, s->stream));
+        if (a.n_cases > 0) {  // a batch's iterations write qW
+            saveR.alloc(N * 32);
+            AFX_CUDA(cudaMemcpyAsync(saveR.p, a.Rq, N * 32, cudaMemcpyDeviceToDevice, s->stream));
+        }
         const int p0 = s->parity;
         cudaEvent_t e0, e1;
         AFX_CUDA(cudaEventCreate(&e0));
@@ -1146,6 +1179,7 @@ int afx_autotune(afx_solver s, int iters, char* variant, int cap, int* block, do
         for (auto& g : s->graphs) cudaGraphExecDestroy(g.second);
         s->graphs.clear();
         AFX_CUDA(cudaMemcpyAsync(a.qm[p0], save.p, N * 32, cudaMemcpyDeviceToDevice, s->stream));
+        if (a.n_cases > 0) AFX_CUDA(cudaMemcpyAsync(a.Rq, saveR.p, N * 32, cudaMemcpyDeviceToDevice, s->stream));
         s->sync_shadow(p0);
         s->set_ctrl(0, 0, 0);
         AFX_CUDA(cudaStreamSynchronize(s->stream));
@@ -1155,7 +1189,11 @@ int afx_autotune(afx_solver s, int iters, char* variant, int cap, int* block, do
         if (variant && cap > 0) std::snprintf(variant, cap, "%s", vnames[best_var]);
         if (block) *block = best_block;
         if (ms_per_iter) *ms_per_iter = best / iters;
-    });
+    }
+}
+
+int afx_autotune(afx_solver s, int iters, char* variant, int cap, int* block, double* ms_per_iter) {
+    return guarded([&] { autotune_impl(s, iters, variant, cap, block, ms_per_iter); });
 }
 
 const char* afx_kernel_name(int k) {
@@ -1190,6 +1228,286 @@ int afx_residual_noalloc(afx_solver s, const double* q_dev, double* R_dev, long 
         s->set_ctrl(0, 0, 0);
         AFX_CUDA(noalloc_residual_f64(s->a, (const int*)s->d_cell_old.p, q_dev, R_dev, s->stream));
         AFX_CUDA(cudaStreamSynchronize(s->stream));
+    });
+}
+
+// ------------------------------------------------------------------ batch
+// A batch is one device solver over the union of its cases' meshes: the
+// meshes share no node, so every face, gradient and limiter stencil stays
+// within its case, and one launch per kernel advances all cases.  Each
+// case's cells are a contiguous device range (case_off); boundary patches are
+// renamed "<case>/<patch>" inside the union.
+}  // extern "C"
+
+struct afx_batch_s {
+    std::unique_ptr<afx_solver_s> s;
+    int n = 0;
+    std::vector<int> cell_off;  // reference-order (== device-order) cell range of each case
+    std::vector<int> bnd_off;   // boundary-edge range of each case
+    std::vector<FarfieldVars> far;  // freestream of each case (solver.h:597-611 per case)
+    std::vector<std::vector<std::string>> patch_names;
+    std::vector<CaseCtrl> h_cctrl;
+    DevBuf case_of, case_off, case_done, cell_sq, cctrl, chist, qfar;
+
+    // per-case freestream from the case's own boundaries; uploaded as state
+    void set_freestream() {
+        far.assign(n, FarfieldVars());
+        for (int c = 0; c < n; ++c)
+            for (int b = bnd_off[c]; b < bnd_off[c + 1]; ++b)
+                if (s->boundary_type[b] == BC_FARFIELD || s->boundary_type[b] == BC_INLET_OUTLET) {
+                    far[c] = s->boundary_vars[b];
+                    break;
+                }
+        std::vector<double> q(4 * (size_t)n);
+        for (int c = 0; c < n; ++c) conservative(s->st, far[c], &q[4 * c]);
+        AFX_CUDA(cudaMemcpyAsync(qfar.p, q.data(), q.size() * 8, cudaMemcpyHostToDevice, s->stream));
+        AFX_CUDA(cudaStreamSynchronize(s->stream));
+    }
+    void read_cases() {
+        h_cctrl.resize(n);
+        AFX_CUDA(cudaMemcpyAsync(h_cctrl.data(), s->a.cctrl, n * sizeof(CaseCtrl), cudaMemcpyDeviceToHost,
+                                 s->stream));
+        AFX_CUDA(cudaStreamSynchronize(s->stream));
+    }
+    void check_case(int c) const {
+        if (c < 0 || c >= n) throw Error(AFX_ERR_ARG, "case index out of range");
+    }
+};
+
+extern "C" {
+
+int afx_batch_create(int n_cases, const afx_mesh* meshes, const afx_config* configs, afx_batch* out) {
+    return guarded([&] {
+        if (n_cases <= 0 || !meshes || !configs || !out) throw Error(AFX_ERR_ARG, "bad argument");
+        if (n_cases > 65535) throw Error(AFX_ERR_ARG, "at most 65535 cases in a batch");
+        auto b = std::make_unique<afx_batch_s>();
+        b->n = n_cases;
+        // the scheme is shared: every case must agree with case 0 on it
+        const Settings& s0 = configs[0] ? configs[0]->s : throw Error(AFX_ERR_ARG, "null config");
+        Settings st = s0;
+        st.bcs.clear();
+        st.bc_order.clear();
+        if (st.fp64_correction_interval > 0 || st.fp64_finish)
+            throw Error(AFX_ERR_CONFIG, "fp64_correction_interval and fp64_finish are single-case options");
+        HostMesh u;
+        b->cell_off.push_back(0);
+        b->bnd_off.push_back(0);
+        b->patch_names.resize(n_cases);
+        for (int c = 0; c < n_cases; ++c) {
+            if (!meshes[c] || !configs[c]) throw Error(AFX_ERR_ARG, "null mesh or config");
+            const Settings& sc = configs[c]->s;
+            if (sc.gamma != s0.gamma || sc.R != s0.R || sc.mu_L != s0.mu_L || sc.Pr_L != s0.Pr_L ||
+                sc.viscosity != s0.viscosity || sc.gradient != s0.gradient || sc.limiter != s0.limiter ||
+                sc.precision != s0.precision || sc.second_order != s0.second_order ||
+                sc.start_cfl != s0.start_cfl || sc.relaxation != s0.relaxation || sc.limiter_k != s0.limiter_k)
+                throw Error(AFX_ERR_CONFIG, "case " + std::to_string(c) +
+                                                ": the scheme settings of a batch must match case 0's (only the "
+                                                "mesh and the boundary conditions vary per case)");
+            const HostMesh& m = meshes[c]->m;
+            const uint32_t node0 = (uint32_t)u.nodesX.size();
+            u.nodesX.insert(u.nodesX.end(), m.nodesX.begin(), m.nodesX.end());
+            u.nodesY.insert(u.nodesY.end(), m.nodesY.begin(), m.nodesY.end());
+            for (uint32_t i = 0; i < m.nRealCells; ++i) {
+                auto cn = m.cellsNodes[i];
+                const int k = m.cellsIsTriangle[i] ? 3 : 4;
+                for (int j = 0; j < k; ++j) cn[j] += node0;
+                u.cellsNodes.push_back(cn);
+                u.cellsIsTriangle.push_back(m.cellsIsTriangle[i]);
+            }
+            const std::string pre = std::to_string(c) + "/";
+            for (size_t e = 0; e < m.bnd0.size(); ++e) {
+                u.bnd0.push_back(m.bnd0[e] + node0);
+                u.bnd1.push_back(m.bnd1[e] + node0);
+                u.bndName.push_back(pre + m.bndName[e]);
+            }
+            for (const auto& kv : sc.bcs) {
+                st.bcs[pre + kv.first] = kv.second;
+                b->patch_names[c].push_back(kv.first);
+            }
+            b->cell_off.push_back((int)u.cellsNodes.size());
+            b->bnd_off.push_back((int)u.bnd0.size());
+        }
+        u.finalize();
+        u.segments = b->cell_off;
+        const DeviceLayout L = build_layout(u);
+        b->s = make_solver(u, L, st);
+        afx_solver_s& s = *b->s;
+        // the union's boundary edges keep the cases' order: case c's are
+        // bnd_off[c]..bnd_off[c+1]
+        std::vector<int> cof(u.nRealCells);
+        for (int c = 0; c < n_cases; ++c)
+            for (int i = b->cell_off[c]; i < b->cell_off[c + 1]; ++i) cof[L.cell_new[i]] = c;
+        for (int c = 0; c < n_cases; ++c)
+            for (int i = b->cell_off[c]; i < b->cell_off[c + 1]; ++i)
+                if (cof[i] != c) throw Error(AFX_ERR_MESH, "batch layout: a case's cells are not contiguous");
+        b->case_of.upload(cof.data(), cof.size() * sizeof(int), s.stream);
+        b->case_off.upload(b->cell_off.data(), b->cell_off.size() * sizeof(int), s.stream);
+        b->case_done.alloc(n_cases * sizeof(int));
+        b->cell_sq.alloc(u.nRealCells * sizeof(double));
+        b->cctrl.alloc(n_cases * sizeof(CaseCtrl));
+        b->chist.alloc((size_t)n_cases * CASE_HIST_CAP * sizeof(double));
+        b->qfar.alloc(4 * (size_t)n_cases * sizeof(double));
+        StepArgs& a = s.a;
+        a.n_cases = n_cases;
+        a.case_of = (const int*)b->case_of.p;
+        a.case_off = (const int*)b->case_off.p;
+        a.case_done = (int*)b->case_done.p;
+        a.cell_sq = (double*)b->cell_sq.p;
+        a.cctrl = (CaseCtrl*)b->cctrl.p;
+        a.chist = (double*)b->chist.p;
+        a.qfar_case = (const double*)b->qfar.p;
+        AFX_CUDA(cudaMemsetAsync(b->cell_sq.p, 0, u.nRealCells * sizeof(double), s.stream));
+        s.set_ctrl(0, 0, 0);
+        b->set_freestream();
+        *out = b.release();
+    });
+}
+
+void afx_batch_free(afx_batch b) { delete b; }
+
+int afx_batch_counts(afx_batch b, int* n_cases, long long* n_cells_total) {
+    return guarded([&] {
+        if (!b) throw Error(AFX_ERR_ARG, "null argument");
+        if (n_cases) *n_cases = b->n;
+        if (n_cells_total) *n_cells_total = b->s->a.n_cells;
+    });
+}
+
+int afx_batch_init_freestream(afx_batch b) {
+    return guarded([&] {
+        if (!b) throw Error(AFX_ERR_ARG, "null argument");
+        afx_solver_s& s = *b->s;
+        for (int c = 0; c < b->n; ++c) {
+            double q[4];
+            conservative(s.st, b->far[c], q);  // init(), solver.h:615-631, per case
+            for (int i = b->cell_off[c]; i < b->cell_off[c + 1]; ++i) std::memcpy(s.h_stage + 4 * (size_t)i, q, 32);
+        }
+        // cases are contiguous device ranges in the same order: no permutation
+        // is needed for a per-case uniform state
+        AFX_CUDA(cudaMemcpyAsync(s.a.qm[s.parity], s.h_stage, (size_t)s.a.n_cells * 32, cudaMemcpyHostToDevice,
+                                 s.stream));
+        s.sync_shadow(s.parity);
+        AFX_CUDA(cudaStreamSynchronize(s.stream));
+    });
+}
+
+int afx_batch_set_state(afx_batch b, int c, const double* q, long long n) {
+    return guarded([&] {
+        if (!b || !q) throw Error(AFX_ERR_ARG, "null argument");
+        b->check_case(c);
+        afx_solver_s& s = *b->s;
+        const size_t N = s.a.n_cells, c0 = b->cell_off[c], nc = b->cell_off[c + 1] - c0;
+        if (n != (long long)(4 * nc)) throw Error(AFX_ERR_ARG, "state size must be 4*n_real_cells of the case");
+        // whole state out in reference order, the case's slice replaced, back in
+        enqueue_permute_out((int)N, (const int*)s.d_cell_old.p, s.a.qm[s.parity], s.d_stage.p, s.stream);
+        AFX_CUDA(cudaMemcpyAsync((double*)s.d_stage.p + 4 * c0, q, nc * 32, cudaMemcpyDefault, s.stream));
+        enqueue_permute_in((int)N, (const int*)s.d_cell_old.p, s.d_stage.p, s.a.qm[s.parity], s.stream);
+        s.sync_shadow(s.parity);
+        AFX_CUDA(cudaStreamSynchronize(s.stream));
+    });
+}
+
+int afx_batch_get_state(afx_batch b, int c, double* q, long long n) {
+    return guarded([&] {
+        if (!b || !q) throw Error(AFX_ERR_ARG, "null argument");
+        b->check_case(c);
+        afx_solver_s& s = *b->s;
+        const size_t N = s.a.n_cells, c0 = b->cell_off[c], nc = b->cell_off[c + 1] - c0;
+        if (n != (long long)(4 * nc)) throw Error(AFX_ERR_ARG, "state size must be 4*n_real_cells of the case");
+        enqueue_permute_out((int)N, (const int*)s.d_cell_old.p, s.a.qm[s.parity], s.d_stage.p, s.stream);
+        AFX_CUDA(cudaMemcpyAsync(q, (const double*)s.d_stage.p + 4 * c0, nc * 32, cudaMemcpyDefault, s.stream));
+        AFX_CUDA(cudaStreamSynchronize(s.stream));
+    });
+}
+
+int afx_batch_iterate(afx_batch b, int n_iters, double* res_norms) {
+    return guarded([&] {
+        if (!b || n_iters < 0) throw Error(AFX_ERR_ARG, "bad argument");
+        afx_solver_s& s = *b->s;
+        s.set_ctrl(0, n_iters, 0);
+        const int done = s.run(n_iters, 0, 0);
+        AFX_CUDA(cudaGetLastError());
+        b->read_cases();
+        bool bad = false;
+        for (int c = 0; c < b->n; ++c) {
+            if (res_norms) res_norms[c] = b->h_cctrl[c].last_norm;
+            bad |= b->h_cctrl[c].status == 4;
+        }
+        if (bad) throw Error(AFX_ERR_NONFINITE, "residual norm is not finite in at least one case");
+        if (done < 0) throw Error(AFX_ERR_STOPPED, "stopped by request");
+    });
+}
+
+int afx_batch_run_to_convergence(afx_batch b, double tol, int max_it, int* iters, double* errs, int* status) {
+    return guarded([&] {
+        if (!b) throw Error(AFX_ERR_ARG, "null argument");
+        afx_solver_s& s = *b->s;
+        if (tol <= 0) tol = s.st.tolerance;
+        if (max_it <= 0) max_it = s.st.max_iterations;
+        s.set_ctrl(1, max_it, tol);
+        // get_uniform_residual per case: each cell's case freestream
+        double qf[4] = {0, 0, 0, 0};
+        if (s.fp64) enqueue_uniform_f64(s.a, s.parity, qf, s.stream);
+        else enqueue_uniform_f32(s.a, s.parity, qf, s.stream);
+        const int done = s.run(max_it, 1, tol);
+        AFX_CUDA(cudaGetLastError());
+        b->read_cases();
+        for (int c = 0; c < b->n; ++c) {
+            if (iters) iters[c] = b->h_cctrl[c].iter;
+            if (errs) errs[c] = b->h_cctrl[c].err;
+            if (status) status[c] = b->h_cctrl[c].status == 4 ? AFX_ERR_NONFINITE : AFX_OK;
+        }
+        if (done < 0) throw Error(AFX_ERR_STOPPED, "stopped by request");
+    });
+}
+
+int afx_batch_case_history(afx_batch b, int c, double* out, int cap, int* n) {
+    return guarded([&] {
+        if (!b || !n) throw Error(AFX_ERR_ARG, "null argument");
+        b->check_case(c);
+        b->read_cases();
+        const int k = std::min(b->h_cctrl[c].hist_n, CASE_HIST_CAP);
+        *n = k;
+        if (out && cap > 0 && k > 0)
+            AFX_CUDA(cudaMemcpy(out, b->s->a.chist + (size_t)c * CASE_HIST_CAP, std::min(k, cap) * 8,
+                                cudaMemcpyDeviceToHost));
+    });
+}
+
+int afx_batch_forces(afx_batch b, int c, const char* patch, double* cl, double* cd, double* cm) {
+    return guarded([&] {
+        if (!b || !patch) throw Error(AFX_ERR_ARG, "null argument");
+        b->check_case(c);
+        forces_impl(b->s.get(), std::to_string(c) + "/" + patch, b->far[c], cl, cd, cm, nullptr, 0, nullptr);
+    });
+}
+
+int afx_batch_set_farfield(afx_batch b, int c, const char* patch, double mach, double angle, double T, double p) {
+    return guarded([&] {
+        if (!b || !patch) throw Error(AFX_ERR_ARG, "null argument");
+        b->check_case(c);
+        afx_solver_s& s = *b->s;
+        auto it = s.st.bcs.find(std::to_string(c) + "/" + patch);
+        if (it == s.st.bcs.end() || it->second.type != "farfield")
+            throw Error(AFX_ERR_ARG, std::string("no farfield patch '") + patch + "' in case " + std::to_string(c));
+        it->second.vars = FarfieldVars{mach, angle, T, p};
+        s.set_bcs();
+        s.refill_bcs();
+        b->set_freestream();
+    });
+}
+
+int afx_batch_autotune(afx_batch b, int iters, char* variant, int cap, int* block, double* ms_per_iter) {
+    return guarded([&] {
+        if (!b) throw Error(AFX_ERR_ARG, "null argument");
+        autotune_impl(b->s.get(), iters, variant, cap, block, ms_per_iter);
+    });
+}
+
+int afx_batch_last_device_seconds(afx_batch b, double* sec) {
+    return guarded([&] {
+        if (!b || !sec) throw Error(AFX_ERR_ARG, "null argument");
+        *sec = b->s->last_sec;
     });
 }
 

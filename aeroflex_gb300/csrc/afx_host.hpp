@@ -80,6 +80,9 @@ struct HostMesh {
     std::vector<std::string> boundaryEdgesPhysicals;
     std::vector<double> wall_dist;
     uint32_t nRealCells = 0;
+    // batch of independent cases: reference-order cell ranges of each case
+    // (empty for a single mesh)
+    std::vector<int> segments;
 
     // raw input before finalize()
     std::vector<uint32_t> bnd0, bnd1;

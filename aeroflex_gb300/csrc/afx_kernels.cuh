@@ -261,6 +261,12 @@ struct StageOut {
     double alpha, relax;
     double* __restrict__ partials;
     const float4* __restrict__ corr;  // FP32-mixed defect correction per cell, or null
+    // batch of independent cases (null for a single case): the case of each
+    // cell, the cases that have stopped (their state is held), and the
+    // per-cell squared residual of the last stage for the per-case norms
+    const int* __restrict__ case_of;
+    const int* __restrict__ case_done;
+    double* __restrict__ cell_sq;
     int mode;                      // 0 stage 0/1, 1 stage 2 (+norm), 2 residual only (write R)
 };
 
@@ -349,7 +355,34 @@ __device__ __forceinline__ void stage_epilogue(const StageOut<T, S>& o, const in
         T R[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) R[k] = Rsum[k] / A;
-        if (o.mode == 2) {
+        if (o.case_done && o.mode != 2 && __ldg(&o.case_done[__ldg(&o.case_of[i])])) {
+            // a case that has stopped keeps its state
+            if (o.mode == 0) {
+                if (sizeof(T) == 4) {
+                    T qs[4];
+                    ld4s(&o.q0s[i], qs);
+                    V4<S> v;
+                    st4(&v, qs);
+                    o.qnext[i] = v;
+                } else {
+                    double q0[4];
+                    ld4(&o.q0[i], q0);
+                    V4<S> v;
+                    st4(&v, q0);
+                    o.qnext[i] = v;
+                }
+            } else {
+                double q0[4];
+                ld4(&o.q0[i], q0);
+                st4(&o.qm_next[i], q0);
+                if (o.qsh_next) {
+                    V4<S> v;
+                    st4(&v, q0);
+                    o.qsh_next[i] = v;
+                }
+                o.cell_sq[i] = 0.0;
+            }
+        } else if (o.mode == 2) {
             double Rd[4] = {(double)R[0], (double)R[1], (double)R[2], (double)R[3]};
             st4(&o.Rq[i], Rd);
         } else if (sizeof(T) == 4) {
@@ -375,6 +408,13 @@ __device__ __forceinline__ void stage_epilogue(const StageOut<T, S>& o, const in
 #pragma unroll
                 for (int k = 0; k < 4; ++k) sq += (double)R[k] * (double)R[k];
             }
+        }
+        if (o.cell_sq && o.mode == 1 && !(o.case_done && __ldg(&o.case_done[__ldg(&o.case_of[i])]))) {
+            // batch: the last stage's qW stays in Rq for a later
+            // get_uniform_residual (each case stops at its own iteration)
+            o.cell_sq[i] = sq;
+            double Rd[4] = {(double)R[0], (double)R[1], (double)R[2], (double)R[3]};
+            st4(&o.Rq[i], Rd);
         }
     }
     if (o.mode == 1) {
@@ -727,12 +767,19 @@ template <class T, class S, int VISC>
 __global__ void __launch_bounds__(256) k_uniform(const KM<T> m, const V4<S>* __restrict__ qmem,
                                                  const V4<T>* __restrict__ gx, const V4<T>* __restrict__ gy,
                                                  const double q0, const double q1, const double q2, const double q3,
-                                                 d4* __restrict__ Rq, double* __restrict__ partials) {
+                                                 d4* __restrict__ Rq, double* __restrict__ partials,
+                                                 const double* __restrict__ qfar_case, const int* __restrict__ case_of,
+                                                 double* __restrict__ cell_sq) {
     __shared__ double sh[32];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double sq = 0;
     if (i < m.n_cells) {
-        const T qf[4] = {(T)q0, (T)q1, (T)q2, (T)q3};
+        T qf[4] = {(T)q0, (T)q1, (T)q2, (T)q3};
+        if (qfar_case) {  // batch: the freestream of this cell's case
+            const int c = __ldg(&case_of[i]);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) qf[k] = (T)__ldg(&qfar_case[4 * c + k]);
+        }
         double acc[4];
         ld4(&Rq[i], acc);
         T accT[4] = {(T)acc[0], (T)acc[1], (T)acc[2], (T)acc[3]};
@@ -796,9 +843,66 @@ __global__ void __launch_bounds__(256) k_uniform(const KM<T> m, const V4<S>* __r
             sq += out[k] * out[k];
         }
         st4(&Rq[i], out);
+        if (cell_sq) cell_sq[i] = sq;
     }
     const double t = block_sum(sq, sh);
     if (threadIdx.x == 0) partials[blockIdx.x] = t;
+}
+
+// Per-case norm and run_solver control of a batch (multigrid.h:195-234 for
+// every case): one block per case sums the per-cell squares of its cells in
+// a fixed order.  A case that stops is marked in case_done (its cells then
+// hold their state); the whole run stops when every case has.
+static __global__ void __launch_bounds__(256) k_case_control(const double* __restrict__ cell_sq,
+                                                             const int* __restrict__ case_off, CaseCtrl* cctrl,
+                                                             int* case_done, double* chist, Ctrl* ctrl, int n_cases,
+                                                             int uniform) {
+    __shared__ double sh[32];
+    if (!uniform && ctrl->done) return;
+    const int c = blockIdx.x;
+    CaseCtrl& cc = cctrl[c];
+    if (!uniform && cc.done) return;
+    const int b0 = case_off[c], b1 = case_off[c + 1];
+    double v = 0;
+    for (int k = b0 + threadIdx.x; k < b1; k += blockDim.x) v += cell_sq[k];
+    const double t = block_sum(v, sh);
+    if (threadIdx.x != 0) return;
+    const double norm = sqrt(t);
+    if (uniform) {
+        cc.err0 = norm;
+        return;
+    }
+    const int i = cc.iter;
+    cc.last_norm = norm;
+    double err = norm;
+    bool stop = false;
+    if (!(norm == norm) || norm > 1.7976931348623157e308) {
+        cc.status = 4;
+        stop = true;
+    }
+    if (ctrl->run_mode) {
+        if (i == 0 && err > 2 * cc.err0) cc.err0 = err;
+        if (err > 0) err /= cc.err0;
+        cc.err = err;
+        if (i % 10 == 0 && cc.hist_n < CASE_HIST_CAP) chist[(size_t)c * CASE_HIST_CAP + cc.hist_n++] = err;
+        if (!((err > ctrl->tol) && (i + 1 < ctrl->max_it))) stop = true;
+    }
+    cc.iter = i + 1;
+    if (ctrl->run_mode == 0) cc.err = err;
+    if (stop) {
+        cc.done = 1;
+        case_done[c] = 1;
+        atomicAdd(&ctrl->ndone, 1);
+    }
+}
+
+// After k_case_control: count the iteration and stop the run once every
+// case has stopped (a separate launch, so no block of k_case_control sees
+// the run's flag change under it).
+static __global__ void k_batch_finalize(Ctrl* ctrl, int n_cases) {
+    if (ctrl->done) return;
+    ctrl->iter += 1;
+    if (ctrl->ndone >= n_cases) ctrl->done = 1;
 }
 
 // Residual-norm finalisation and the run_solver control (multigrid.h:195-234)

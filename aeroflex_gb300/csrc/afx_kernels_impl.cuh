@@ -136,6 +136,9 @@ StageOut<T, S> base_out(const StepArgs& a, int p) {
     o.relax = a.relax;
     o.partials = a.partials;
     o.corr = (const float4*)a.corr;
+    o.case_of = a.case_of;
+    o.case_done = a.case_done;
+    o.cell_sq = a.cell_sq;
     o.mode = 0;
     return o;
 }
@@ -169,7 +172,13 @@ void iteration(const StepArgs& a, int p, cudaStream_t s) {
         }
         launch_stage<T, S>(a, m, qk, q, o, st == 0, s);
     }
-    k_control<<<1, 1024, 0, s>>>(a.partials, nblocks(a.n_cells, a.block), a.ctrl, a.hist, a.norms, 0);
+    if (a.n_cases > 0) {
+        k_case_control<<<a.n_cases, 256, 0, s>>>(a.cell_sq, a.case_off, a.cctrl, a.case_done, a.chist, a.ctrl,
+                                                 a.n_cases, 0);
+        k_batch_finalize<<<1, 1, 0, s>>>(a.ctrl, a.n_cases);
+    } else {
+        k_control<<<1, 1024, 0, s>>>(a.partials, nblocks(a.n_cells, a.block), a.ctrl, a.hist, a.norms, 0);
+    }
     mark(a, K_CONTROL, s);
 }
 
@@ -201,11 +210,17 @@ void uniform(const StepArgs& a, int p, const double* qf, cudaStream_t s) {
     const V4<S>* q = (const V4<S>*)a.qsh[p];
     if (a.visc == 1)
         k_uniform<T, S, 1><<<nb, a.block, 0, s>>>(m, q, (const V4<T>*)a.gx, (const V4<T>*)a.gy, qf[0], qf[1],
-                                                   qf[2], qf[3], (d4*)a.Rq, a.partials);
+                                                   qf[2], qf[3], (d4*)a.Rq, a.partials, a.qfar_case, a.case_of,
+                                                   a.cell_sq);
     else
         k_uniform<T, S, 0><<<nb, a.block, 0, s>>>(m, q, (const V4<T>*)a.gx, (const V4<T>*)a.gy, qf[0], qf[1],
-                                                   qf[2], qf[3], (d4*)a.Rq, a.partials);
-    k_control<<<1, 1024, 0, s>>>(a.partials, nb, a.ctrl, a.hist, nullptr, 1);
+                                                   qf[2], qf[3], (d4*)a.Rq, a.partials, a.qfar_case, a.case_of,
+                                                   a.cell_sq);
+    if (a.n_cases > 0)
+        k_case_control<<<a.n_cases, 256, 0, s>>>(a.cell_sq, a.case_off, a.cctrl, a.case_done, a.chist, a.ctrl,
+                                                 a.n_cases, 1);
+    else
+        k_control<<<1, 1024, 0, s>>>(a.partials, nb, a.ctrl, a.hist, nullptr, 1);
 }
 
 }  // namespace dev

@@ -17,7 +17,7 @@ struct Ctrl {
     int max_it;
     int hist_n;
     int nparts;     // partial sums written by the last stage kernel
-    int pad;
+    int ndone;      // batch: cases that have stopped
     double err0;
     double err;     // last normalised residual (run_mode 1)
     double tol;
@@ -25,6 +25,13 @@ struct Ctrl {
 };
 
 constexpr int HIST_CAP = 1 << 16;
+
+// Per-case run_solver state of a batch (one per case).
+struct CaseCtrl {
+    int done, iter, status, hist_n;
+    double err0, err, last_norm;
+};
+constexpr int CASE_HIST_CAP = 4096;  // history entries kept per case (every 10th iteration)
 
 // Eager-launch profiler: an event after every kernel of an iteration, so the
 // host can time each kernel on the stream it runs on.
@@ -97,6 +104,15 @@ struct StepArgs {
     double* hist = nullptr;    // [HIST_CAP] run_solver history (every 10th)
     double* norms = nullptr;   // optional per-iteration norms
     const void* corr = nullptr;  // float4 [N]: FP32-mixed defect correction (null: off)
+    // batch of independent cases (n_cases == 0: a single case)
+    int n_cases = 0;
+    const int* case_of = nullptr;     // [N] case of each device cell
+    const int* case_off = nullptr;    // [n_cases+1] device cell range of each case
+    int* case_done = nullptr;         // [n_cases] 1 once a case has stopped
+    double* cell_sq = nullptr;        // [N] squared last-stage residual of each cell
+    CaseCtrl* cctrl = nullptr;        // [n_cases]
+    double* chist = nullptr;          // [n_cases * CASE_HIST_CAP]
+    const double* qfar_case = nullptr;  // [4 * n_cases] freestream state of each case
     Prof* prof = nullptr;      // eager profiling only (never inside a graph)
 };
 

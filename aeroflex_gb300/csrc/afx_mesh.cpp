@@ -421,24 +421,29 @@ DeviceLayout build_layout(const HostMesh& m) {
     L.n_faces = E;
     L.n_bnd = B;
 
-    // cells along a Hilbert curve of their centroids
-    double xmin = 1e300, xmax = -1e300, ymin = 1e300, ymax = -1e300;
-    for (int i = 0; i < N; ++i) {
-        xmin = std::min(xmin, m.cellsCentersX[i]);
-        xmax = std::max(xmax, m.cellsCentersX[i]);
-        ymin = std::min(ymin, m.cellsCentersY[i]);
-        ymax = std::max(ymax, m.cellsCentersY[i]);
-    }
-    const double span = std::max(std::max(xmax - xmin, ymax - ymin), 1e-300);
+    // cells along a Hilbert curve of their centroids, within each segment
+    // (a batch of independent cases keeps each case's cells contiguous)
+    std::vector<int> seg = m.segments;
+    if (seg.empty()) seg = {0, N};
     std::vector<uint64_t> hk(N);
     std::vector<uint32_t> hv(N);
-    for (int i = 0; i < N; ++i) {
-        uint32_t gx = (uint32_t)std::min(65535.0, std::floor((m.cellsCentersX[i] - xmin) / span * 65535.0));
-        uint32_t gy = (uint32_t)std::min(65535.0, std::floor((m.cellsCentersY[i] - ymin) / span * 65535.0));
-        hk[i] = hilbert(gx, gy);
-        hv[i] = (uint32_t)i;
+    for (size_t sg = 0; sg + 1 < seg.size(); ++sg) {
+        double xmin = 1e300, xmax = -1e300, ymin = 1e300, ymax = -1e300;
+        for (int i = seg[sg]; i < seg[sg + 1]; ++i) {
+            xmin = std::min(xmin, m.cellsCentersX[i]);
+            xmax = std::max(xmax, m.cellsCentersX[i]);
+            ymin = std::min(ymin, m.cellsCentersY[i]);
+            ymax = std::max(ymax, m.cellsCentersY[i]);
+        }
+        const double span = std::max(std::max(xmax - xmin, ymax - ymin), 1e-300);
+        for (int i = seg[sg]; i < seg[sg + 1]; ++i) {
+            uint32_t gx = (uint32_t)std::min(65535.0, std::floor((m.cellsCentersX[i] - xmin) / span * 65535.0));
+            uint32_t gy = (uint32_t)std::min(65535.0, std::floor((m.cellsCentersY[i] - ymin) / span * 65535.0));
+            hk[i] = ((uint64_t)sg << 32) | hilbert(gx, gy);
+            hv[i] = (uint32_t)i;
+        }
     }
-    radix_sort(hk, hv, 32);
+    radix_sort(hk, hv, seg.size() > 2 ? 48 : 32);
     L.cell_old.assign(hv.begin(), hv.end());
     L.cell_new.assign(N, 0);
     for (int i = 0; i < N; ++i) L.cell_new[L.cell_old[i]] = i;

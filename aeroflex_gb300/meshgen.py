@@ -242,3 +242,25 @@ def write_gmsh(path, m):
     out.append("$EndElements")
     with open(path, "w") as f:
         f.write("\n".join(out) + "\n")
+
+
+def polar_sweep_cases(n_cases=256, seed=4, n_min=5000, n_max=200000, split=False):
+    """Batched polar-sweep workload: ``n_cases`` NACA 4-digit airfoils with
+    max camber m ~ U[0, 6]%, thickness t ~ U[8, 18]% and camber position
+    p ~ U[0.2, 0.6]; cell count log-uniform in [n_min, n_max] (O-meshes with
+    n_surf : n_rad = 2 : 1); angle of attack ~ U[-4, 12] degrees and Mach
+    ~ U[0.1, 0.7].  Returns a list of dicts with the mesh and the flow."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n_cases):
+        m = rng.uniform(0.0, 0.06)
+        t = rng.uniform(0.08, 0.18)
+        p = rng.uniform(0.2, 0.6)
+        n = math.exp(rng.uniform(math.log(n_min), math.log(n_max)))
+        aoa = rng.uniform(-4.0, 12.0)
+        mach = rng.uniform(0.1, 0.7)
+        n_rad = max(8, int(round(math.sqrt(n / (4.0 if split else 2.0)))))
+        n_surf = 2 * n_rad
+        mesh = airfoil_omesh(n_surf=n_surf, n_rad=n_rad, m=m, p=p, t=t, split=split)
+        out.append(dict(mesh=mesh, m=m, t=t, p=p, aoa_deg=aoa, mach=mach, n_cells=len(mesh["cells"])))
+    return out

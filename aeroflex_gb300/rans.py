@@ -27,7 +27,10 @@ ABI_SYMBOLS = [
     "afx_solver_free", "afx_init_freestream", "afx_set_state", "afx_get_state", "afx_residual", "afx_iterate",
     "afx_run_to_convergence", "afx_residual_history", "afx_forces", "afx_set_farfield", "afx_request_stop",
     "afx_last_device_seconds", "afx_profile_iterations", "afx_kernel_name", "afx_autotune",
-    "afx_residual_noalloc",
+    "afx_residual_noalloc", "afx_batch_create", "afx_batch_free", "afx_batch_counts", "afx_batch_init_freestream",
+    "afx_batch_set_state", "afx_batch_get_state", "afx_batch_iterate", "afx_batch_run_to_convergence",
+    "afx_batch_case_history", "afx_batch_forces", "afx_batch_set_farfield", "afx_batch_autotune",
+    "afx_batch_last_device_seconds",
 ]
 N_KERNEL_KINDS = 7
 
@@ -89,6 +92,19 @@ def lib():
         "afx_kernel_name": (cp, [i]),
         "afx_autotune": (i, [vp, i, ctypes.c_char_p, i, P(i), P(d)]),
         "afx_residual_noalloc": (i, [vp, vp, vp, ll]),
+        "afx_batch_create": (i, [i, vp, vp, P(vp)]),
+        "afx_batch_free": (None, [vp]),
+        "afx_batch_counts": (i, [vp, P(i), P(ll)]),
+        "afx_batch_init_freestream": (i, [vp]),
+        "afx_batch_set_state": (i, [vp, i, vp, ll]),
+        "afx_batch_get_state": (i, [vp, i, vp, ll]),
+        "afx_batch_iterate": (i, [vp, i, vp]),
+        "afx_batch_run_to_convergence": (i, [vp, d, i, vp, vp, vp]),
+        "afx_batch_case_history": (i, [vp, i, vp, i, P(i)]),
+        "afx_batch_forces": (i, [vp, i, cp, P(d), P(d), P(d)]),
+        "afx_batch_set_farfield": (i, [vp, i, cp, d, d, d, d]),
+        "afx_batch_autotune": (i, [vp, i, ctypes.c_char_p, i, P(i), P(d)]),
+        "afx_batch_last_device_seconds": (i, [vp, P(d)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -300,3 +316,89 @@ def get_wall_profile(s, patch="wall", cap=1 << 20):
     _check(lib().afx_forces(s.h, patch.encode(), ctypes.byref(cl), ctypes.byref(cd), ctypes.byref(cm), _ptr(cp), cap,
                             ctypes.byref(n)))
     return dict(cl=cl.value, cd=cd.value, cm=cm.value, cp=cp[: n.value].copy())
+
+
+class Batch:
+    """Many independent load cases (own mesh, angle, Mach) advanced together:
+    each case follows `multigrid<explicitSolver>::run_solver`
+    (multigrid.h:183-234) on its own, one launch per kernel for all of them."""
+
+    def __init__(self, meshes, settings):
+        meshes, settings = list(meshes), list(settings)
+        if len(meshes) != len(settings):
+            raise ValueError("one Settings per mesh")
+        self._keep = (meshes, settings)
+        mh = (ctypes.c_void_p * len(meshes))(*[m.h.value for m in meshes])
+        sh = (ctypes.c_void_p * len(settings))(*[s.h.value for s in settings])
+        h = ctypes.c_void_p()
+        _check(lib().afx_batch_create(len(meshes), ctypes.cast(mh, ctypes.c_void_p), ctypes.cast(sh, ctypes.c_void_p),
+                                      ctypes.byref(h)))
+        self.h = h
+        self.n = len(meshes)
+        self.n_real = [m.nRealCells for m in meshes]
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.afx_batch_free(self.h)
+            self.h = None
+
+    def __len__(self):
+        return self.n
+
+    def n_cells_total(self):
+        n = ctypes.c_longlong()
+        _check(lib().afx_batch_counts(self.h, None, ctypes.byref(n)))
+        return n.value
+
+    def init(self):
+        _check(lib().afx_batch_init_freestream(self.h))
+
+    def set_q(self, c, q):
+        q = np.ascontiguousarray(q, np.float64).reshape(-1)
+        _check(lib().afx_batch_set_state(self.h, int(c), _ptr(q), q.size))
+
+    def get_q(self, c):
+        out = np.empty(4 * self.n_real[c], np.float64)
+        _check(lib().afx_batch_get_state(self.h, int(c), _ptr(out), out.size))
+        return out
+
+    def iterate(self, n):
+        r = np.zeros(self.n, np.float64)
+        _check(lib().afx_batch_iterate(self.h, int(n), _ptr(r)))
+        return r
+
+    def run_solver(self, tol=0.0, max_it=0):
+        """Returns (iterations, err/err_0, status) arrays, one entry per case."""
+        it = np.zeros(self.n, np.int32)
+        err = np.zeros(self.n, np.float64)
+        st = np.zeros(self.n, np.int32)
+        _check(lib().afx_batch_run_to_convergence(self.h, float(tol), int(max_it), _ptr(it), _ptr(err), _ptr(st)))
+        return it, err, st
+
+    def history(self, c):
+        n = ctypes.c_int()
+        _check(lib().afx_batch_case_history(self.h, int(c), None, 0, ctypes.byref(n)))
+        out = np.empty(n.value, np.float64)
+        _check(lib().afx_batch_case_history(self.h, int(c), _ptr(out), n.value, ctypes.byref(n)))
+        return out
+
+    def forces(self, c, patch="wall"):
+        cl, cd, cm = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        _check(lib().afx_batch_forces(self.h, int(c), patch.encode(), ctypes.byref(cl), ctypes.byref(cd),
+                                      ctypes.byref(cm)))
+        return dict(cl=cl.value, cd=cd.value, cm=cm.value)
+
+    def set_farfield(self, c, patch, mach, angle, T=1.0, p=1.0):
+        _check(lib().afx_batch_set_farfield(self.h, int(c), patch.encode(), mach, angle, T, p))
+
+    def autotune(self, iters=5):
+        buf = ctypes.create_string_buffer(16)
+        blk = ctypes.c_int()
+        ms = ctypes.c_double()
+        _check(lib().afx_batch_autotune(self.h, int(iters), buf, 16, ctypes.byref(blk), ctypes.byref(ms)))
+        return dict(variant=buf.value.decode(), block=blk.value, ms_per_iter=ms.value)
+
+    def last_device_seconds(self):
+        s = ctypes.c_double()
+        _check(lib().afx_batch_last_device_seconds(self.h, ctypes.byref(s)))
+        return s.value

@@ -38,6 +38,7 @@ typedef enum {
 typedef struct afx_mesh_s* afx_mesh;
 typedef struct afx_config_s* afx_config;
 typedef struct afx_solver_s* afx_solver;
+typedef struct afx_batch_s* afx_batch;
 
 /* Thread-local text of the last error. */
 const char* afx_last_error(void);
@@ -167,6 +168,48 @@ int afx_autotune(afx_solver s, int iters, char* variant, int cap, int* block, do
  * caller serialises them.  The first call on each device looks up the
  * array's address; make it before any stream capture. */
 int afx_residual_noalloc(afx_solver s, const double* q_dev, double* R_dev, long long n);
+
+/* ---- Batched load cases.  No single counterpart in the reference: its
+ * polar sweep runs one case after another (src/rans/include/rans/rans.h:
+ * 92-105 loops over the angles, multigrid.h:183-234 run_solver per case).  A
+ * batch advances many independent cases -- each with its own mesh, angle,
+ * Mach and farfield -- in one launch per kernel, one device solver over the
+ * union of the meshes.  Every case follows the reference's run_solver logic
+ * on its own (err_0, err/err_0 < tol, max iterations, history every 10th
+ * iteration); a case that stops holds its state while the others go on.
+ * In FP64 each case's state, iteration count and history are bit-identical
+ * to a single afx_solver on that case alone (norms: same to ~1e-15).
+ *
+ * All configs must share the scheme (gamma, R, mu, Pr, viscosity, gradient,
+ * limiter, precision, second_order, start_cfl, relaxation, limiter_k); the
+ * boundary conditions come from each case's own config, keyed by the case
+ * mesh's patch names.  Launch settings (kernel_variant, block_size) are case
+ * 0's.  fp64_correction_interval and fp64_finish are single-case options. */
+int afx_batch_create(int n_cases, const afx_mesh* meshes, const afx_config* configs, afx_batch* out);
+void afx_batch_free(afx_batch b);
+int afx_batch_counts(afx_batch b, int* n_cases, long long* n_cells_total);
+/* init() (solver.h:615-631) of every case with its own freestream. */
+int afx_batch_init_freestream(afx_batch b);
+/* State of case c in the case mesh's reference cell order (4*n_real doubles). */
+int afx_batch_set_state(afx_batch b, int c, const double* q, long long n);
+int afx_batch_get_state(afx_batch b, int c, double* q, long long n);
+/* n iterations of every case; res_norms[c] = ||qW||_2 of case c's last
+ * stage (may be NULL).  AFX_ERR_NONFINITE if any case's norm is not finite
+ * (that case stops where it went non-finite; the others complete). */
+int afx_batch_iterate(afx_batch b, int n_iters, double* res_norms);
+/* run_solver of every case at once; per case: iterations, final err/err_0
+ * and status (AFX_OK or AFX_ERR_NONFINITE).  tol <= 0 / max_it <= 0: case
+ * 0's config values.  Returns when every case has stopped. */
+int afx_batch_run_to_convergence(afx_batch b, double tol, int max_it, int* iters, double* errs, int* status);
+/* err/err_0 every 10th iteration of case c's last run (up to 4096 entries). */
+int afx_batch_case_history(afx_batch b, int c, double* out, int cap, int* n);
+/* get_wall_profile (post.h:301-387) of case c over its patch `patch`. */
+int afx_batch_forces(afx_batch b, int c, const char* patch, double* cl, double* cd, double* cm);
+/* rans.h:92-98 for case c: new farfield conditions, state kept. */
+int afx_batch_set_farfield(afx_batch b, int c, const char* patch, double mach, double angle, double T, double p);
+/* afx_autotune over the whole batch (state and qW put back). */
+int afx_batch_autotune(afx_batch b, int iters, char* variant, int cap, int* block, double* ms_per_iter);
+int afx_batch_last_device_seconds(afx_batch b, double* sec);
 
 #ifdef __cplusplus
 }

@@ -32,6 +32,12 @@ def oracle_solver(orc, m, bcs, **settings):
 
 
 def gpu_solver(afx, m, bcs, precision="fp64", **settings):
+    st = gpu_settings(afx, bcs, precision, **settings)
+    gm = afx.mesh.from_arrays(m)
+    return afx.Solver(gm, st)
+
+
+def gpu_settings(afx, bcs, precision="fp64", **settings):
     st = afx.Settings()
     st.set("solver", "explicit")
     st.set("precision", precision)
@@ -43,8 +49,20 @@ def gpu_solver(afx, m, bcs, precision="fp64", **settings):
         st.set(k, v)
     for name, b in bcs.items():
         st.set_bc(name, b["type"], b.get("T", 1.0), b.get("mach", 0.2), b.get("angle", 0.0), b.get("p", 1.0))
-    gm = afx.mesh.from_arrays(m)
-    return afx.Solver(gm, st)
+    return st
+
+
+def batch_cases():
+    """Four small cases of uneven size, shape and flow (a polar-sweep batch
+    in miniature): O-meshes of different resolution and camber, and a
+    jittered channel."""
+    out = []
+    for (ns, nr, mach, aoa, kw) in [(32, 16, 0.5, 1.25, {}), (48, 24, 0.3, 4.0, dict(m=0.04, p=0.4, t=0.10)),
+                                    (40, 20, 0.6, -2.0, dict(t=0.15))]:
+        out.append(omesh_case(ns, nr, mach=mach, aoa_deg=aoa, **kw))
+    m, bcs, _ = channel_case(24, 12, mach=0.4, seed=5)
+    out.append((m, bcs))
+    return out
 
 
 def rel_l2(a, b):

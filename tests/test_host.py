@@ -172,3 +172,17 @@ def test_solver_without_gpu_fails_loudly(afx):
     with pytest.raises(afx.AfxError) as e:
         afx.Solver(m, afx.Settings())
     assert e.value.code == 7
+
+
+def test_batch_checks_schemes_then_fails_loudly_without_gpu(afx):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("GPU present")
+    meshes = [afx.mesh.from_arrays(meshgen.airfoil_omesh(16, 8)), afx.mesh.from_arrays(meshgen.airfoil_omesh(20, 8))]
+    sets = [afx.Settings(), afx.Settings().set("limiter", "michalak")]
+    with pytest.raises(afx.AfxError) as e:
+        afx.Batch(meshes, sets)
+    assert e.value.code == 2 and "case 1" in str(e.value)
+    with pytest.raises(afx.AfxError) as e:
+        afx.Batch(meshes, [afx.Settings(), afx.Settings()])
+    assert e.value.code == 7
