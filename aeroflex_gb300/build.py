@@ -43,6 +43,7 @@ def _units():
         (cxx + ["-c"], "afx_abi.cpp"),
         (nv + ["-fmad=false", "-c"], "afx_kernels_f64.cu"),
         (nv + ["-fmad=false", "-c"], "afx_noalloc.cu"),
+        (nv + ["-fmad=false", "-c"], "afx_adjoint.cu"),
         (nv + ["-use_fast_math", "-c"], "afx_kernels_f32.cu"),
     ], nvcc
 

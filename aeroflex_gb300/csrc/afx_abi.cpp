@@ -225,6 +225,45 @@ struct afx_solver_s {
         double xmin = 0, xmax = 0, x_moment = 0, y_moment = 0;
     };
     std::map<std::string, std::unique_ptr<PatchForces>> patches;
+    // adjoint work arrays (allocated on first use) and the last adjoint state
+    struct AdjointBufs {
+        DevBuf v, fbar, gbx, gby, qbar, lw, lt, u, bqbar, g, q, lam[2], ls[2], partials;
+        AdjArgs args(const void* v_dev, void* u_dev) const {
+            AdjArgs j;
+            j.v = v_dev;
+            j.fbar = fbar.p;
+            j.gbx = gbx.p;
+            j.gby = gby.p;
+            j.qbar = qbar.p;
+            j.lw = lw.p;
+            j.lt = lt.p;
+            j.u = u_dev;
+            j.bqbar = bqbar.p;
+            return j;
+        }
+    };
+    std::unique_ptr<AdjointBufs> adj;
+    int adj_parity = 0;  // lam[adj_parity] holds the last adjoint solution
+    AdjointBufs& adjoint() {
+        if (!fp64) throw Error(AFX_ERR_CONFIG, "the adjoint needs an fp64 solver");
+        if (a.visc != 0) throw Error(AFX_ERR_CONFIG, "the adjoint covers the inviscid flux only");
+        if (!adj) {
+            const size_t N = a.n_cells, F = a.n_faces, B = std::max(a.n_bnd, 1);
+            auto b = std::make_unique<AdjointBufs>();
+            for (DevBuf* d : {&b->v, &b->gbx, &b->gby, &b->qbar, &b->u, &b->g, &b->q, &b->lam[0], &b->lam[1],
+                              &b->ls[0], &b->ls[1]})
+                d->alloc(N * 32);
+            b->fbar.alloc(F * 64);
+            b->lw.alloc(N * 64);
+            b->lt.alloc(N * 32);
+            b->bqbar.alloc(B * 32);
+            b->partials.alloc(((N + 255) / 256) * 8);
+            for (DevBuf* d : {&b->gbx, &b->gby, &b->lw, &b->lt, &b->lam[0], &b->lam[1]})
+                AFX_CUDA(cudaMemsetAsync(d->p, 0, d->bytes, stream));
+            adj = std::move(b);
+        }
+        return *adj;
+    }
 
     void* dalloc(size_t n) {
         bufs.emplace_back(new DevBuf());
@@ -995,8 +1034,9 @@ int afx_residual_history(afx_solver s, double* out, int cap, int* n) {
 
 // get_wall_profile (post.h:301-387) over the boundary edges named `patch`,
 // with the freestream `vf`.
-static void forces_impl(afx_solver_s* s, const std::string& patch, const FarfieldVars& vf, double* cl, double* cd,
-                        double* cm, double* cp, int cap, int* n_cp) {
+// Force-integration arguments of the boundary edges named `patch` (their
+// geometry is uploaded on first use), with the freestream `vf`.
+static ForceArgs force_args(afx_solver_s* s, const std::string& patch, const FarfieldVars& vf) {
     {
         auto& pf = s->patches[patch];
         if (!pf) {
@@ -1046,19 +1086,27 @@ static void forces_impl(afx_solver_s* s, const std::string& patch, const Farfiel
         f.q = (const double*)s->a.qm[s->parity];
         f.cp = (double*)pf->cp.p;
         f.sums = (double*)pf->sums.p;
+        return f;
+    }
+}
+
+static void forces_impl(afx_solver_s* s, const std::string& patch, const FarfieldVars& vf, double* cl, double* cd,
+                        double* cm, double* cp, int cap, int* n_cp) {
+    {
+        const ForceArgs f = force_args(s, patch, vf);
         enqueue_forces(f, s->stream);
         double sums[3];
-        AFX_CUDA(cudaMemcpyAsync(sums, pf->sums.p, 24, cudaMemcpyDeviceToHost, s->stream));
-        std::vector<double> cph(pf->n);
-        AFX_CUDA(cudaMemcpyAsync(cph.data(), pf->cp.p, pf->n * 8, cudaMemcpyDeviceToHost, s->stream));
+        AFX_CUDA(cudaMemcpyAsync(sums, f.sums, 24, cudaMemcpyDeviceToHost, s->stream));
+        std::vector<double> cph(f.n);
+        AFX_CUDA(cudaMemcpyAsync(cph.data(), f.cp, f.n * 8, cudaMemcpyDeviceToHost, s->stream));
         AFX_CUDA(cudaStreamSynchronize(s->stream));
         const double fx = sums[0], fy = sums[1], aoa = vf.angle;  // post.h:379-384
         if (cd) *cd = fx * std::cos(aoa) + fy * std::sin(aoa);
         if (cl) *cl = -fx * std::sin(aoa) + fy * std::cos(aoa);
         if (cm) *cm = sums[2];
-        if (n_cp) *n_cp = pf->n;
+        if (n_cp) *n_cp = f.n;
         if (cp)
-            for (int i = 0; i < pf->n && i < cap; ++i) cp[i] = cph[i];
+            for (int i = 0; i < f.n && i < cap; ++i) cp[i] = cph[i];
     }
 }
 
@@ -1508,6 +1556,169 @@ int afx_batch_last_device_seconds(afx_batch b, double* sec) {
     return guarded([&] {
         if (!b || !sec) throw Error(AFX_ERR_ARG, "null argument");
         *sec = b->s->last_sec;
+    });
+}
+
+// ---------------------------------------------------------------- adjoint
+int afx_residual_vjp(afx_solver s, const double* q, const double* v, double* u, double* bq_bar, long long n) {
+    return guarded([&] {
+        if (!s || !v || !u) throw Error(AFX_ERR_ARG, "null argument");
+        const size_t N = s->a.n_cells, B = s->a.n_bnd;
+        if (n != (long long)(4 * N)) throw Error(AFX_ERR_ARG, "state size must be 4*n_real_cells");
+        auto& J = s->adjoint();
+        s->materialize_qW();  // the prep below overwrites the last stage's gradients
+        s->set_ctrl(0, 0, 0);
+        StepArgs a = s->a;
+        int p = s->parity;
+        if (q) {  // the caller's state in a scratch buffer; the solver's own state is kept
+            AFX_CUDA(cudaMemcpyAsync(s->d_stage.p, q, N * 32, cudaMemcpyDefault, s->stream));
+            enqueue_permute_in((int)N, (const int*)s->d_cell_old.p, s->d_stage.p, J.q.p, s->stream);
+            a.qm[0] = a.qsh[0] = J.q.p;
+            p = 0;
+        }
+        AFX_CUDA(cudaMemcpyAsync(s->d_stage.p, v, N * 32, cudaMemcpyDefault, s->stream));
+        enqueue_permute_in((int)N, (const int*)s->d_cell_old.p, s->d_stage.p, J.v.p, s->stream);
+        enqueue_adjoint_prep(a, p, false, s->stream);
+        enqueue_vjp(a, p, J.args(J.v.p, J.u.p), s->stream);
+        enqueue_permute_out((int)N, (const int*)s->d_cell_old.p, J.u.p, s->d_stage.p, s->stream);
+        AFX_CUDA(cudaMemcpyAsync(u, s->d_stage.p, N * 32, cudaMemcpyDefault, s->stream));
+        if (bq_bar && B > 0) AFX_CUDA(cudaMemcpyAsync(bq_bar, J.bqbar.p, B * 32, cudaMemcpyDefault, s->stream));
+        AFX_CUDA(cudaStreamSynchronize(s->stream));
+        AFX_CUDA(cudaGetLastError());
+    });
+}
+
+int afx_boundary_states(afx_solver s, double* bq, long long n) {
+    return guarded([&] {
+        if (!s || !bq) throw Error(AFX_ERR_ARG, "null argument");
+        const size_t B = s->boundary_type.size();
+        if (n != (long long)(4 * B)) throw Error(AFX_ERR_ARG, "size must be 4*n_boundary_edges");
+        for (size_t b = 0; b < B; ++b) conservative(s->st, s->boundary_vars[b], bq + 4 * b);
+    });
+}
+
+int afx_adjoint_solve(afx_solver s, const char* patch, const char* objective, double tol, int max_it, double* dJ,
+                      int* iters, double* res) {
+    return guarded([&] {
+        if (!s || !patch || !objective || !dJ) throw Error(AFX_ERR_ARG, "null argument");
+        const std::string obj = objective;
+        if (obj != "cl" && obj != "cd") throw Error(AFX_ERR_ARG, "objective must be \"cl\" or \"cd\"");
+        if (tol <= 0) tol = 1e-10;
+        if (max_it <= 0) max_it = 100000;
+        auto& J = s->adjoint();
+        const size_t N = s->a.n_cells, B = s->a.n_bnd;
+        s->materialize_qW();
+        s->set_ctrl(0, 0, 0);
+        const int p = s->parity;
+        const StepArgs& a = s->a;
+        const FarfieldVars vf = s->freestream();
+        // forces at the converged state and dJ/dq of J = cx*fx + cy*fy
+        double cl = 0, cd = 0;
+        forces_impl(s, patch, vf, &cl, &cd, nullptr, nullptr, 0, nullptr);
+        const double ca = std::cos(vf.angle), sa = std::sin(vf.angle);
+        const double cx = obj == "cl" ? -sa : ca, cy = obj == "cl" ? ca : sa;
+        ForceArgs f = force_args(s, patch, vf);
+        AFX_CUDA(cudaMemsetAsync(J.g.p, 0, N * 32, s->stream));
+        enqueue_objective_grad(f, cx, cy, J.g.p, s->stream);
+        // gradients, limiter and local time step of the converged state
+        enqueue_adjoint_prep(a, p, true, s->stream);
+        // pseudo-time iteration lam <- lam + relax*dt*(J^T lam + dJ/dq) with
+        // the solver's three stages (alpha = 1/4, 1/2, 1), from lam = 0
+        AFX_CUDA(cudaMemsetAsync(J.lam[0].p, 0, N * 32, s->stream));
+        static const double alpha[3] = {0.25, 0.5, 1.0};
+        const int nparts = (int)((N + 255) / 256);
+        std::vector<double> parts(nparts);
+        int q = 0, it = 0;
+        double r0 = -1, r = 0;
+        const int chunk = 10;
+        auto one = [&](int qq, bool norm) {
+            const void* l0 = J.lam[qq].p;
+            for (int st = 0; st < 3; ++st) {
+                const void* lk = st == 0 ? l0 : J.ls[st - 1].p;
+                enqueue_vjp(a, p, J.args(lk, J.u.p), s->stream);
+                void* out = st < 2 ? J.ls[st].p : J.lam[qq ^ 1].p;
+                enqueue_adjoint_update((int)N, l0, J.u.p, J.g.p, a.dt, alpha[st], a.relax, out,
+                                       (st == 2 && norm) ? (double*)J.partials.p : nullptr, s->stream);
+            }
+        };
+        // a graph of `chunk` iterations (even, so it starts and ends on lam[0])
+        cudaGraph_t gr;
+        cudaGraphExec_t ge;
+        AFX_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+        for (int k = 0; k < chunk; ++k) one(k & 1, k == chunk - 1);
+        AFX_CUDA(cudaStreamEndCapture(s->stream, &gr));
+        AFX_CUDA(cudaGraphInstantiate(&ge, gr, 0));
+        cudaGraphDestroy(gr);
+        AFX_CUDA(cudaEventRecord(s->ev0, s->stream));
+        try {
+            while (it < max_it) {
+                AFX_CUDA(cudaGraphLaunch(ge, s->stream));
+                it += chunk;
+                AFX_CUDA(cudaMemcpyAsync(parts.data(), J.partials.p, nparts * 8, cudaMemcpyDeviceToHost, s->stream));
+                AFX_CUDA(cudaStreamSynchronize(s->stream));
+                double t = 0;
+                for (double x : parts) t += x;
+                r = std::sqrt(t);
+                if (!(r == r) || r > 1.7976931348623157e308) throw Error(AFX_ERR_NONFINITE, "adjoint diverged");
+                if (r0 < 0) {
+                    // the first chunk's residual stands in for ||dJ/dq|| (lam = 0)
+                    std::vector<double> gh(4 * N);
+                    AFX_CUDA(cudaMemcpy(gh.data(), J.g.p, N * 32, cudaMemcpyDeviceToHost));
+                    double g2 = 0;
+                    for (double x : gh) g2 += x * x;
+                    r0 = std::sqrt(g2) > 0 ? std::sqrt(g2) : 1.0;
+                }
+                if (r / r0 < tol || s->stop.load()) break;
+            }
+        } catch (...) {
+            cudaGraphExecDestroy(ge);
+            throw;
+        }
+        AFX_CUDA(cudaEventRecord(s->ev1, s->stream));
+        cudaGraphExecDestroy(ge);
+        AFX_CUDA(cudaEventSynchronize(s->ev1));
+        float ms = 0;
+        AFX_CUDA(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+        s->last_sec = ms * 1e-3;
+        s->adj_parity = q;
+        if (iters) *iters = it;
+        if (res) *res = r / r0;
+        // dJ/dalpha, dJ/dM = explicit terms + lam . dR/dbq . dbq/d(alpha, M)
+        enqueue_vjp(a, p, J.args(J.lam[q].p, J.u.p), s->stream);
+        std::vector<double> bb(4 * B);
+        if (B) AFX_CUDA(cudaMemcpyAsync(bb.data(), J.bqbar.p, B * 32, cudaMemcpyDeviceToHost, s->stream));
+        AFX_CUDA(cudaStreamSynchronize(s->stream));
+        const double Jv = obj == "cl" ? cl : cd;
+        double da = obj == "cl" ? -cd : cl;  // d/dalpha of (cx, cy) at fixed forces
+        double dm = -2.0 * Jv / vf.mach;      // cp ~ 1/M^2
+        for (size_t b = 0; b < B; ++b) {
+            if (s->boundary_type[b] != BC_FARFIELD) continue;
+            double qb[4];
+            conservative(s->st, s->boundary_vars[b], qb);
+            const FarfieldVars& bv = s->boundary_vars[b];
+            const double kin = qb[3] - bv.p / (s->st.gamma - 1);
+            da += bb[4 * b + 1] * (-qb[2]) + bb[4 * b + 2] * qb[1];
+            if (bv.mach != 0)
+                dm += (bb[4 * b + 1] * qb[1] + bb[4 * b + 2] * qb[2] + bb[4 * b + 3] * 2.0 * kin) / bv.mach;
+        }
+        dJ[0] = da;
+        dJ[1] = dm;
+        if (s->stop.load()) {
+            s->stop.store(0);
+            throw Error(AFX_ERR_STOPPED, "stopped by request");
+        }
+    });
+}
+
+int afx_adjoint_state(afx_solver s, double* lam, long long n) {
+    return guarded([&] {
+        if (!s || !lam) throw Error(AFX_ERR_ARG, "null argument");
+        const size_t N = s->a.n_cells;
+        if (n != (long long)(4 * N)) throw Error(AFX_ERR_ARG, "size must be 4*n_real_cells");
+        auto& J = s->adjoint();
+        enqueue_permute_out((int)N, (const int*)s->d_cell_old.p, J.lam[s->adj_parity].p, s->d_stage.p, s->stream);
+        AFX_CUDA(cudaMemcpyAsync(lam, s->d_stage.p, N * 32, cudaMemcpyDefault, s->stream));
+        AFX_CUDA(cudaStreamSynchronize(s->stream));
     });
 }
 

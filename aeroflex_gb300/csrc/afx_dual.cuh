@@ -1,0 +1,48 @@
+// One-direction forward-mode dual number for the adjoint kernels.
+//
+// The face physics of afx_device.cuh is templated on its arithmetic type, so
+// instantiating it with Dual gives the exact directional derivative of a face
+// flux, ghost state or limiter value next to its value: one pass per input
+// direction, all in registers.  The adjoint kernels use these columns of the
+// local Jacobians on the fly and never store a Jacobian.
+//
+// Branches (entropy fix, limiter cases, characteristic boundary cases, min /
+// max) follow the value, so the derivative is the one of the active branch.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace afx {
+namespace dev {
+
+struct Dual {
+    double v, d;
+    __device__ __forceinline__ Dual() : v(0), d(0) {}
+    __device__ __forceinline__ Dual(double x) : v(x), d(0) {}
+    __device__ __forceinline__ Dual(double x, double dx) : v(x), d(dx) {}
+};
+
+__device__ __forceinline__ Dual operator+(Dual a, Dual b) { return Dual(a.v + b.v, a.d + b.d); }
+__device__ __forceinline__ Dual operator-(Dual a, Dual b) { return Dual(a.v - b.v, a.d - b.d); }
+__device__ __forceinline__ Dual operator-(Dual a) { return Dual(-a.v, -a.d); }
+__device__ __forceinline__ Dual operator*(Dual a, Dual b) { return Dual(a.v * b.v, a.d * b.v + a.v * b.d); }
+__device__ __forceinline__ Dual operator/(Dual a, Dual b) {
+    const double r = a.v / b.v;
+    return Dual(r, (a.d - r * b.d) / b.v);
+}
+__device__ __forceinline__ Dual& operator+=(Dual& a, Dual b) { return a = a + b; }
+__device__ __forceinline__ Dual& operator-=(Dual& a, Dual b) { return a = a - b; }
+__device__ __forceinline__ Dual& operator*=(Dual& a, Dual b) { return a = a * b; }
+__device__ __forceinline__ bool operator<(Dual a, Dual b) { return a.v < b.v; }
+__device__ __forceinline__ bool operator>(Dual a, Dual b) { return a.v > b.v; }
+__device__ __forceinline__ bool operator<=(Dual a, Dual b) { return a.v <= b.v; }
+__device__ __forceinline__ bool operator>=(Dual a, Dual b) { return a.v >= b.v; }
+
+__device__ __forceinline__ Dual dsqrt(Dual x) {
+    const double s = sqrt(x.v);
+    return Dual(s, x.d / (2.0 * s));
+}
+__device__ __forceinline__ Dual dabs(Dual x) { return x.v < 0 ? -x : x; }
+
+}  // namespace dev
+}  // namespace afx

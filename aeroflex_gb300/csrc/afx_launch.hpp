@@ -142,4 +142,26 @@ struct ForceArgs {
 };
 void enqueue_forces(const ForceArgs& f, cudaStream_t s);
 
+// Adjoint of the FP64 residual (afx_adjoint.cu): u = (dR/dq)^T v and
+// bqbar = (dR/dbq)^T v at the state of parity p.  Device-order arrays.
+struct AdjArgs {
+    const void* v = nullptr;  // d4 [N] weights on the residual
+    void* fbar = nullptr;     // d4 [2F] per face: adjoint of the left input, of the right input / boundary state
+    void* gbx = nullptr;      // d4 [N] adjoint of the x gradient
+    void* gby = nullptr;      // d4 [N] adjoint of the y gradient
+    void* qbar = nullptr;     // d4 [N] state adjoint before the neighbour terms
+    void* lw = nullptr;       // d4 [2N] limiter max/min weights
+    void* lt = nullptr;       // int4 [2N] limiter max/min target cells
+    void* u = nullptr;        // d4 [N] result
+    void* bqbar = nullptr;    // d4 [B] result (boundary states)
+};
+// gradients and limiter of state p (and the local time step when with_dt)
+void enqueue_adjoint_prep(const StepArgs& a, int p, bool with_dt, cudaStream_t s);
+void enqueue_vjp(const StepArgs& a, int p, const AdjArgs& j, cudaStream_t s);
+// lam_out = lam0 + alpha*relax*dt*(u + g); ||u + g||^2 block partials (256 cells per block) if partials
+void enqueue_adjoint_update(int n, const void* lam0, const void* u, const void* g, const void* dt, double alpha,
+                            double relax, void* lam_out, double* partials, cudaStream_t s);
+// g += dJ/dq for J = cx*fx + cy*fy over the patch of f (g zeroed by the caller)
+void enqueue_objective_grad(const ForceArgs& f, double cx, double cy, void* g, cudaStream_t s);
+
 }  // namespace afx

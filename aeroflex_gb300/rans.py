@@ -30,7 +30,8 @@ ABI_SYMBOLS = [
     "afx_residual_noalloc", "afx_batch_create", "afx_batch_free", "afx_batch_counts", "afx_batch_init_freestream",
     "afx_batch_set_state", "afx_batch_get_state", "afx_batch_iterate", "afx_batch_run_to_convergence",
     "afx_batch_case_history", "afx_batch_forces", "afx_batch_set_farfield", "afx_batch_autotune",
-    "afx_batch_last_device_seconds",
+    "afx_batch_last_device_seconds", "afx_residual_vjp", "afx_boundary_states", "afx_adjoint_solve",
+    "afx_adjoint_state",
 ]
 N_KERNEL_KINDS = 7
 
@@ -105,6 +106,10 @@ def lib():
         "afx_batch_set_farfield": (i, [vp, i, cp, d, d, d, d]),
         "afx_batch_autotune": (i, [vp, i, ctypes.c_char_p, i, P(i), P(d)]),
         "afx_batch_last_device_seconds": (i, [vp, P(d)]),
+        "afx_residual_vjp": (i, [vp, vp, vp, vp, vp, ll]),
+        "afx_boundary_states": (i, [vp, vp, ll]),
+        "afx_adjoint_solve": (i, [vp, cp, cp, d, i, vp, P(i), P(d)]),
+        "afx_adjoint_state": (i, [vp, vp, ll]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -237,6 +242,8 @@ class Solver:
         _check(lib().afx_solver_create(m.h, settings.h, ctypes.byref(h)))
         self.h = h
         self.n_real = m.nRealCells
+        self.n_boundary = m.n_boundary
+        self.mesh_boundary_names = m.boundary_names()
 
     def __del__(self):
         if getattr(self, "h", None) and _lib is not None:
@@ -297,6 +304,38 @@ class Solver:
         ms = ctypes.c_double()
         _check(lib().afx_autotune(self.h, int(iters), buf, 16, ctypes.byref(blk), ctypes.byref(ms)))
         return dict(variant=buf.value.decode(), block=blk.value, ms_per_iter=ms.value)
+
+    def residual_vjp(self, v, q=None):
+        """((dR/dq)^T v, (dR/dbq)^T v) at state q (default: the solver's);
+        the second is (n_boundary, 4)."""
+        v = np.ascontiguousarray(v, np.float64).reshape(-1)
+        u = np.empty_like(v)
+        bq = np.empty((self.n_boundary, 4), np.float64)
+        qp = None
+        if q is not None:
+            q = np.ascontiguousarray(q, np.float64).reshape(-1)
+            qp = _ptr(q)
+        _check(lib().afx_residual_vjp(self.h, qp, _ptr(v), _ptr(u), _ptr(bq) if self.n_boundary else None, v.size))
+        return u, bq
+
+    def boundary_states(self):
+        bq = np.empty((self.n_boundary, 4), np.float64)
+        _check(lib().afx_boundary_states(self.h, _ptr(bq), bq.size))
+        return bq
+
+    def adjoint_solve(self, patch="wall", objective="cl", tol=0.0, max_it=0):
+        """(dJ/dangle, dJ/dMach), iterations, relative adjoint residual."""
+        dJ = np.zeros(2, np.float64)
+        it = ctypes.c_int()
+        res = ctypes.c_double()
+        _check(lib().afx_adjoint_solve(self.h, patch.encode(), objective.encode(), float(tol), int(max_it), _ptr(dJ),
+                                       ctypes.byref(it), ctypes.byref(res)))
+        return (float(dJ[0]), float(dJ[1])), it.value, res.value
+
+    def adjoint_state(self):
+        lam = np.empty(4 * self.n_real, np.float64)
+        _check(lib().afx_adjoint_state(self.h, _ptr(lam), lam.size))
+        return lam
 
     def profile_iterations(self, n):
         """Per-kernel device time (CUDA events on the solver's stream) over n
@@ -362,9 +401,14 @@ class Batch:
         _check(lib().afx_batch_get_state(self.h, int(c), _ptr(out), out.size))
         return out
 
-    def iterate(self, n):
+    def iterate(self, n, raise_nonfinite=True):
+        """n iterations of every case; returns each case's last norm.  With
+        raise_nonfinite=False a case whose norm went non-finite (that case
+        then holds its state) shows as a non-finite entry instead of raising."""
         r = np.zeros(self.n, np.float64)
-        _check(lib().afx_batch_iterate(self.h, int(n), _ptr(r)))
+        rc = lib().afx_batch_iterate(self.h, int(n), _ptr(r))
+        if rc != 0 and not (rc == 4 and not raise_nonfinite):
+            _check(rc)
         return r
 
     def run_solver(self, tol=0.0, max_it=0):

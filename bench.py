@@ -95,11 +95,11 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def _setup_gpu(precision, m, q0, variant="auto"):
+def _setup_gpu(precision, m, q0, variant="auto", block=0):
     from aeroflex_gb300 import rans
     st = rans.Settings()
     st.set("solver", "explicit").set("precision", precision).set("start_cfl", 1.0).set("relaxation", 0.9)
-    st.set("kernel_variant", variant)
+    st.set("kernel_variant", variant).set("block_size", block)
     st.set_bc("farfield", "farfield", 1.0, MACH, 0.0, 1.0).set_bc("wall", "slip-wall")
     g = rans.Solver(m, st)
     g.init()
@@ -172,7 +172,7 @@ def run_lean(args):
     q0 = meshgen.density_bump_state(marr, mach=MACH)
     m = rans.mesh.from_arrays(marr)
     for precision in args.precision.split(","):
-        g = _setup_gpu(precision, m, q0, args.variant)
+        g = _setup_gpu(precision, m, q0, args.variant, args.block)
         g.iterate(args.warmup)
         g.iterate(args.steps)
         print(json.dumps({"precision": precision, "cells": m.nRealCells, "steps": args.steps,
@@ -327,6 +327,64 @@ def time_to_cl(budget_s=60.0):
     return out
 
 
+def batch_sweep(n_cases=256, K=100, K64=10, warmup=3):
+    """Batched polar sweep: ``n_cases`` NACA 4-digit cases (camber U[0,6]%,
+    thickness U[8,18]%, camber position U[0.2,0.6], log-uniform 5k-200k
+    quad cells, AoA U[-4,12] deg, Mach U[0.1,0.7], seed 4), Euler, CFL 1.
+    FP32-mixed batch (one launch per kernel for all cases, autotuned
+    variant/block) against the FP64 path run case by case, and the FP64
+    batch.  Rate = cells x 3 stages x iterations / device seconds."""
+    from aeroflex_gb300 import meshgen, rans
+
+    t0 = time.time()
+    cases = meshgen.polar_sweep_cases(n_cases, seed=4)
+    meshes = [rans.mesh.from_arrays(c["mesh"]) for c in cases]
+    ncell = np.array([m.nRealCells for m in meshes])
+    N = int(ncell.sum())
+
+    def settings(c, prec):
+        st = rans.Settings().set("solver", "explicit").set("precision", prec).set("start_cfl", 1.0)
+        st.set_bc("farfield", "farfield", 1.0, c["mach"], c["aoa_deg"] * 0.01745, 1.0).set_bc("wall", "slip-wall")
+        return st
+
+    out = {"cases": n_cases, "cells_total": N, "cells_min": int(ncell.min()), "cells_max": int(ncell.max()),
+           "workload": "polar sweep: %d NACA 4-digit O-meshes (quads, log-uniform 5k-200k cells), AoA U[-4,12] deg, "
+                       "Mach U[0.1,0.7], Euler, CFL 1, seed 4" % n_cases}
+    for prec, k in (("fp32-mixed", K), ("fp64", K64)):
+        b = rans.Batch(meshes, [settings(c, prec) for c in cases])
+        b.init()
+        tuned = b.autotune(2)
+        b.init()
+        b.iterate(warmup, raise_nonfinite=False)
+        b.init()
+        norms = b.iterate(k, raise_nonfinite=False)
+        sec = b.last_device_seconds()
+        out["batch_" + prec.replace("-", "_")] = {
+            "value": N * 3 * k / sec, "unit": "cell-residual evals/s", "ms_per_iteration": sec / k * 1e3,
+            "iterations": k, "tuned": tuned, "finite_cases": int(np.isfinite(norms).sum())}
+        del b
+    # the FP64 path case by case (the reference's polar loop, one solver per case)
+    dev, its = 0.0, K64
+    for c, m in zip(cases, meshes):
+        s = rans.Solver(m, settings(c, "fp64"))
+        s.init()
+        s.iterate(warmup)
+        s.init()
+        try:
+            s.iterate(its)
+        except rans.AfxError as e:  # a diverging case: its iterations still ran
+            if e.code != 4:
+                raise
+        dev += s.last_device_seconds()
+        del s
+    out["per_case_fp64"] = {"value": N * 3 * its / dev, "unit": "cell-residual evals/s",
+                            "ms_per_sweep_iteration": dev / its * 1e3, "iterations": its}
+    out["speedup_batch_fp32_mixed_vs_per_case_fp64"] = out["batch_fp32_mixed"]["value"] / out["per_case_fp64"]["value"]
+    out["speedup_batch_fp64_vs_per_case_fp64"] = out["batch_fp64"]["value"] / out["per_case_fp64"]["value"]
+    out["wall_s"] = time.time() - t0
+    return out
+
+
 def cpu_baseline(budget_s=12.0):
     """The oracle (plain-C++ restatement of the reference's explicit solver)
     on a 512 x 256 sample of the same generator, all host threads."""
@@ -385,11 +443,14 @@ def main():
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-cl", action="store_true", help="skip the time-to-C_L leg")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched polar-sweep leg")
+    ap.add_argument("--batch-cases", type=int, default=256)
     ap.add_argument("--nx", type=int, default=NX)
     ap.add_argument("--ny", type=int, default=NY)
     ap.add_argument("--lean", action="store_true", help="warm-up + timed iterations only (for ncu)")
     ap.add_argument("--precision", default="fp32-mixed", help="--lean: comma-separated precisions")
     ap.add_argument("--variant", default="auto", help="--lean: residual kernel variant (auto|gather|face|tile)")
+    ap.add_argument("--block", type=int, default=0, help="--lean: threads per block (0: the library's default)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank = int(os.environ.get("RANK", "0"))
@@ -447,6 +508,8 @@ def main():
         line["cpu_baseline"] = cpu_baseline()
     if not args.no_cl:
         line["time_to_cl"] = time_to_cl()
+    if not args.no_batch:
+        line["batch"] = batch_sweep(args.batch_cases)
     print(json.dumps(line))
 
 

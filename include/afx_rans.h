@@ -169,6 +169,34 @@ int afx_autotune(afx_solver s, int iters, char* variant, int cap, int* block, do
  * array's address; make it before any stream capture. */
 int afx_residual_noalloc(afx_solver s, const double* q_dev, double* R_dev, long long n);
 
+/* ---- Adjoint of the FP64 residual.  No counterpart in the reference (it
+ * has no adjoint).  R(q) is the residual afx_residual returns (first-stage
+ * semantics: gradients and limiter formed from q, solver.h:745-799); bq are
+ * the boundary states of the boundary edges (core.h:73-83 for farfield
+ * patches).  Inviscid flux only; first or second order; Venkatakrishnan or
+ * Michalak limiter (the derivative of the active branch: min/max and limiter
+ * cases follow the state).  FP64 solvers only (AFX_ERR_CONFIG otherwise).
+ *
+ * u = (dR/dq)^T v and, if bq_bar != NULL, bq_bar = (dR/dbq)^T v (4 per
+ * boundary edge, boundary order).  q: the state to linearise about, or NULL
+ * for the solver's state (the solver's state is not changed either way).
+ * q, v, u: 4*n_real doubles in reference cell order, host or device. */
+int afx_residual_vjp(afx_solver s, const double* q, const double* v, double* u, double* bq_bar, long long n);
+/* Boundary states bq (4 per boundary edge, conservative variables). */
+int afx_boundary_states(afx_solver s, double* bq, long long n);
+/* Sensitivities of a force coefficient J ("cl" or "cd" over `patch`,
+ * post.h:301-387) at the solver's (converged) state: solves
+ * (dR/dq)^T lam = -(dJ/dq)^T by pseudo-time iteration with the solver's own
+ * local time step and three stages, until ||(dR/dq)^T lam + dJ/dq|| falls
+ * below tol * ||dJ/dq|| (tol <= 0: 1e-10) or max_it iterations
+ * (<= 0: 100000).  dJ[0] = dJ/d(angle) per radian of the farfield angle,
+ * dJ[1] = dJ/d(Mach), both for every farfield-type boundary together.
+ * iters, res: iterations run and the final relative adjoint residual. */
+int afx_adjoint_solve(afx_solver s, const char* patch, const char* objective, double tol, int max_it, double* dJ,
+                      int* iters, double* res);
+/* The adjoint state lam of the last afx_adjoint_solve (reference order). */
+int afx_adjoint_state(afx_solver s, double* lam, long long n);
+
 /* ---- Batched load cases.  No single counterpart in the reference: its
  * polar sweep runs one case after another (src/rans/include/rans/rans.h:
  * 92-105 loops over the angles, multigrid.h:183-234 run_solver per case).  A
