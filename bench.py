@@ -217,7 +217,11 @@ def run_gpu(args):
         launches_per_iter = sum(v[1] for v in prof.values()) / n_prof
         entry = dict(value=evals, ms_per_step=sec / K * 1e3, steps=K, tuned=tuned,
                      kernels={k: dict(ms_total=v[0], launches=v[1], share=v[0] / tot) for k, v in prof.items()},
-                     roofline=dict(kernel=kname, bound="hbm", achieved=achieved, peak=hbm_peak, unit="GB/s",
+                     # the FP64 path is bound by the FP64 pipe (87% active under ncu,
+                     # profiles/k_face_flux_fp64_channel1024x512.md): its HBM
+                     # fraction is reported for reference only
+                     roofline=dict(kernel=kname, bound="hbm" if precision == "fp32-mixed" else "fp64-pipe",
+                                   achieved=achieved, peak=hbm_peak, unit="GB/s",
                                    frac=achieved / hbm_peak, peak_source=peak_kind,
                                    traffic=measured_traffic(kname, precision, N, F),
                                    algorithmic_bytes_per_launch=ab, launch_ms=per_launch_s * 1e3),
