@@ -247,6 +247,7 @@ struct afx_solver_s {
     AdjointBufs& adjoint() {
         if (!fp64) throw Error(AFX_ERR_CONFIG, "the adjoint needs an fp64 solver");
         if (a.visc != 0) throw Error(AFX_ERR_CONFIG, "the adjoint covers the inviscid flux only");
+        if (a.lsq) throw Error(AFX_ERR_CONFIG, "the adjoint covers the Green-Gauss gradient only");
         if (!adj) {
             const size_t N = a.n_cells, F = a.n_faces, B = std::max(a.n_bnd, 1);
             auto b = std::make_unique<AdjointBufs>();
@@ -835,8 +836,47 @@ static std::unique_ptr<afx_solver_s> make_solver(const HostMesh& m, const Device
         a.second = st.second_order ? 1 : 0;
         a.need_grad = (st.second_order || vc != VISC_INVISCID) ? 1 : 0;
         a.limiter = st.limiter == "michalak" ? 1 : 0;
-        if (st.gradient == "least-squares")
-            throw Error(AFX_ERR_CONFIG, "least-squares gradients are not available in this build");
+        std::vector<double> lsqw64;
+        if (st.gradient == "least-squares") {
+            // solver.h:402-422 per real cell, over its local edges in their
+            // own order: M = (d^T d)^-1 (closed form), weights M d_j
+            std::vector<int> face_of_edge(L.n_faces);
+            for (int f = 0; f < L.n_faces; ++f) face_of_edge[L.face_edge[f]] = f;
+            lsqw64.assign(8 * N, 0.0);
+            std::vector<int> code(N);
+            for (size_t i = 0; i < N; ++i) {
+                const uint32_t c = (uint32_t)L.cell_old[i];
+                const uint32_t nj = m.cellsIsTriangle[c] ? 3 : 4;
+                double dx[4], dy[4], a00 = 0, a01 = 0, a11 = 0;
+                int cd = (int)nj << 8;
+                for (uint32_t j = 0; j < nj; ++j) {
+                    const uint32_t e = m.cellsEdges[c][j];
+                    const uint32_t cn = m.edgesCells[e][0] == c ? m.edgesCells[e][1] : m.edgesCells[e][0];
+                    dx[j] = m.cellsCentersX[cn] - m.cellsCentersX[c];
+                    dy[j] = m.cellsCentersY[cn] - m.cellsCentersY[c];
+                    a00 += dx[j] * dx[j];
+                    a01 += dx[j] * dy[j];
+                    a11 += dy[j] * dy[j];
+                    int slot = -1;
+                    for (int sl = 0; sl < 4; ++sl) {
+                        const int v = L.cslot[4 * i + sl];
+                        if (v != 0 && (v > 0 ? v : -v) - 1 == face_of_edge[e]) slot = sl;
+                    }
+                    if (slot < 0) throw Error(AFX_ERR_MESH, "least squares: cell edge not among its faces");
+                    cd |= slot << (2 * j);
+                }
+                const double invdet = 1.0 / (a00 * a11 - a01 * a01);
+                const double M0 = a11 * invdet, M1 = -a01 * invdet, M2 = -a01 * invdet, M3 = a00 * invdet;
+                for (uint32_t j = 0; j < nj; ++j) {
+                    lsqw64[8 * i + 2 * j] = M0 * dx[j] + M1 * dy[j];
+                    lsqw64[8 * i + 2 * j + 1] = M2 * dx[j] + M3 * dy[j];
+                }
+                code[i] = cd;
+            }
+            a.lsq = 1;
+            a.lsqw = s->fp64 ? s->dupload(lsqw64) : s->dupload(cast_vec<float>(lsqw64));
+            a.lsqs = (const int*)s->dupload(code);
+        }
         // defaults from measurement on GB300: the FP64 path is FP64-pipe bound,
         // so each face flux is formed once; FP32-mixed re-forms fluxes in the
         // gather.  afx_autotune() times both on the actual mesh.
@@ -875,6 +915,7 @@ static std::unique_ptr<afx_solver_s> make_solver(const HostMesh& m, const Device
             b.fd0 = s->dupload(L.fd0);
             b.fd1 = s->dupload(L.fd1);
             b.ft = s->dupload(L.ft);
+            if (a.lsq) b.lsqw = s->dupload(lsqw64);
             b.bq = s->dalloc(std::max<size_t>(B, 1) * 32);
             for (int p = 0; p < 2; ++p) b.qsh[p] = b.qm[p];
             b.qs[0] = b.qs[1] = nullptr;  // residual launches read no stage state

@@ -105,6 +105,9 @@ struct KM {
     const V4<T>* __restrict__ bq;
     T gamma, R, mu, kheat, limk, cfl;
     int limiter;
+    int lsq;                          // least-squares gradient
+    const V2<T>* __restrict__ lsqw;   // 4 per cell: (M d_j) of local edge j
+    const int* __restrict__ lsqs;     // per cell: slot of local edge j (2 bits each), edge count << 8
 };
 
 __device__ __forceinline__ bool two_sided(int bt) { return bt == BT_INTERNAL || bt == BT_INOUT; }

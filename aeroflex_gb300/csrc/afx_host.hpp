@@ -74,6 +74,7 @@ struct HostMesh {
     std::vector<std::array<uint32_t, 4>> cellsNodes;
     std::vector<uint8_t> cellsIsTriangle;
     std::vector<std::array<uint32_t, 2>> edgesNodes, edgesCells;
+    std::vector<std::array<uint32_t, 4>> cellsEdges;  // real cells: edge of local edge j (nodes j, j+1)
     std::vector<double> edgesLengths, edgesNormalsX, edgesNormalsY, edgesCentersX, edgesCentersY;
     std::vector<double> cellsAreas, cellsCentersX, cellsCentersY;
     std::vector<uint32_t> boundaryEdges;

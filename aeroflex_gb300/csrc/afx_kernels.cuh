@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(256) k_prep(const KM<T> m, const V4<S>* __rest
                 }
                 eigsum += eig * Lg.x;
             }
-            if (GRAD) {
+            if (GRAD && !m.lsq) {
                 T qRv[4];
                 ghost_state(bt, m.gamma, n.x, n.y, q0c, q1c, qRv);
                 const T g = Lg.y;
@@ -120,10 +120,43 @@ __global__ void __launch_bounds__(256) k_prep(const KM<T> m, const V4<S>* __rest
     if (DTP) dt[i] = m.cfl * A / eigsum;
     if (!GRAD) return;
     T gxi[4], gyi[4];
+    if (m.lsq) {
+        // least squares (solver.h:470-513): g = sum_j (M d_j) (q_i - vars(q_i, q_n))
+        // over the cell's local edges j in their own order
+        const int code = __ldg(&m.lsqs[i]);
+        const int nj = code >> 8;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        gxi[k] = sgx[k] / A;
-        gyi[k] = sgy[k] / A;
+        for (int k = 0; k < 4; ++k) gxi[k] = gyi[k] = T(0);
+#pragma unroll 1
+        for (int j = 0; j < nj; ++j) {
+            const int s = (code >> (2 * j)) & 3;
+            const int fs = pick(sl, s);
+            const int f = (fs > 0 ? fs : -fs) - 1;
+            const int o = pick(nb, s);
+            const V2<T> n = __ldg(&m.fn[f]);
+            T qo[4], qR[4];
+            int bt = BT_INTERNAL;
+            if (o >= 0) {
+                ld4s(&q[o], qo);
+            } else {
+                bt = __ldg(&m.btype[-o - 1]);
+                ld4c<T>(&m.bq[-o - 1], qo);
+            }
+            ghost_state(bt, m.gamma, n.x, n.y, qi, qo, qR);
+            const V2<T> w = __ldg(&m.lsqw[4 * i + j]);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const T d = qi[k] - qR[k];
+                gxi[k] += w.x * d;
+                gyi[k] += w.y * d;
+            }
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            gxi[k] = sgx[k] / A;
+            gyi[k] = sgy[k] / A;
+        }
     }
     V4<T> vx, vy;
     st4(&vx, gxi);

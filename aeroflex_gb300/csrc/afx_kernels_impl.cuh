@@ -29,6 +29,9 @@ KM<T> make_km(const StepArgs& a) {
     m.limk = (T)a.limiter_k;
     m.cfl = (T)a.cfl;
     m.limiter = a.limiter;
+    m.lsq = a.lsq;
+    m.lsqw = (const V2<T>*)a.lsqw;
+    m.lsqs = a.lsqs;
     return m;
 }
 

@@ -77,6 +77,10 @@ struct StepArgs {
     int second = 1;       // second-order reconstruction
     int need_grad = 1;    // gradients computed (second order or viscous model)
     int limiter = 0;      // 0 Venkatakrishnan, 1 Michalak
+    // least-squares gradient (solver.h:402-422, 470-513) instead of Green-Gauss
+    int lsq = 0;
+    const void* lsqw = nullptr;  // T2 [4N]: (M d_j)^T of each local edge j of each cell
+    const int* lsqs = nullptr;   // [N]: cslot slot of local edge j in bits 2j..2j+1, edge count in bits 8..
     // residual kernel: 0 gather (cell gather re-forming fluxes), 1 face (face
     // kernel + ordered cell sum through HBM), 2 tile (shared-memory face tile)
     int variant = 1;

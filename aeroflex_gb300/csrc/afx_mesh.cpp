@@ -260,7 +260,6 @@ void HostMesh::finalize() {
 
     // first occurrence creates the edge; ids follow first-occurrence order
     const size_t H = key.size();
-    std::vector<uint32_t> edge_of_pos(4 * (size_t)N, 0xFFFFFFFFu);
     std::vector<uint8_t> first(4 * (size_t)N, 0);
     for (size_t s = 0; s < H;) {
         size_t t = s;
@@ -274,6 +273,7 @@ void HostMesh::finalize() {
         if (first[p]) id_of_first[p] = E++;
     edgesNodes.assign(E, {0, 0});
     edgesCells.assign(E, {0, 0});
+    cellsEdges.assign(N, {0, 0, 0, 0});
     std::vector<uint8_t> has_second(E, 0);
     std::vector<uint64_t> ukey(E);
     for (size_t s = 0; s < H;) {
@@ -289,6 +289,7 @@ void HostMesh::finalize() {
         // convert_node_face_info (mesh.h:344-375): the last other cell wins
         for (size_t u = s; u < t; ++u) {
             const uint32_t c = pos[u] / 4;
+            cellsEdges[c][pos[u] % 4] = eid;  // cellsEdges(i, j): local edge j of cell i
             if (c != c0) {
                 edgesCells[eid][1] = c;
                 has_second[eid] = 1;

@@ -29,6 +29,8 @@ def _warm_state(orc, m, bcs, n, **st):
     dict(viscosity="laminar"),
     dict(viscosity="laminar", second_order=False),
     dict(viscosity="spallart-allmaras"),
+    dict(gradient="least-squares"),
+    dict(gradient="least-squares", viscosity="laminar"),
 ])
 def test_residual_bitexact_omesh(afx, orc, variant):
     m, bcs = omesh_case(48, 24)
@@ -43,14 +45,16 @@ def test_residual_bitexact_omesh(afx, orc, variant):
     np.testing.assert_array_equal(Rg, Ro)
 
 
-@pytest.mark.parametrize("kv", ["gather", "face", "tile"])
+@pytest.mark.parametrize("kv", ["gather", "face", "tile", "lsq"])
 def test_residual_bitexact_shuffled_channel(afx, orc, kv):
     m, bcs, q = channel_case(64, 32)
-    so = oracle_solver(orc, m, bcs)
+    extra = dict(gradient="least-squares") if kv == "lsq" else {}
+    kv = "face" if kv == "lsq" else kv
+    so = oracle_solver(orc, m, bcs, **extra)
     so.init()
     so.set_q(q)
     Ro = so.residual()
-    g = gpu_solver(afx, m, bcs, kernel_variant=kv)
+    g = gpu_solver(afx, m, bcs, kernel_variant=kv, **extra)
     g.init()
     g.set_q(q)
     np.testing.assert_array_equal(g.residual(), Ro)
@@ -63,6 +67,8 @@ def test_residual_bitexact_shuffled_channel(afx, orc, kv):
     dict(kernel_variant="tile"), dict(kernel_variant="tile", block_size=64),
     dict(kernel_variant="tile", block_size=256, viscosity="laminar"),
     dict(kernel_variant="tile", second_order=False),
+    dict(gradient="least-squares"), dict(gradient="least-squares", kernel_variant="tile"),
+    dict(gradient="least-squares", kernel_variant="gather", limiter="michalak"),
 ])
 def test_iterations_bitexact(afx, orc, variant):
     m, bcs = omesh_case(48, 24)
