@@ -29,6 +29,12 @@ long long noalloc_max_cells();
 long long noalloc_max_faces();
 cudaError_t noalloc_residual_f64(const StepArgs& a, const int* cell_old, const double* q_ref, double* R_ref,
                                  cudaStream_t s);
+struct ImplicitEngine;
+ImplicitEngine* implicit_create(const StepArgs& a, bool f32, const std::vector<int>& colors, cudaStream_t s);
+void implicit_destroy(ImplicitEngine* e);
+void implicit_fill(ImplicitEngine* e, const StepArgs& a, int p, cudaStream_t s);
+int implicit_solve_update(ImplicitEngine* e, const StepArgs& a, int p, const double* b, double relax,
+                          cudaStream_t s);
 }  // namespace afx
 
 using namespace afx;
@@ -281,6 +287,7 @@ struct afx_solver_s {
 
     ~afx_solver_s() {
         if (stream) cudaStreamSynchronize(stream);
+        implicit_destroy(imp);
         for (auto& g : graphs) cudaGraphExecDestroy(g.second);
         for (auto& g : graphs64) cudaGraphExecDestroy(g.second);
         if (h_ctrl) cudaFreeHost(h_ctrl);
@@ -289,6 +296,63 @@ struct afx_solver_s {
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (stream) cudaStreamDestroy(stream);
+    }
+
+    // implicit solver (solver.h:852-1213), when settings.solver == "implicit"
+    ImplicitEngine* imp = nullptr;
+    void* imp_b = nullptr;  // FP64 right-hand side
+    int imp_lin_iters = 0;
+    // the FP64 machine of the implicit path: the solver itself (FP64) or its
+    // FP64 residual machine (FP32-mixed: FP32 Jacobian and Krylov vectors)
+    StepArgs& A64() { return fp64 ? a : a64; }
+
+    // ||RhoVector|| of parity p (fillRhoRHS, solver.h:1094-1152) into imp_b
+    double imp_rhs(int p) {
+        StepArgs r = A64();
+        r.Rq = imp_b;
+        enqueue_rhs_f64(r, p, stream);
+        const int nb = (r.n_cells + r.block - 1) / r.block;
+        std::vector<double> parts(nb);
+        AFX_CUDA(cudaMemcpyAsync(parts.data(), r.partials, nb * 8, cudaMemcpyDeviceToHost, stream));
+        AFX_CUDA(cudaStreamSynchronize(stream));
+        double t = 0;
+        for (double x : parts) t += x;
+        return std::sqrt(t);
+    }
+
+    // fill + compute + solve(relaxation, tol, rhs_iterations) of
+    // implicitSolver (solver.h:1000-1213) at the given CFL; returns the final
+    // ||RhoVector||, or -1 if the system could not be solved
+    double implicit_iteration(double cfl, double tol_abs) {
+        StepArgs m = A64();
+        m.cfl = cfl;
+        implicit_fill(imp, m, parity, stream);
+        imp_lin_iters = 0;
+        auto solve_update = [&]() {
+            const int it = implicit_solve_update(imp, A64(), parity, (const double*)imp_b, st.relaxation, stream);
+            if (it < 0) return false;
+            imp_lin_iters += it;
+            return true;
+        };
+        double err = imp_rhs(parity);
+        if (!(err == err)) return err;
+        if (err < tol_abs) return err;
+        const double err_ini = err;
+        if (!solve_update()) return -1;
+        for (int i = 0; i < st.rhs_iterations; ++i) {
+            err = imp_rhs(parity);
+            if (!(err == err)) return err;
+            if (err < tol_abs) return err;
+            if (err > 10 * err_ini) return err;
+            if (!solve_update()) return -1;
+        }
+        return imp_rhs(parity);
+    }
+
+    // after FP64 updates of the master state, the FP32 shadow follows
+    void imp_sync() {
+        if (!fp64) sync_shadow(parity);
+        pending_last = -1;
     }
 
     // get_boundary_variables, solver.h:597-611
@@ -904,7 +968,8 @@ static std::unique_ptr<afx_solver_s> make_solver(const HostMesh& m, const Device
         a.hist = (double*)s->dalloc(HIST_CAP * sizeof(double));
         s->d_cell_old.upload(L.cell_old.data(), N * sizeof(int), s->stream);
         s->set_launch(variant, block);
-        if (!s->fp64 && (st.fp64_correction_interval > 0 || st.fp64_finish)) {
+        const bool implicit = st.solver == "implicit";
+        if (!s->fp64 && (st.fp64_correction_interval > 0 || st.fp64_finish || implicit)) {
             // FP64 residual machine on the same FP64 master state
             s->corr_interval = st.fp64_correction_interval;
             StepArgs& b = s->a64;
@@ -949,6 +1014,24 @@ static std::unique_ptr<afx_solver_s> make_solver(const HostMesh& m, const Device
                 c.norms = a.norms;
                 c.block = N >= 600 * 256 ? 256 : (N >= 300 * 128 ? 128 : 64);
             }
+        }
+        if (implicit) {
+            // greedy colouring of the cell graph in device order (no two
+            // face neighbours share a colour): the Gauss-Seidel preconditioner
+            // updates one colour at a time
+            std::vector<int> color(N, -1);
+            for (size_t i = 0; i < N; ++i) {
+                unsigned used = 0;
+                for (int k = 0; k < 4; ++k) {
+                    const int o = L.cnbr[4 * i + k];
+                    if (L.cslot[4 * i + k] != 0 && o >= 0 && color[o] >= 0 && color[o] < 32) used |= 1u << color[o];
+                }
+                int c = 0;
+                while (used & (1u << c)) ++c;
+                color[i] = c;
+            }
+            s->imp_b = s->dalloc(N * 32);
+            s->imp = implicit_create(s->A64(), !s->fp64, color, s->stream);
         }
         s->d_stage.alloc(N * 32);
         AFX_CUDA(cudaHostAlloc((void**)&s->h_stage, N * 32, cudaHostAllocDefault));
@@ -1029,9 +1112,77 @@ int afx_residual(afx_solver s, double* R, long long n) {
     });
 }
 
+// The implicit path of afx_iterate / afx_run_to_convergence: the loop of
+// multigrid<implicitSolver>::run_solver (multigrid.h:240-293) with its CFL
+// ramp min(start + (i+1) slope, max); run_mode 0 runs n iterations without
+// the convergence test.
+static int implicit_run(afx_solver_s* s, int n, int run_mode, double tol, double* last) {
+    s->ensure_shadow();
+    s->materialize_qW();
+    s->set_ctrl(0, 0, 0);
+    StepArgs& A = s->A64();
+    if (A.ctrl != s->a.ctrl) AFX_CUDA(cudaMemsetAsync(A.ctrl, 0, sizeof(Ctrl), s->stream));
+    double err0 = 1.0;
+    if (run_mode == 1) {
+        double qf[4];
+        conservative(s->st, s->freestream(), qf);
+        enqueue_uniform_f64(A, s->parity, qf, s->stream);  // qW (last dQ) + freestream fluxes
+        Ctrl c;
+        AFX_CUDA(cudaMemcpyAsync(&c, A.ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, s->stream));
+        AFX_CUDA(cudaStreamSynchronize(s->stream));
+        err0 = c.err0;
+    }
+    AFX_CUDA(cudaEventRecord(s->ev0, s->stream));
+    double cfl = s->st.start_cfl, err = 0;
+    int i = 0;
+    s->hist.clear();
+    bool stopped = false;
+    do {
+        if (s->stop.load()) {
+            stopped = true;
+            break;
+        }
+        const double e = s->implicit_iteration(cfl, run_mode == 1 ? err0 * tol : 0.0);
+        if (!(e == e) || e > 1.7976931348623157e308) {
+            s->imp_sync();
+            throw Error(AFX_ERR_NONFINITE, "residual norm is not finite");
+        }
+        if (e < 0) {
+            s->imp_sync();
+            throw Error(AFX_ERR_DIVERGED, "implicit solve failed (singular diagonal block)");
+        }
+        err = e;
+        if (run_mode == 1) {
+            if (i == 0 && err > 2 * err0) err0 = err;
+            err /= err0;
+        }
+        cfl = std::min(s->st.start_cfl + (i + 1) * s->st.slope_cfl, s->st.max_cfl);
+        ++i;
+        s->hist.push_back(err);
+    } while ((run_mode == 0 ? i < n : (err > tol && i < n)));
+    AFX_CUDA(cudaEventRecord(s->ev1, s->stream));
+    AFX_CUDA(cudaEventSynchronize(s->ev1));
+    float ms = 0;
+    AFX_CUDA(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+    s->last_sec = ms * 1e-3;
+    s->imp_sync();
+    if (last) *last = err;
+    if (stopped) {
+        s->stop.store(0);
+        throw Error(AFX_ERR_STOPPED, "stopped by request");
+    }
+    return i;
+}
+
 int afx_iterate(afx_solver s, int n_iters, double* res_norm) {
     return guarded([&] {
         if (!s || n_iters < 0) throw Error(AFX_ERR_ARG, "bad argument");
+        if (s->imp) {
+            double e = 0;
+            if (n_iters > 0) implicit_run(s, n_iters, 0, 0, &e);
+            if (res_norm) *res_norm = e;
+            return;
+        }
         s->set_ctrl(0, n_iters, 0);
         const int done = s->run(n_iters, 0, 0);
         AFX_CUDA(cudaGetLastError());
@@ -1046,6 +1197,13 @@ int afx_run_to_convergence(afx_solver s, double tol, int max_it, int* iters, dou
         if (!s) throw Error(AFX_ERR_ARG, "null argument");
         if (tol <= 0) tol = s->st.tolerance;
         if (max_it <= 0) max_it = s->st.max_iterations;
+        if (s->imp) {
+            double e = 0;
+            const int n = implicit_run(s, max_it, 1, tol, &e);
+            if (iters) *iters = n;
+            if (err) *err = e;
+            return;
+        }
         s->materialize_qW();
         s->set_ctrl(1, max_it, tol);
         double qf[4];

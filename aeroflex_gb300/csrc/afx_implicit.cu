@@ -1,0 +1,654 @@
+// Implicit solver of the rans path on the GPU (implicitSolver, solver.h:852-1213,
+// driven by multigrid<implicitSolver>::run_solver, multigrid.h:240-293).
+//
+// Each iteration assembles the reference's linear system
+//     (A_i/dt_i I + sum_faces dF/dq L) dQ = -sum_faces F L
+// over the real cells (ghost rows are identity with a zero right-hand side in
+// the reference, so ghost unknowns stay zero and drop out), solves it with
+// restarted GMRES(30) to a relative tolerance of 1e-2 (at most 500 Krylov
+// iterations), and updates q += relaxation dQ, followed by up to
+// rhs_iterations chord steps with the same matrix.
+//
+// GB300 form:
+//   * block storage: one 4x4 diagonal block per cell and the two 4x4 flux
+//     Jacobians J = dF/dq_c0 L, K = dF/dq_c1 L per face (off-diagonal blocks
+//     K for row c0 and -J for row c1), never a general sparse matrix;
+//   * face Jacobians by the reference's one-sided differences
+//     (physics.h:533-578: step max(1e-6, 1e-6 |q|)), one thread per face;
+//   * preconditioner: one symmetric multicolour block Gauss-Seidel sweep
+//     (cells coloured so no two neighbours share a colour; forward then
+//     backward over the colours), a fixed linear operator, so right
+//     preconditioned GMRES applies unchanged;
+//   * Krylov vectors and matrix blocks in T = double (FP64 path) or float
+//     (FP32-mixed path: the right-hand side, the update and the norms stay
+//     FP64, so the iteration converges to the FP64 solution);
+//   * every reduction is a fixed-order two-level sum (deterministic);
+//     Arnoldi steps after convergence are skipped on the device, so a
+//     restart cycle is launched without host round trips.
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "afx_host.hpp"
+#include "afx_kernels_impl.cuh"
+
+namespace afx {
+namespace dev {
+
+constexpr int GM_M = 30;       // GMRES restart length (Eigen's default)
+constexpr int DOT_THREADS = 256;
+
+struct GmresCtl {
+    int stop;    // the current cycle has converged / ended
+    int k;       // Arnoldi steps taken in the current cycle
+    int iters;   // Krylov iterations of this solve
+    int pad;
+    double tol;  // absolute residual target
+    double res;  // current residual estimate
+    double H[(GM_M + 1) * GM_M];  // column-major: H[i + (GM_M + 1) * j]
+    double g[GM_M + 1], cs[GM_M], sn[GM_M], y[GM_M];
+    double hnext;  // h_{j+1,j} of the last step (before rotation)
+};
+
+template <class T> struct B4;
+template <> struct B4<double> { using type = d4; };
+template <> struct B4<float> { using type = float4; };
+
+__device__ __forceinline__ void ldb(const d4* p, double* v) { ld4(p, v); }
+__device__ __forceinline__ void ldb(const float4* p, double* v) {
+    const float4 a = *p;
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+}
+__device__ __forceinline__ void stb(d4* p, const double* v) { st4(p, v); }
+__device__ __forceinline__ void stb(float4* p, const double* v) {
+    *p = make_float4((float)v[0], (float)v[1], (float)v[2], (float)v[3]);
+}
+
+// 4x4 block (row-major, T) times a 4-vector, accumulated in double
+template <class T>
+__device__ __forceinline__ void bmv_add(const T* __restrict__ B, const double* x, double* y, const double sgn) {
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        double s = 0;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) s += (double)B[4 * r + c] * x[c];
+        y[r] += sgn * s;
+    }
+}
+
+// ------------------------------------------------------------- assembly
+// F of face f for the cell states (no reconstruction; the ghost side is the
+// stored boundary state), as the reference's flux functor evaluates it.
+template <int VISC>
+__device__ __forceinline__ void flux_cells(const KM<double>& m, const int bt, const double nx, const double ny,
+                                           const double* qL, const double* qR, const double* fgx, const double* fgy,
+                                           double* F) {
+    face_flux<double, VISC>(m, bt, nx, ny, qL, qR, fgx, fgy, F);
+}
+
+// calc_convective_jacobian (physics.h:533-578) times the face length:
+// J = dF/dq_L, K = dF/dq_R by one-sided differences with the reference's
+// step and its in-place perturb/restore of each component.
+template <class T, int VISC>
+__global__ void __launch_bounds__(128) k_imp_jac(const KM<double> m, const int n_faces, const d4* __restrict__ q,
+                                                 const d4* __restrict__ gx, const d4* __restrict__ gy,
+                                                 T* __restrict__ jf, const Ctrl* __restrict__ ctrl) {
+    if (ctrl->done) return;
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= n_faces) return;
+    const int2 cc = __ldg(&m.fcell[f]);
+    const double2 n = __ldg(&m.fn[f]);
+    const double L = __ldg(&m.fLg[f]).x;
+    double qL[4], qR[4];
+    ld4(&q[cc.x], qL);
+    int bt = BT_INTERNAL;
+    if (cc.y >= 0) {
+        ld4(&q[cc.y], qR);
+    } else {
+        bt = __ldg(&m.btype[-cc.y - 1]);
+        ld4(&m.bq[-cc.y - 1], qR);
+    }
+    double fgx[4] = {0, 0, 0, 0}, fgy[4] = {0, 0, 0, 0};
+    if (VISC == 1 && two_sided(bt)) {
+        double gx0[4], gy0[4], gx1[4] = {0, 0, 0, 0}, gy1[4] = {0, 0, 0, 0};
+        ld4(&gx[cc.x], gx0);
+        ld4(&gy[cc.x], gy0);
+        if (cc.y >= 0) {
+            ld4(&gx[cc.y], gx1);
+            ld4(&gy[cc.y], gy1);
+        }
+        face_gradient(qL, qR, gx0, gy0, gx1, gy1, ldv4<double>(&m.ft[f]), fgx, fgy);
+    }
+    double f0[4];
+    flux_cells<VISC>(m, bt, n.x, n.y, qL, qR, fgx, fgy, f0);
+    T* out = jf + 32 * (size_t)f;
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
+        const double upd = fmax(1e-6, fabs(qL[c]) * 1e-6);
+        qL[c] += upd;
+        double fp[4];
+        flux_cells<VISC>(m, bt, n.x, n.y, qL, qR, fgx, fgy, fp);
+        qL[c] -= upd;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) out[4 * r + c] = (T)((fp[r] - f0[r]) / upd * L);
+    }
+    if (cc.y >= 0) {
+#pragma unroll 1
+        for (int c = 0; c < 4; ++c) {
+            const double upd = fmax(1e-6, fabs(qR[c]) * 1e-6);
+            qR[c] += upd;
+            double fp[4];
+            flux_cells<VISC>(m, bt, n.x, n.y, qL, qR, fgx, fgy, fp);
+            qR[c] -= upd;
+#pragma unroll
+            for (int r = 0; r < 4; ++r) out[16 + 4 * r + c] = (T)((fp[r] - f0[r]) / upd * L);
+        }
+    }
+}
+
+// Diagonal block A/dt I + sum (own: J, other: -K) and its inverse (Gauss-
+// Jordan with partial pivoting, in double).
+template <class T>
+__global__ void __launch_bounds__(128) k_imp_diag(const KM<double> m, const double* __restrict__ dt,
+                                                  const T* __restrict__ jf, T* __restrict__ dblk,
+                                                  T* __restrict__ dinv, int* __restrict__ singular,
+                                                  const Ctrl* __restrict__ ctrl) {
+    if (ctrl->done) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.n_cells) return;
+    double D[16];
+    const double ad = __ldg(&m.area[i]) / __ldg(&dt[i]);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) D[k] = (k % 5 == 0) ? ad : 0.0;
+    const int4 sl = __ldg(&m.cslot[i]);
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+        const int fs = pick(sl, s);
+        if (fs == 0) continue;
+        const int f = (fs > 0 ? fs : -fs) - 1;
+        const T* B = jf + 32 * (size_t)f + (fs > 0 ? 0 : 16);
+        const double sg = fs > 0 ? 1.0 : -1.0;
+#pragma unroll
+        for (int k = 0; k < 16; ++k) D[k] += sg * (double)B[k];
+    }
+    T* Do = dblk + 16 * (size_t)i;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) Do[k] = (T)D[k];
+    double I[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) I[k] = (k % 5 == 0) ? 1.0 : 0.0;
+    for (int c = 0; c < 4; ++c) {
+        int p = c;
+        double best = fabs(D[4 * c + c]);
+        for (int r = c + 1; r < 4; ++r)
+            if (fabs(D[4 * r + c]) > best) {
+                best = fabs(D[4 * r + c]);
+                p = r;
+            }
+        if (!(best > 0)) {
+            *singular = 1;
+            return;
+        }
+        if (p != c)
+            for (int k = 0; k < 4; ++k) {
+                double t = D[4 * c + k];
+                D[4 * c + k] = D[4 * p + k];
+                D[4 * p + k] = t;
+                t = I[4 * c + k];
+                I[4 * c + k] = I[4 * p + k];
+                I[4 * p + k] = t;
+            }
+        const double inv = 1.0 / D[4 * c + c];
+        for (int k = 0; k < 4; ++k) {
+            D[4 * c + k] *= inv;
+            I[4 * c + k] *= inv;
+        }
+        for (int r = 0; r < 4; ++r) {
+            if (r == c) continue;
+            const double fct = D[4 * r + c];
+            for (int k = 0; k < 4; ++k) {
+                D[4 * r + k] -= fct * D[4 * c + k];
+                I[4 * r + k] -= fct * I[4 * c + k];
+            }
+        }
+    }
+    T* Io = dinv + 16 * (size_t)i;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) Io[k] = (T)I[k];
+}
+
+// --------------------------------------------------------- linear algebra
+// y = M x (gather over each cell's faces, edge order)
+template <class T>
+__global__ void __launch_bounds__(256) k_imp_spmv(const KM<double> m, const T* __restrict__ jf,
+                                                  const T* __restrict__ dblk, const typename B4<T>::type* __restrict__ x,
+                                                  typename B4<T>::type* __restrict__ y, const int* __restrict__ stop) {
+    if (stop && *stop) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.n_cells) return;
+    double xi[4], yi[4] = {0, 0, 0, 0};
+    ldb(&x[i], xi);
+    bmv_add(dblk + 16 * (size_t)i, xi, yi, 1.0);
+    const int4 sl = __ldg(&m.cslot[i]);
+    const int4 nb = __ldg(&m.cnbr[i]);
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+        const int fs = pick(sl, s);
+        const int o = pick(nb, s);
+        if (fs == 0 || o < 0) continue;
+        const int f = (fs > 0 ? fs : -fs) - 1;
+        double xo[4];
+        ldb(&x[o], xo);
+        // row c0: K x_c1; row c1: -J x_c0
+        bmv_add(jf + 32 * (size_t)f + (fs > 0 ? 16 : 0), xo, yi, fs > 0 ? 1.0 : -1.0);
+    }
+    stb(&y[i], yi);
+}
+
+// One colour of a block Gauss-Seidel sweep: x_i = D_i^-1 (r_i - sum O x_n)
+template <class T>
+__global__ void __launch_bounds__(256) k_imp_gs(const KM<double> m, const T* __restrict__ jf,
+                                                const T* __restrict__ dinv, const int* __restrict__ cells,
+                                                const int n, const typename B4<T>::type* __restrict__ r,
+                                                typename B4<T>::type* __restrict__ x, const int* __restrict__ stop) {
+    if (stop && *stop) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int i = __ldg(&cells[t]);
+    double s[4];
+    ldb(&r[i], s);
+    const int4 sl = __ldg(&m.cslot[i]);
+    const int4 nb = __ldg(&m.cnbr[i]);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int fs = pick(sl, k);
+        const int o = pick(nb, k);
+        if (fs == 0 || o < 0) continue;
+        const int f = (fs > 0 ? fs : -fs) - 1;
+        double xo[4];
+        ldb(&x[o], xo);
+        bmv_add(jf + 32 * (size_t)f + (fs > 0 ? 16 : 0), xo, s, fs > 0 ? -1.0 : 1.0);
+    }
+    double xi[4] = {0, 0, 0, 0};
+    bmv_add(dinv + 16 * (size_t)i, s, xi, 1.0);
+    stb(&x[i], xi);
+}
+
+template <class T>
+__global__ void k_imp_zero(const int n4, T* __restrict__ x, const int* __restrict__ stop) {
+    if (stop && *stop) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n4) x[i] = T(0);
+}
+
+// Partial dot products of w with v_0..v_{nv-1} (v_j = V + j*n): block b
+// writes part[b*nv + j]
+template <class T>
+__global__ void __launch_bounds__(DOT_THREADS) k_imp_dots(const int n, const int nv, const T* __restrict__ V,
+                                                          const T* __restrict__ w, double* __restrict__ part,
+                                                          const int* __restrict__ stop) {
+    __shared__ double sh[32];
+    if (stop && *stop) return;
+    for (int j = 0; j < nv; ++j) {
+        double s = 0;
+        const T* v = V + (size_t)j * n;
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+            s += (double)v[i] * (double)w[i];
+        const double t = block_sum(s, sh);
+        if (threadIdx.x == 0) part[(size_t)blockIdx.x * nv + j] = t;
+        __syncthreads();
+    }
+}
+
+// Fixed-order sum of the partials: out[j] = sum_b part[b*nv + j]
+__global__ void k_imp_dots_final(const int nb, const int nv, const double* __restrict__ part, double* __restrict__ out,
+                                 const int* __restrict__ stop) {
+    __shared__ double sh[32];
+    if (stop && *stop) return;
+    for (int j = 0; j < nv; ++j) {
+        double s = 0;
+        for (int b = threadIdx.x; b < nb; b += blockDim.x) s += part[(size_t)b * nv + j];
+        const double t = block_sum(s, sh);
+        if (threadIdx.x == 0) out[j] = t;
+        __syncthreads();
+    }
+}
+
+// w -= sum_j h[j] v_j
+template <class T>
+__global__ void __launch_bounds__(256) k_imp_orth(const int n, const int nv, const T* __restrict__ V,
+                                                  const double* __restrict__ h, T* __restrict__ w,
+                                                  const int* __restrict__ stop) {
+    if (stop && *stop) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double s = (double)w[i];
+    for (int j = 0; j < nv; ++j) s -= h[j] * (double)V[(size_t)j * n + i];
+    w[i] = (T)s;
+}
+
+// v = w * scale[0] (scale read from the device)
+template <class T>
+__global__ void __launch_bounds__(256) k_imp_scale(const int n, const T* __restrict__ w, const double* __restrict__ scale,
+                                                   T* __restrict__ v, const int* __restrict__ stop) {
+    if (stop && *stop) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) v[i] = (T)((double)w[i] * scale[0]);
+}
+
+// Arnoldi step j, classical Gram-Schmidt twice: h1 (first pass) and h2
+// (second pass) are summed into column j; then Givens rotations and the
+// residual estimate.  One thread.
+__global__ void k_imp_arnoldi(GmresCtl* c, const int j, const double* __restrict__ h1, const double* __restrict__ h2,
+                              const double* __restrict__ ww, double* __restrict__ scale) {
+    if (c->stop) return;
+    double* H = c->H + (GM_M + 1) * j;
+    for (int i = 0; i <= j; ++i) H[i] = h1[i] + h2[i];
+    const double hn = sqrt(fmax(ww[0], 0.0));
+    H[j + 1] = hn;
+    c->hnext = hn;
+    scale[0] = hn > 0 ? 1.0 / hn : 0.0;
+    for (int i = 0; i < j; ++i) {
+        const double a = H[i], b = H[i + 1];
+        H[i] = c->cs[i] * a + c->sn[i] * b;
+        H[i + 1] = -c->sn[i] * a + c->cs[i] * b;
+    }
+    const double a = H[j], b = H[j + 1];
+    const double r = sqrt(a * a + b * b);
+    const double cs = r > 0 ? a / r : 1.0, sn = r > 0 ? b / r : 0.0;
+    c->cs[j] = cs;
+    c->sn[j] = sn;
+    H[j] = r;
+    H[j + 1] = 0;
+    c->g[j + 1] = -sn * c->g[j];
+    c->g[j] = cs * c->g[j];
+    c->res = fabs(c->g[j + 1]);
+    c->k = j + 1;
+    c->iters += 1;
+    if (c->res <= c->tol || j + 1 == GM_M || hn == 0) c->stop = 1;
+}
+
+// Back substitution R y = g over the k steps of the cycle (one thread)
+__global__ void k_imp_solve_y(GmresCtl* c) {
+    const int k = c->k;
+    for (int i = k - 1; i >= 0; --i) {
+        double s = c->g[i];
+        for (int l = i + 1; l < k; ++l) s -= c->H[i + (GM_M + 1) * l] * c->y[l];
+        const double d = c->H[i + (GM_M + 1) * i];
+        c->y[i] = d != 0 ? s / d : 0.0;
+    }
+}
+
+// t = sum_j y_j v_j over the k steps
+template <class T>
+__global__ void __launch_bounds__(256) k_imp_lincomb(const int n, const T* __restrict__ V, const GmresCtl* __restrict__ c,
+                                                     T* __restrict__ t) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double s = 0;
+    for (int j = 0; j < c->k; ++j) s += c->y[j] * (double)V[(size_t)j * n + i];
+    t[i] = (T)s;
+}
+
+// x (double) += z;  r = b - y  (b double), both 4N long
+template <class T>
+__global__ void __launch_bounds__(256) k_imp_addx(const int n, const T* __restrict__ z, double* __restrict__ x) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] += (double)z[i];
+}
+template <class T>
+__global__ void __launch_bounds__(256) k_imp_resid(const int n, const double* __restrict__ b, const T* __restrict__ y,
+                                                   T* __restrict__ r) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) r[i] = (T)(b[i] - (double)y[i]);
+}
+template <class T>
+__global__ void __launch_bounds__(256) k_imp_cast(const int n, const double* __restrict__ x, T* __restrict__ t) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) t[i] = (T)x[i];
+}
+
+// q += relax * dq over the real cells; dq also becomes qW (the reference's
+// qW holds the last linear solution, read by get_uniform_residual)
+__global__ void __launch_bounds__(256) k_imp_update(const int n, const double* __restrict__ dq, const double relax,
+                                                    double* __restrict__ q, double* __restrict__ qW) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    q[i] += dq[i] * relax;
+    qW[i] = dq[i];
+}
+
+// GMRES initialisation of a cycle: g = (beta, 0, ...), stop = beta <= tol
+__global__ void k_imp_cycle_init(GmresCtl* c, const double* __restrict__ rr, double* __restrict__ scale, const int first,
+                                 const double rel_tol) {
+    const double beta = sqrt(fmax(rr[0], 0.0));
+    if (first) {
+        c->tol = rel_tol * beta;
+        c->iters = 0;
+    }
+    for (int i = 0; i <= GM_M; ++i) c->g[i] = 0;
+    c->g[0] = beta;
+    c->res = beta;
+    c->k = 0;
+    c->stop = (beta <= c->tol) ? 1 : 0;
+    scale[0] = beta > 0 ? 1.0 / beta : 0.0;
+}
+
+}  // namespace dev
+
+// ----------------------------------------------------------------- host
+namespace {
+
+inline int nb_(long long n, int b) { return (int)((n + b - 1) / b); }
+
+}  // namespace
+
+struct ImplicitEngine {
+    bool f32 = false;
+    int N = 0, F = 0, n4 = 0;
+    int n_colors = 0;
+    std::vector<int> color_ptr;
+    void* jf = nullptr;
+    void* dblk = nullptr;
+    void* dinv = nullptr;
+    int* color_cells = nullptr;
+    int* singular = nullptr;
+    void* V = nullptr;     // (GM_M+1) x 4N
+    void* w = nullptr;     // 4N
+    void* z = nullptr;     // 4N
+    void* t = nullptr;     // 4N
+    double* x = nullptr;   // 4N, the solution dQ
+    double* part = nullptr;
+    double* small = nullptr;  // h1[GM_M+1], h2[GM_M+1], ww, scale
+    int nbd = 0;
+    dev::GmresCtl* ctl = nullptr;
+    dev::GmresCtl* h_ctl = nullptr;
+    int last_iters = 0;
+
+    size_t ts() const { return f32 ? 4 : 8; }
+};
+
+ImplicitEngine* implicit_create(const StepArgs& a, bool f32, const std::vector<int>& colors, cudaStream_t s) {
+    auto* e = new ImplicitEngine();
+    e->f32 = f32;
+    e->N = a.n_cells;
+    e->F = a.n_faces;
+    e->n4 = 4 * a.n_cells;
+    int nc = 0;
+    for (int c : colors) nc = std::max(nc, c + 1);
+    e->n_colors = nc;
+    e->color_ptr.assign(nc + 1, 0);
+    for (int c : colors) e->color_ptr[c + 1]++;
+    for (int c = 0; c < nc; ++c) e->color_ptr[c + 1] += e->color_ptr[c];
+    std::vector<int> cells(colors.size()), fill(e->color_ptr.begin(), e->color_ptr.end() - 1);
+    for (int i = 0; i < (int)colors.size(); ++i) cells[fill[colors[i]]++] = i;
+    const size_t T = e->ts();
+    auto chk = [](cudaError_t r) {
+        if (r != cudaSuccess) throw Error(7, std::string("implicit solver: ") + cudaGetErrorString(r));
+    };
+    chk(cudaMalloc(&e->jf, (size_t)e->F * 32 * T));
+    chk(cudaMalloc(&e->dblk, (size_t)e->N * 16 * T));
+    chk(cudaMalloc(&e->dinv, (size_t)e->N * 16 * T));
+    chk(cudaMalloc((void**)&e->color_cells, std::max<size_t>(cells.size(), 1) * sizeof(int)));
+    chk(cudaMalloc((void**)&e->singular, sizeof(int)));
+    chk(cudaMalloc(&e->V, (size_t)(dev::GM_M + 1) * e->n4 * T));
+    chk(cudaMalloc(&e->w, (size_t)e->n4 * T));
+    chk(cudaMalloc(&e->z, (size_t)e->n4 * T));
+    chk(cudaMalloc(&e->t, (size_t)e->n4 * T));
+    chk(cudaMalloc((void**)&e->x, (size_t)e->n4 * 8));
+    e->nbd = std::min(1024, nb_(e->n4, dev::DOT_THREADS * 4));
+    chk(cudaMalloc((void**)&e->part, (size_t)e->nbd * (dev::GM_M + 1) * 8));
+    chk(cudaMalloc((void**)&e->small, (2 * (dev::GM_M + 1) + 2) * 8));
+    chk(cudaMalloc((void**)&e->ctl, sizeof(dev::GmresCtl)));
+    chk(cudaHostAlloc((void**)&e->h_ctl, sizeof(dev::GmresCtl), cudaHostAllocDefault));
+    chk(cudaMemcpyAsync(e->color_cells, cells.data(), cells.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    chk(cudaMemsetAsync(e->jf, 0, (size_t)e->F * 32 * T, s));
+    chk(cudaStreamSynchronize(s));
+    return e;
+}
+
+void implicit_destroy(ImplicitEngine* e) {
+    if (!e) return;
+    for (void* p : {e->jf, e->dblk, e->dinv, (void*)e->color_cells, (void*)e->singular, e->V, e->w, e->z, e->t,
+                    (void*)e->x, (void*)e->part, (void*)e->small, (void*)e->ctl})
+        if (p) cudaFree(p);
+    if (e->h_ctl) cudaFreeHost(e->h_ctl);
+    delete e;
+}
+
+// fillRhoLHS (solver.h:1016-1090): dt from the state of parity p at the CFL
+// in a.cfl, face Jacobians, diagonal blocks and their inverses.
+void implicit_fill(ImplicitEngine* e, const StepArgs& a0, int p, cudaStream_t s) {
+    using namespace dev;
+    StepArgs a = a0;
+    a.variant = 0;  // the prep that also forms dt
+    a.second = 0;   // gradients only when viscous (solver.h:1023-1026)
+    a.need_grad = a.visc == 1 ? 1 : 0;
+    const KM<double> m = make_km<double>(a);
+    launch_prep<double, double>(a, m, (const d4*)a.qm[p], s);
+    cudaMemsetAsync(e->singular, 0, sizeof(int), s);
+    const d4* q = (const d4*)a.qm[p];
+    const int nf = nb_(a.n_faces, 128), nc = nb_(a.n_cells, 128);
+    if (e->f32) {
+        if (a.visc == 1)
+            k_imp_jac<float, 1><<<nf, 128, 0, s>>>(m, a.n_faces, q, (const d4*)a.gx, (const d4*)a.gy, (float*)e->jf,
+                                                   a.ctrl);
+        else
+            k_imp_jac<float, 0><<<nf, 128, 0, s>>>(m, a.n_faces, q, (const d4*)a.gx, (const d4*)a.gy, (float*)e->jf,
+                                                   a.ctrl);
+        k_imp_diag<float><<<nc, 128, 0, s>>>(m, (const double*)a.dt, (const float*)e->jf, (float*)e->dblk,
+                                             (float*)e->dinv, e->singular, a.ctrl);
+    } else {
+        if (a.visc == 1)
+            k_imp_jac<double, 1><<<nf, 128, 0, s>>>(m, a.n_faces, q, (const d4*)a.gx, (const d4*)a.gy,
+                                                    (double*)e->jf, a.ctrl);
+        else
+            k_imp_jac<double, 0><<<nf, 128, 0, s>>>(m, a.n_faces, q, (const d4*)a.gx, (const d4*)a.gy,
+                                                    (double*)e->jf, a.ctrl);
+        k_imp_diag<double><<<nc, 128, 0, s>>>(m, (const double*)a.dt, (const double*)e->jf, (double*)e->dblk,
+                                              (double*)e->dinv, e->singular, a.ctrl);
+    }
+}
+
+namespace {
+
+template <class T>
+struct Ops {
+    ImplicitEngine* e;
+    const StepArgs& a;
+    cudaStream_t s;
+    dev::KM<double> m;
+    using V4 = typename dev::B4<T>::type;
+    Ops(ImplicitEngine* e_, const StepArgs& a_, cudaStream_t s_) : e(e_), a(a_), s(s_), m(dev::make_km<double>(a_)) {}
+    T* vec(int j) const { return (T*)e->V + (size_t)j * e->n4; }
+    int* stop() const { return &e->ctl->stop; }
+    void spmv(const T* x, T* y, const int* st) const {
+        dev::k_imp_spmv<T><<<nb_(e->N, 256), 256, 0, s>>>(m, (const T*)e->jf, (const T*)e->dblk, (const V4*)x, (V4*)y,
+                                                          st);
+    }
+    // one symmetric multicolour block Gauss-Seidel sweep from x = 0
+    void precond(const T* r, T* x, const int* st) const {
+        dev::k_imp_zero<T><<<nb_(e->n4, 256), 256, 0, s>>>(e->n4, x, st);
+        for (int pass = 0; pass < 2; ++pass)
+            for (int k = 0; k < e->n_colors; ++k) {
+                const int c = pass == 0 ? k : e->n_colors - 1 - k;
+                const int c0 = e->color_ptr[c], cn = e->color_ptr[c + 1] - c0;
+                if (cn == 0) continue;
+                dev::k_imp_gs<T><<<nb_(cn, 256), 256, 0, s>>>(m, (const T*)e->jf, (const T*)e->dinv,
+                                                              e->color_cells + c0, cn, (const V4*)r, (V4*)x, st);
+            }
+    }
+    void dots(int nv, const T* V, const T* w, double* out, const int* st) const {
+        dev::k_imp_dots<T><<<e->nbd, dev::DOT_THREADS, 0, s>>>(e->n4, nv, V, w, e->part, st);
+        dev::k_imp_dots_final<<<1, 256, 0, s>>>(e->nbd, nv, e->part, out, st);
+    }
+};
+
+template <class T>
+int gmres(ImplicitEngine* e, const StepArgs& a, const double* b, cudaStream_t s, int max_iters) {
+    using namespace dev;
+    Ops<T> o(e, a, s);
+    const int n = e->n4;
+    double* h1 = e->small;
+    double* h2 = e->small + (GM_M + 1);
+    double* ww = e->small + 2 * (GM_M + 1);
+    double* scale = ww + 1;
+    cudaMemsetAsync(e->x, 0, (size_t)n * 8, s);
+    int total = 0;
+    for (int cycle = 0; total < max_iters; ++cycle) {
+        // r = b - M x (x = 0 on the first cycle)
+        T* v0 = o.vec(0);
+        if (cycle == 0) {
+            k_imp_cast<T><<<nb_(n, 256), 256, 0, s>>>(n, b, v0);
+        } else {
+            k_imp_cast<T><<<nb_(n, 256), 256, 0, s>>>(n, e->x, (T*)e->t);
+            o.spmv((const T*)e->t, (T*)e->w, nullptr);
+            k_imp_resid<T><<<nb_(n, 256), 256, 0, s>>>(n, b, (const T*)e->w, v0);
+        }
+        o.dots(1, v0, v0, ww, nullptr);
+        k_imp_cycle_init<<<1, 1, 0, s>>>(e->ctl, ww, scale, cycle == 0, 1e-2);
+        k_imp_scale<T><<<nb_(n, 256), 256, 0, s>>>(n, v0, scale, v0, o.stop());
+        for (int j = 0; j < GM_M; ++j) {
+            o.precond(o.vec(j), (T*)e->z, o.stop());
+            o.spmv((const T*)e->z, (T*)e->w, o.stop());
+            o.dots(j + 1, o.vec(0), (const T*)e->w, h1, o.stop());
+            k_imp_orth<T><<<nb_(n, 256), 256, 0, s>>>(n, j + 1, o.vec(0), h1, (T*)e->w, o.stop());
+            o.dots(j + 1, o.vec(0), (const T*)e->w, h2, o.stop());
+            k_imp_orth<T><<<nb_(n, 256), 256, 0, s>>>(n, j + 1, o.vec(0), h2, (T*)e->w, o.stop());
+            o.dots(1, (const T*)e->w, (const T*)e->w, ww, o.stop());
+            k_imp_arnoldi<<<1, 1, 0, s>>>(e->ctl, j, h1, h2, ww, scale);
+            k_imp_scale<T><<<nb_(n, 256), 256, 0, s>>>(n, (const T*)e->w, scale, o.vec(j + 1), o.stop());
+        }
+        cudaMemcpyAsync(e->h_ctl, e->ctl, sizeof(GmresCtl), cudaMemcpyDeviceToHost, s);
+        cudaStreamSynchronize(s);
+        const int k = e->h_ctl->k;
+        if (k > 0) {
+            k_imp_solve_y<<<1, 1, 0, s>>>(e->ctl);
+            k_imp_lincomb<T><<<nb_(n, 256), 256, 0, s>>>(n, o.vec(0), e->ctl, (T*)e->t);
+            o.precond((const T*)e->t, (T*)e->z, nullptr);
+            k_imp_addx<T><<<nb_(n, 256), 256, 0, s>>>(n, (const T*)e->z, e->x);
+        }
+        total = e->h_ctl->iters;
+        if (e->h_ctl->res <= e->h_ctl->tol || k == 0) break;
+    }
+    return total;
+}
+
+}  // namespace
+
+// Solves M dQ = b (b: FP64 right-hand side over the real cells, AoS) and
+// applies q += relax dQ to the FP64 state; dQ is also copied to qW.
+// Returns the Krylov iterations, or -1 if a diagonal block was singular.
+int implicit_solve_update(ImplicitEngine* e, const StepArgs& a, int p, const double* b, double relax,
+                          cudaStream_t s) {
+    int sing = 0;
+    cudaMemcpyAsync(&sing, e->singular, sizeof(int), cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    if (sing) return -1;
+    const int it = e->f32 ? gmres<float>(e, a, b, s, 500) : gmres<double>(e, a, b, s, 500);
+    dev::k_imp_update<<<nb_(e->n4, 256), 256, 0, s>>>(e->n4, e->x, relax, (double*)a.qm[p], (double*)a.Rq);
+    e->last_iters = it;
+    return it;
+}
+
+}  // namespace afx

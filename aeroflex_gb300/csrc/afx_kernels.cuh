@@ -388,7 +388,7 @@ __device__ __forceinline__ void stage_epilogue(const StageOut<T, S>& o, const in
         T R[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) R[k] = Rsum[k] / A;
-        if (o.case_done && o.mode != 2 && __ldg(&o.case_done[__ldg(&o.case_of[i])])) {
+        if (o.case_done && o.mode < 2 && __ldg(&o.case_done[__ldg(&o.case_of[i])])) {
             // a case that has stopped keeps its state
             if (o.mode == 0) {
                 if (sizeof(T) == 4) {
@@ -418,6 +418,13 @@ __device__ __forceinline__ void stage_epilogue(const StageOut<T, S>& o, const in
         } else if (o.mode == 2) {
             double Rd[4] = {(double)R[0], (double)R[1], (double)R[2], (double)R[3]};
             st4(&o.Rq[i], Rd);
+        } else if (o.mode == 3) {
+            // implicit right-hand side: the face sums, not divided by the area
+            // (solver.h:1079-1152), and their squared norm
+            double Rd[4] = {(double)Rsum[0], (double)Rsum[1], (double)Rsum[2], (double)Rsum[3]};
+            st4(&o.Rq[i], Rd);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) sq += Rd[k] * Rd[k];
         } else if (sizeof(T) == 4) {
             stage_epilogue_mixed<S>(o, i, R, dti, sq);
         } else {
@@ -450,7 +457,7 @@ __device__ __forceinline__ void stage_epilogue(const StageOut<T, S>& o, const in
             st4(&o.Rq[i], Rd);
         }
     }
-    if (o.mode == 1) {
+    if (o.mode == 1 || o.mode == 3) {
         const double t = block_sum(sq, sh);
         if (threadIdx.x == 0) o.partials[blockIdx.x] = t;
     }
@@ -564,7 +571,7 @@ __global__ void __launch_bounds__(256) k_resid_gather(const KM<T> m, const V4<S>
             }
         }
         A = __ldg(&m.area[i]);
-        if (o.mode != 2) dti = o.dt[i];
+        if (o.mode < 2) dti = o.dt[i];
     }
     stage_epilogue<T, S>(o, i, active, Rs, A, dti, o.mode == 1 ? extra : 0.0, sh);
 }
@@ -735,7 +742,7 @@ __global__ void __launch_bounds__(256) k_resid_tile(const KM<T> m, const TileVie
         if (EIG) {
             dti = m.cfl * A / eigsum;
             o.dt[i] = dti;
-        } else if (o.mode != 2) {
+        } else if (o.mode < 2) {
             dti = o.dt[i];
         }
     }
@@ -787,7 +794,7 @@ __global__ void __launch_bounds__(256) k_cell_sum(const KM<T> m, const V4<T>* __
         if (DT) {
             dti = m.cfl * A / eigsum;
             o.dt[i] = dti;
-        } else if (o.mode != 2) {
+        } else if (o.mode < 2) {
             dti = o.dt[i];
         }
     }

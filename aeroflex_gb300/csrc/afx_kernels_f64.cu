@@ -9,6 +9,7 @@ namespace afx {
 
 void enqueue_iteration_f64(const StepArgs& a, int p, cudaStream_t s) { dev::iteration<double, double, false>(a, p, s); }
 void enqueue_residual_f64(const StepArgs& a, int p, cudaStream_t s) { dev::residual<double, double>(a, p, s); }
+void enqueue_rhs_f64(const StepArgs& a, int p, cudaStream_t s) { dev::rhs<double, double>(a, p, s); }
 void enqueue_last_stage_residual_f64(const StepArgs& a, int p, cudaStream_t s) {
     dev::last_stage_residual<double, double>(a, p, s);
 }

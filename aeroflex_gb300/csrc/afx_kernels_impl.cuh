@@ -196,6 +196,18 @@ void residual(const StepArgs& a, int p, cudaStream_t s) {
     launch_stage<T, S>(a, m, q, q, o, false, s);
 }
 
+// Implicit right-hand side of state parity p (first-stage reconstruction,
+// face sums not divided by the area) -> Rq, ||.||^2 block partials.
+template <class T, class S>
+void rhs(const StepArgs& a, int p, cudaStream_t s) {
+    const KM<T> m = make_km<T>(a);
+    const V4<S>* q = (const V4<S>*)a.qsh[p];
+    launch_prep<T, S>(a, m, q, s);
+    StageOut<T, S> o = base_out<T, S>(a, p);
+    o.mode = 3;
+    launch_stage<T, S>(a, m, q, q, o, false, s);
+}
+
 // qW of the last stage of the iteration that read parity p (stage state in
 // qs[1], gradients and stage-3 limiter still in place).
 template <class T, class S>
