@@ -1921,6 +1921,13 @@ int afx_adjoint_state(afx_solver s, double* lam, long long n) {
     });
 }
 
+int afx_linear_iterations(afx_solver s, int* n) {
+    return guarded([&] {
+        if (!s || !n) throw Error(AFX_ERR_ARG, "null argument");
+        *n = s->imp ? s->imp_lin_iters : 0;
+    });
+}
+
 int afx_request_stop(afx_solver s) {
     if (!s) return AFX_ERR_ARG;
     s->stop.store(1);

@@ -42,7 +42,10 @@ struct GmresCtl {
     int stop;    // the current cycle has converged / ended
     int k;       // Arnoldi steps taken in the current cycle
     int iters;   // Krylov iterations of this solve
+    int halt;    // no further restart cycle
+    int max_iters;
     int pad;
+    cudaGraphConditionalHandle hin, hout;  // WHILE conditions: Arnoldi steps, restart cycles
     double tol;  // absolute residual target
     double res;  // current residual estimate
     double H[(GM_M + 1) * GM_M];  // column-major: H[i + (GM_M + 1) * j]
@@ -245,15 +248,19 @@ __global__ void __launch_bounds__(256) k_imp_spmv(const KM<double> m, const T* _
     stb(&y[i], yi);
 }
 
-// One colour of a block Gauss-Seidel sweep: x_i = D_i^-1 (r_i - sum O x_n)
+// One colour of a block Gauss-Seidel sweep: x_i = D_i^-1 (r_i - sum O x_n).
+// r = rbase + (*rk) * stride when rk is given (the current Krylov vector).
 template <class T>
 __global__ void __launch_bounds__(256) k_imp_gs(const KM<double> m, const T* __restrict__ jf,
                                                 const T* __restrict__ dinv, const int* __restrict__ cells,
-                                                const int n, const typename B4<T>::type* __restrict__ r,
-                                                typename B4<T>::type* __restrict__ x, const int* __restrict__ stop) {
+                                                const int n, const T* __restrict__ rbase, const int* __restrict__ rk,
+                                                const long long stride, typename B4<T>::type* __restrict__ x,
+                                                const int* __restrict__ stop) {
     if (stop && *stop) return;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
+    const typename B4<T>::type* r =
+        reinterpret_cast<const typename B4<T>::type*>(rbase + (rk ? (long long)*rk * stride : 0));
     const int i = __ldg(&cells[t]);
     double s[4];
     ldb(&r[i], s);
@@ -281,45 +288,68 @@ __global__ void k_imp_zero(const int n4, T* __restrict__ x, const int* __restric
     if (i < n4) x[i] = T(0);
 }
 
-// Partial dot products of w with v_0..v_{nv-1} (v_j = V + j*n): block b
-// writes part[b*nv + j]
+// Dot products of w with v_0..v_{nv-1} (v_j = V + j*n) in one launch: each
+// block writes its partial sums, and the last block to finish adds the
+// partials in block order (a fixed order, so the result is deterministic)
+// and re-arms the counter.
 template <class T>
-__global__ void __launch_bounds__(DOT_THREADS) k_imp_dots(const int n, const int nv, const T* __restrict__ V,
-                                                          const T* __restrict__ w, double* __restrict__ part,
-                                                          const int* __restrict__ stop) {
-    __shared__ double sh[32];
+__global__ void __launch_bounds__(DOT_THREADS) k_imp_dots(const int n, int nv, const int* __restrict__ nvk,
+                                                          const T* __restrict__ V, const T* __restrict__ w,
+                                                          double* __restrict__ part, unsigned* __restrict__ counter,
+                                                          double* __restrict__ out, const int* __restrict__ stop) {
+    __shared__ double sh[DOT_THREADS / 32][GM_M + 1];
+    __shared__ bool last;
     if (stop && *stop) return;
-    for (int j = 0; j < nv; ++j) {
-        double s = 0;
-        const T* v = V + (size_t)j * n;
-        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-            s += (double)v[i] * (double)w[i];
-        const double t = block_sum(s, sh);
-        if (threadIdx.x == 0) part[(size_t)blockIdx.x * nv + j] = t;
-        __syncthreads();
+    if (nvk) nv = *nvk + 1;  // v_0 .. v_k of the current Arnoldi step
+    // one pass over w and the nv vectors, nv accumulators per thread
+    double acc[GM_M + 1];
+#pragma unroll
+    for (int j = 0; j <= GM_M; ++j) acc[j] = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double wi = (double)w[i];
+#pragma unroll
+        for (int j = 0; j <= GM_M; ++j)
+            if (j < nv) acc[j] += (double)V[(size_t)j * n + i] * wi;
     }
-}
-
-// Fixed-order sum of the partials: out[j] = sum_b part[b*nv + j]
-__global__ void k_imp_dots_final(const int nb, const int nv, const double* __restrict__ part, double* __restrict__ out,
-                                 const int* __restrict__ stop) {
-    __shared__ double sh[32];
-    if (stop && *stop) return;
-    for (int j = 0; j < nv; ++j) {
-        double s = 0;
-        for (int b = threadIdx.x; b < nb; b += blockDim.x) s += part[(size_t)b * nv + j];
-        const double t = block_sum(s, sh);
-        if (threadIdx.x == 0) out[j] = t;
-        __syncthreads();
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+#pragma unroll
+    for (int j = 0; j <= GM_M; ++j) {
+        if (j >= nv) break;
+        double v = acc[j];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) sh[wp][j] = v;
     }
+    __syncthreads();
+    if ((int)threadIdx.x < nv) {
+        double t = 0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += sh[k][threadIdx.x];
+        part[(size_t)blockIdx.x * nv + threadIdx.x] = t;
+        __threadfence();  // the partials are visible before the block is counted
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    // the last block: each of nv threads adds the block partials in block order
+    if ((int)threadIdx.x < nv) {
+        double t = 0;
+        for (int b = 0; b < (int)gridDim.x; ++b) t += ((volatile double*)part)[(size_t)b * nv + threadIdx.x];
+        out[threadIdx.x] = t;
+    }
+    if (threadIdx.x == 0) *counter = 0;
 }
 
 // w -= sum_j h[j] v_j
 template <class T>
-__global__ void __launch_bounds__(256) k_imp_orth(const int n, const int nv, const T* __restrict__ V,
-                                                  const double* __restrict__ h, T* __restrict__ w,
-                                                  const int* __restrict__ stop) {
+__global__ void __launch_bounds__(256) k_imp_orth(const int n, int nv, const int* __restrict__ nvk,
+                                                  const T* __restrict__ V, const double* __restrict__ h,
+                                                  T* __restrict__ w, const int* __restrict__ stop) {
     if (stop && *stop) return;
+    if (nvk) nv = *nvk + 1;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double s = (double)w[i];
@@ -328,55 +358,90 @@ __global__ void __launch_bounds__(256) k_imp_orth(const int n, const int nv, con
 }
 
 // v = w * scale[0] (scale read from the device)
+// v = w * scale[0]; with vk given, v = vbase + (*vk) * n (the next Krylov vector)
 template <class T>
 __global__ void __launch_bounds__(256) k_imp_scale(const int n, const T* __restrict__ w, const double* __restrict__ scale,
-                                                   T* __restrict__ v, const int* __restrict__ stop) {
+                                                   T* __restrict__ v, const int* __restrict__ vk,
+                                                   const int* __restrict__ stop) {
     if (stop && *stop) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (vk) v += (long long)*vk * n;
     if (i < n) v[i] = (T)((double)w[i] * scale[0]);
 }
 
-// Arnoldi step j, classical Gram-Schmidt twice: h1 (first pass) and h2
-// (second pass) are summed into column j; then Givens rotations and the
-// residual estimate.  One thread.
-__global__ void k_imp_arnoldi(GmresCtl* c, const int j, const double* __restrict__ h1, const double* __restrict__ h2,
-                              const double* __restrict__ ww, double* __restrict__ scale) {
-    if (c->stop) return;
-    double* H = c->H + (GM_M + 1) * j;
-    for (int i = 0; i <= j; ++i) H[i] = h1[i] + h2[i];
-    const double hn = sqrt(fmax(ww[0], 0.0));
-    H[j + 1] = hn;
-    c->hnext = hn;
-    scale[0] = hn > 0 ? 1.0 / hn : 0.0;
-    for (int i = 0; i < j; ++i) {
-        const double a = H[i], b = H[i + 1];
-        H[i] = c->cs[i] * a + c->sn[i] * b;
-        H[i + 1] = -c->sn[i] * a + c->cs[i] * b;
+// Arnoldi step j = c->k, classical Gram-Schmidt twice: h1 (first pass) and
+// h2 (second pass) are summed into column j; then the Givens rotations and
+// the residual estimate.  One warp: the column and the rotations are staged
+// in shared memory so the sequential part runs on shared memory, not on
+// dependent global loads.
+__global__ void __launch_bounds__(32) k_imp_arnoldi(GmresCtl* c, const double* __restrict__ h1,
+                                                    const double* __restrict__ h2, const double* __restrict__ ww,
+                                                    double* __restrict__ scale) {
+    __shared__ double col[GM_M + 1], cs[GM_M], sn[GM_M], gj[1];
+    const int lane = threadIdx.x;
+    if (c->stop) {
+        if (lane == 0) cudaGraphSetConditional(c->hin, 0);
+        return;
     }
-    const double a = H[j], b = H[j + 1];
-    const double r = sqrt(a * a + b * b);
-    const double cs = r > 0 ? a / r : 1.0, sn = r > 0 ? b / r : 0.0;
-    c->cs[j] = cs;
-    c->sn[j] = sn;
-    H[j] = r;
-    H[j + 1] = 0;
-    c->g[j + 1] = -sn * c->g[j];
-    c->g[j] = cs * c->g[j];
-    c->res = fabs(c->g[j + 1]);
-    c->k = j + 1;
-    c->iters += 1;
-    if (c->res <= c->tol || j + 1 == GM_M || hn == 0) c->stop = 1;
+    const int j = c->k;
+    for (int t = lane; t <= j; t += 32) col[t] = h1[t] + h2[t];
+    for (int t = lane; t < j; t += 32) {
+        cs[t] = c->cs[t];
+        sn[t] = c->sn[t];
+    }
+    if (lane == 0) gj[0] = c->g[j];
+    __syncwarp();
+    if (lane == 0) {
+        const double hn = sqrt(fmax(ww[0], 0.0));
+        col[j + 1] = hn;
+        c->hnext = hn;
+        scale[0] = hn > 0 ? 1.0 / hn : 0.0;
+        for (int i = 0; i < j; ++i) {
+            const double a = col[i], b = col[i + 1];
+            col[i] = cs[i] * a + sn[i] * b;
+            col[i + 1] = -sn[i] * a + cs[i] * b;
+        }
+        const double a = col[j], b = col[j + 1];
+        const double r = sqrt(a * a + b * b);
+        const double cj = r > 0 ? a / r : 1.0, sj = r > 0 ? b / r : 0.0;
+        c->cs[j] = cj;
+        c->sn[j] = sj;
+        col[j] = r;
+        col[j + 1] = 0;
+        const double g = gj[0];
+        c->g[j + 1] = -sj * g;
+        c->g[j] = cj * g;
+        c->res = fabs(sj * g);
+        c->k = j + 1;
+        c->iters += 1;
+        const int st = (c->res <= c->tol || j + 1 == GM_M || hn == 0 || c->iters >= c->max_iters) ? 1 : 0;
+        c->stop = st;
+        cudaGraphSetConditional(c->hin, st ? 0 : 1);
+    }
+    __syncwarp();
+    for (int t = lane; t <= j + 1; t += 32) c->H[t + (GM_M + 1) * j] = col[t];
 }
 
-// Back substitution R y = g over the k steps of the cycle (one thread)
-__global__ void k_imp_solve_y(GmresCtl* c) {
+// Back substitution R y = g over the k steps of the cycle (one warp; the
+// triangle is staged in shared memory)
+__global__ void __launch_bounds__(32) k_imp_solve_y(GmresCtl* c) {
+    __shared__ double R[GM_M * GM_M], g[GM_M], y[GM_M];
     const int k = c->k;
-    for (int i = k - 1; i >= 0; --i) {
-        double s = c->g[i];
-        for (int l = i + 1; l < k; ++l) s -= c->H[i + (GM_M + 1) * l] * c->y[l];
-        const double d = c->H[i + (GM_M + 1) * i];
-        c->y[i] = d != 0 ? s / d : 0.0;
+    for (int t = threadIdx.x; t < k * k; t += 32) {
+        const int i = t % k, l = t / k;
+        R[i + GM_M * l] = c->H[i + (GM_M + 1) * l];
     }
+    for (int t = threadIdx.x; t < k; t += 32) g[t] = c->g[t];
+    __syncwarp();
+    if (threadIdx.x == 0)
+        for (int i = k - 1; i >= 0; --i) {
+            double s = g[i];
+            for (int l = i + 1; l < k; ++l) s -= R[i + GM_M * l] * y[l];
+            const double d = R[i + GM_M * i];
+            y[i] = d != 0 ? s / d : 0.0;
+        }
+    __syncwarp();
+    for (int t = threadIdx.x; t < k; t += 32) c->y[t] = y[t];
 }
 
 // t = sum_j y_j v_j over the k steps
@@ -398,12 +463,15 @@ __global__ void __launch_bounds__(256) k_imp_addx(const int n, const T* __restri
 }
 template <class T>
 __global__ void __launch_bounds__(256) k_imp_resid(const int n, const double* __restrict__ b, const T* __restrict__ y,
-                                                   T* __restrict__ r) {
+                                                   T* __restrict__ r, const int* __restrict__ stop) {
+    if (stop && *stop) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) r[i] = (T)(b[i] - (double)y[i]);
 }
 template <class T>
-__global__ void __launch_bounds__(256) k_imp_cast(const int n, const double* __restrict__ x, T* __restrict__ t) {
+__global__ void __launch_bounds__(256) k_imp_cast(const int n, const double* __restrict__ x, T* __restrict__ t,
+                                                  const int* __restrict__ stop) {
+    if (stop && *stop) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) t[i] = (T)x[i];
 }
@@ -420,18 +488,33 @@ __global__ void __launch_bounds__(256) k_imp_update(const int n, const double* _
 
 // GMRES initialisation of a cycle: g = (beta, 0, ...), stop = beta <= tol
 __global__ void k_imp_cycle_init(GmresCtl* c, const double* __restrict__ rr, double* __restrict__ scale, const int first,
-                                 const double rel_tol) {
+                                 const double rel_tol, const int max_iters) {
+    if (!first && c->halt) return;
     const double beta = sqrt(fmax(rr[0], 0.0));
     if (first) {
         c->tol = rel_tol * beta;
         c->iters = 0;
+        c->max_iters = max_iters;
     }
     for (int i = 0; i <= GM_M; ++i) c->g[i] = 0;
     c->g[0] = beta;
     c->res = beta;
     c->k = 0;
     c->stop = (beta <= c->tol) ? 1 : 0;
+    c->halt = c->stop;
     scale[0] = beta > 0 ? 1.0 / beta : 0.0;
+    if (first) cudaGraphSetConditional(c->hout, c->stop ? 0 : 1);
+}
+
+// Start of a restart cycle (inside the restart loop's body): enter the
+// Arnoldi loop unless the cycle is already converged
+__global__ void k_imp_enter(GmresCtl* c) { cudaGraphSetConditional(c->hin, c->stop ? 0 : 1); }
+
+// End of a restart cycle: another one if not converged and under the limit
+__global__ void k_imp_outer_check(GmresCtl* c) {
+    const int cont = (c->res > c->tol) && (c->iters < c->max_iters) && (c->k > 0);
+    c->halt = cont ? 0 : 1;
+    cudaGraphSetConditional(c->hout, cont ? 1 : 0);
 }
 
 }  // namespace dev
@@ -459,7 +542,11 @@ struct ImplicitEngine {
     void* t = nullptr;     // 4N
     double* x = nullptr;   // 4N, the solution dQ
     double* part = nullptr;
+    unsigned* counter = nullptr;  // last-block counter of the dot kernel
     double* small = nullptr;  // h1[GM_M+1], h2[GM_M+1], ww, scale
+    cudaGraphExec_t cyc[2] = {nullptr, nullptr};  // cyc[0]: the GMRES solve graph
+    cudaStream_t s2 = nullptr, s3 = nullptr;      // capture streams of the loop bodies
+    const void* cyc_b = nullptr;                  // right-hand side the graphs were captured with
     int nbd = 0;
     dev::GmresCtl* ctl = nullptr;
     dev::GmresCtl* h_ctl = nullptr;
@@ -499,6 +586,8 @@ ImplicitEngine* implicit_create(const StepArgs& a, bool f32, const std::vector<i
     e->nbd = std::min(1024, nb_(e->n4, dev::DOT_THREADS * 4));
     chk(cudaMalloc((void**)&e->part, (size_t)e->nbd * (dev::GM_M + 1) * 8));
     chk(cudaMalloc((void**)&e->small, (2 * (dev::GM_M + 1) + 2) * 8));
+    chk(cudaMalloc((void**)&e->counter, sizeof(unsigned)));
+    chk(cudaMemsetAsync(e->counter, 0, sizeof(unsigned), s));
     chk(cudaMalloc((void**)&e->ctl, sizeof(dev::GmresCtl)));
     chk(cudaHostAlloc((void**)&e->h_ctl, sizeof(dev::GmresCtl), cudaHostAllocDefault));
     chk(cudaMemcpyAsync(e->color_cells, cells.data(), cells.size() * sizeof(int), cudaMemcpyHostToDevice, s));
@@ -509,8 +598,12 @@ ImplicitEngine* implicit_create(const StepArgs& a, bool f32, const std::vector<i
 
 void implicit_destroy(ImplicitEngine* e) {
     if (!e) return;
+    for (int k = 0; k < 2; ++k)
+        if (e->cyc[k]) cudaGraphExecDestroy(e->cyc[k]);
+    if (e->s2) cudaStreamDestroy(e->s2);
+    if (e->s3) cudaStreamDestroy(e->s3);
     for (void* p : {e->jf, e->dblk, e->dinv, (void*)e->color_cells, (void*)e->singular, e->V, e->w, e->z, e->t,
-                    (void*)e->x, (void*)e->part, (void*)e->small, (void*)e->ctl})
+                    (void*)e->x, (void*)e->part, (void*)e->small, (void*)e->ctl, (void*)e->counter})
         if (p) cudaFree(p);
     if (e->h_ctl) cudaFreeHost(e->h_ctl);
     delete e;
@@ -566,8 +659,9 @@ struct Ops {
         dev::k_imp_spmv<T><<<nb_(e->N, 256), 256, 0, s>>>(m, (const T*)e->jf, (const T*)e->dblk, (const V4*)x, (V4*)y,
                                                           st);
     }
-    // one symmetric multicolour block Gauss-Seidel sweep from x = 0
-    void precond(const T* r, T* x, const int* st) const {
+    // one symmetric multicolour block Gauss-Seidel sweep from x = 0; the
+    // input is r, or the current Krylov vector V + k*n when rk is given
+    void precond(const T* r, const int* rk, T* x, const int* st) const {
         dev::k_imp_zero<T><<<nb_(e->n4, 256), 256, 0, s>>>(e->n4, x, st);
         for (int pass = 0; pass < 2; ++pass)
             for (int k = 0; k < e->n_colors; ++k) {
@@ -575,63 +669,131 @@ struct Ops {
                 const int c0 = e->color_ptr[c], cn = e->color_ptr[c + 1] - c0;
                 if (cn == 0) continue;
                 dev::k_imp_gs<T><<<nb_(cn, 256), 256, 0, s>>>(m, (const T*)e->jf, (const T*)e->dinv,
-                                                              e->color_cells + c0, cn, (const V4*)r, (V4*)x, st);
+                                                              e->color_cells + c0, cn, r, rk, (long long)e->n4,
+                                                              (V4*)x, st);
             }
     }
-    void dots(int nv, const T* V, const T* w, double* out, const int* st) const {
-        dev::k_imp_dots<T><<<e->nbd, dev::DOT_THREADS, 0, s>>>(e->n4, nv, V, w, e->part, st);
-        dev::k_imp_dots_final<<<1, 256, 0, s>>>(e->nbd, nv, e->part, out, st);
+    void dots(int nv, const int* nvk, const T* V, const T* w, double* out, const int* st) const {
+        dev::k_imp_dots<T><<<e->nbd, dev::DOT_THREADS, 0, s>>>(e->n4, nv, nvk, V, w, e->part, e->counter, out, st);
     }
 };
 
+// Adds a WHILE node at the capture position of stream st (the work captured
+// next on st follows the loop) and returns its body graph.
+cudaGraph_t add_while(cudaStream_t st, cudaGraphConditionalHandle* h) {
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g;
+    const cudaGraphNode_t* deps = nullptr;
+    const cudaGraphEdgeData* ed = nullptr;
+    size_t nd = 0;
+    auto chk = [](cudaError_t r) {
+        if (r != cudaSuccess) throw Error(7, std::string("implicit solver graph: ") + cudaGetErrorString(r));
+    };
+    chk(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, &ed, &nd));
+    chk(cudaGraphConditionalHandleCreate(h, g, 0, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams p{};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = *h;
+    p.conditional.type = cudaGraphCondTypeWhile;
+    p.conditional.size = 1;
+    cudaGraphNode_t node;
+    chk(cudaGraphAddNode(&node, g, deps, ed, nd, &p));
+    chk(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    return p.conditional.phGraph_out[0];
+}
+
+// The whole GMRES solve of M dQ = b as one graph: restart cycles and Arnoldi
+// steps are WHILE loops whose conditions the kernels set on the device, so
+// a solve runs without host round trips and without idle launches.
 template <class T>
-int gmres(ImplicitEngine* e, const StepArgs& a, const double* b, cudaStream_t s, int max_iters) {
+cudaGraphExec_t build_gmres_graph(ImplicitEngine* e, const Ops<T>& o0, const double* b, cudaStream_t s,
+                                  cudaStream_t s2, cudaStream_t s3, int max_iters) {
     using namespace dev;
-    Ops<T> o(e, a, s);
     const int n = e->n4;
     double* h1 = e->small;
     double* h2 = e->small + (GM_M + 1);
     double* ww = e->small + 2 * (GM_M + 1);
     double* scale = ww + 1;
+    int* kptr = &e->ctl->k;
+    int* stop = &e->ctl->stop;
+    int* halt = &e->ctl->halt;
+    auto chk = [](cudaError_t r) {
+        if (r != cudaSuccess) throw Error(7, std::string("implicit solver graph: ") + cudaGetErrorString(r));
+    };
+    cudaGraphConditionalHandle hout, hin;
+    // main graph: first cycle set-up, the restart loop, the control block back to the host
+    chk(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    Ops<T> o(e, o0.a, s);
+    T* v0 = o.vec(0);
     cudaMemsetAsync(e->x, 0, (size_t)n * 8, s);
-    int total = 0;
-    for (int cycle = 0; total < max_iters; ++cycle) {
-        // r = b - M x (x = 0 on the first cycle)
-        T* v0 = o.vec(0);
-        if (cycle == 0) {
-            k_imp_cast<T><<<nb_(n, 256), 256, 0, s>>>(n, b, v0);
-        } else {
-            k_imp_cast<T><<<nb_(n, 256), 256, 0, s>>>(n, e->x, (T*)e->t);
-            o.spmv((const T*)e->t, (T*)e->w, nullptr);
-            k_imp_resid<T><<<nb_(n, 256), 256, 0, s>>>(n, b, (const T*)e->w, v0);
-        }
-        o.dots(1, v0, v0, ww, nullptr);
-        k_imp_cycle_init<<<1, 1, 0, s>>>(e->ctl, ww, scale, cycle == 0, 1e-2);
-        k_imp_scale<T><<<nb_(n, 256), 256, 0, s>>>(n, v0, scale, v0, o.stop());
-        for (int j = 0; j < GM_M; ++j) {
-            o.precond(o.vec(j), (T*)e->z, o.stop());
-            o.spmv((const T*)e->z, (T*)e->w, o.stop());
-            o.dots(j + 1, o.vec(0), (const T*)e->w, h1, o.stop());
-            k_imp_orth<T><<<nb_(n, 256), 256, 0, s>>>(n, j + 1, o.vec(0), h1, (T*)e->w, o.stop());
-            o.dots(j + 1, o.vec(0), (const T*)e->w, h2, o.stop());
-            k_imp_orth<T><<<nb_(n, 256), 256, 0, s>>>(n, j + 1, o.vec(0), h2, (T*)e->w, o.stop());
-            o.dots(1, (const T*)e->w, (const T*)e->w, ww, o.stop());
-            k_imp_arnoldi<<<1, 1, 0, s>>>(e->ctl, j, h1, h2, ww, scale);
-            k_imp_scale<T><<<nb_(n, 256), 256, 0, s>>>(n, (const T*)e->w, scale, o.vec(j + 1), o.stop());
-        }
-        cudaMemcpyAsync(e->h_ctl, e->ctl, sizeof(GmresCtl), cudaMemcpyDeviceToHost, s);
-        cudaStreamSynchronize(s);
-        const int k = e->h_ctl->k;
-        if (k > 0) {
-            k_imp_solve_y<<<1, 1, 0, s>>>(e->ctl);
-            k_imp_lincomb<T><<<nb_(n, 256), 256, 0, s>>>(n, o.vec(0), e->ctl, (T*)e->t);
-            o.precond((const T*)e->t, (T*)e->z, nullptr);
-            k_imp_addx<T><<<nb_(n, 256), 256, 0, s>>>(n, (const T*)e->z, e->x);
-        }
-        total = e->h_ctl->iters;
-        if (e->h_ctl->res <= e->h_ctl->tol || k == 0) break;
+    k_imp_cast<T><<<nb_(n, 256), 256, 0, s>>>(n, b, v0, nullptr);
+    o.dots(1, nullptr, v0, v0, ww, nullptr);
+    k_imp_cycle_init<<<1, 1, 0, s>>>(e->ctl, ww, scale, 1, 1e-2, max_iters);
+    k_imp_scale<T><<<nb_(n, 256), 256, 0, s>>>(n, v0, scale, v0, nullptr, stop);
+    cudaGraph_t body_out = add_while(s, &hout);
+    cudaMemcpyAsync(e->h_ctl, e->ctl, sizeof(GmresCtl), cudaMemcpyDeviceToHost, s);
+    cudaGraph_t G;
+    chk(cudaStreamEndCapture(s, &G));
+    // restart-cycle body: the Arnoldi loop, the update of x, the next residual
+    chk(cudaStreamBeginCaptureToGraph(s2, body_out, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    {
+        Ops<T> q(e, o0.a, s2);
+        k_imp_enter<<<1, 1, 0, s2>>>(e->ctl);
+        cudaGraph_t body_in = add_while(s2, &hin);
+        k_imp_solve_y<<<1, 32, 0, s2>>>(e->ctl);
+        k_imp_lincomb<T><<<nb_(n, 256), 256, 0, s2>>>(n, q.vec(0), e->ctl, (T*)e->t);
+        q.precond((const T*)e->t, nullptr, (T*)e->z, nullptr);
+        k_imp_addx<T><<<nb_(n, 256), 256, 0, s2>>>(n, (const T*)e->z, e->x);
+        k_imp_outer_check<<<1, 1, 0, s2>>>(e->ctl);
+        k_imp_cast<T><<<nb_(n, 256), 256, 0, s2>>>(n, e->x, (T*)e->t, halt);
+        q.spmv((const T*)e->t, (T*)e->w, halt);
+        k_imp_resid<T><<<nb_(n, 256), 256, 0, s2>>>(n, b, (const T*)e->w, q.vec(0), halt);
+        q.dots(1, nullptr, q.vec(0), q.vec(0), ww, halt);
+        k_imp_cycle_init<<<1, 1, 0, s2>>>(e->ctl, ww, scale, 0, 1e-2, max_iters);
+        k_imp_scale<T><<<nb_(n, 256), 256, 0, s2>>>(n, q.vec(0), scale, q.vec(0), nullptr, halt);
+        chk(cudaStreamEndCapture(s2, &body_out));
+        // Arnoldi step k: z = P^-1 v_k, w = M z, CGS2 against v_0..v_k, rotations, v_{k+1}
+        chk(cudaStreamBeginCaptureToGraph(s3, body_in, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        Ops<T> r(e, o0.a, s3);
+        r.precond(r.vec(0), kptr, (T*)e->z, stop);
+        r.spmv((const T*)e->z, (T*)e->w, stop);
+        r.dots(0, kptr, r.vec(0), (const T*)e->w, h1, stop);
+        k_imp_orth<T><<<nb_(n, 256), 256, 0, s3>>>(n, 0, kptr, r.vec(0), h1, (T*)e->w, stop);
+        r.dots(0, kptr, r.vec(0), (const T*)e->w, h2, stop);
+        k_imp_orth<T><<<nb_(n, 256), 256, 0, s3>>>(n, 0, kptr, r.vec(0), h2, (T*)e->w, stop);
+        r.dots(1, nullptr, (const T*)e->w, (const T*)e->w, ww, stop);
+        k_imp_arnoldi<<<1, 32, 0, s3>>>(e->ctl, h1, h2, ww, scale);
+        k_imp_scale<T><<<nb_(n, 256), 256, 0, s3>>>(n, (const T*)e->w, scale, r.vec(0), kptr, stop);
+        chk(cudaStreamEndCapture(s3, &body_in));
     }
-    return total;
+    cudaGraphExec_t ex;
+    const cudaError_t ri = cudaGraphInstantiate(&ex, G, 0);
+    cudaGraphDestroy(G);
+    chk(ri);
+    e->h_ctl->hin = hin;
+    e->h_ctl->hout = hout;
+    chk(cudaMemcpyAsync(&e->ctl->hin, &e->h_ctl->hin, 2 * sizeof(cudaGraphConditionalHandle), cudaMemcpyHostToDevice,
+                        s));
+    chk(cudaStreamSynchronize(s));
+    return ex;
+}
+
+template <class T>
+int gmres(ImplicitEngine* e, const StepArgs& a, const double* b, cudaStream_t s, int max_iters) {
+    Ops<T> o(e, a, s);
+    if (e->cyc_b != b || !e->cyc[0]) {
+        if (e->cyc[0]) cudaGraphExecDestroy(e->cyc[0]);
+        e->cyc[0] = nullptr;
+        if (!e->s2) {
+            cudaStreamCreateWithFlags(&e->s2, cudaStreamNonBlocking);
+            cudaStreamCreateWithFlags(&e->s3, cudaStreamNonBlocking);
+        }
+        e->cyc[0] = build_gmres_graph<T>(e, o, b, s, e->s2, e->s3, max_iters);
+        e->cyc_b = b;
+    }
+    if (cudaGraphLaunch(e->cyc[0], s) != cudaSuccess) throw Error(7, "implicit solver: graph launch failed");
+    if (cudaStreamSynchronize(s) != cudaSuccess) throw Error(7, "implicit solver: GMRES failed");
+    return e->h_ctl->iters;
 }
 
 }  // namespace

@@ -31,7 +31,7 @@ ABI_SYMBOLS = [
     "afx_batch_set_state", "afx_batch_get_state", "afx_batch_iterate", "afx_batch_run_to_convergence",
     "afx_batch_case_history", "afx_batch_forces", "afx_batch_set_farfield", "afx_batch_autotune",
     "afx_batch_last_device_seconds", "afx_residual_vjp", "afx_boundary_states", "afx_adjoint_solve",
-    "afx_adjoint_state",
+    "afx_adjoint_state", "afx_linear_iterations",
 ]
 N_KERNEL_KINDS = 7
 
@@ -110,6 +110,7 @@ def lib():
         "afx_boundary_states": (i, [vp, vp, ll]),
         "afx_adjoint_solve": (i, [vp, cp, cp, d, i, vp, P(i), P(d)]),
         "afx_adjoint_state": (i, [vp, vp, ll]),
+        "afx_linear_iterations": (i, [vp, P(i)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -304,6 +305,12 @@ class Solver:
         ms = ctypes.c_double()
         _check(lib().afx_autotune(self.h, int(iters), buf, 16, ctypes.byref(blk), ctypes.byref(ms)))
         return dict(variant=buf.value.decode(), block=blk.value, ms_per_iter=ms.value)
+
+    def linear_iterations(self):
+        """Krylov iterations of the last implicit iteration (0: explicit solver)."""
+        n = ctypes.c_int()
+        _check(lib().afx_linear_iterations(self.h, ctypes.byref(n)))
+        return n.value
 
     def residual_vjp(self, v, q=None):
         """((dR/dq)^T v, (dR/dbq)^T v) at state q (default: the solver's);

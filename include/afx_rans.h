@@ -169,6 +169,13 @@ int afx_autotune(afx_solver s, int iters, char* variant, int cap, int* block, do
  * array's address; make it before any stream capture. */
 int afx_residual_noalloc(afx_solver s, const double* q_dev, double* R_dev, long long n);
 
+/* Implicit solver (settings solver = "implicit"): Krylov (GMRES)
+ * iterations of the last implicit iteration, over its first solve and its
+ * rhs_iterations chord solves (solver.h:1170-1213).  0 for the explicit
+ * solver.  No counterpart in the reference (Eigen's iterations() is only
+ * printed under RANS_DEBUG). */
+int afx_linear_iterations(afx_solver s, int* n);
+
 /* ---- Adjoint of the FP64 residual.  No counterpart in the reference (it
  * has no adjoint).  R(q) is the residual afx_residual returns (first-stage
  * semantics: gradients and limiter formed from q, solver.h:745-799); bq are
