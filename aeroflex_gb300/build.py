@@ -45,6 +45,7 @@ def _units():
         (nv + ["-fmad=false", "-c"], "afx_noalloc.cu"),
         (nv + ["-fmad=false", "-c"], "afx_adjoint.cu"),
         (nv + ["-c"], "afx_implicit.cu"),
+        (nv + ["-fmad=false", "-c"], "afx_prolong.cu"),
         (nv + ["-use_fast_math", "-c"], "afx_kernels_f32.cu"),
     ], nvcc
 

@@ -29,6 +29,10 @@ long long noalloc_max_cells();
 long long noalloc_max_faces();
 cudaError_t noalloc_residual_f64(const StepArgs& a, const int* cell_old, const double* q_ref, double* R_ref,
                                  cudaStream_t s);
+void enqueue_prolong(int nc, const double* cx, const double* cy, const double* ca, const void* coarse_full, int nf,
+                     const double* fx, const double* fy, void* fine_q, cudaStream_t s);
+void enqueue_full_state(int n, int nb, const int* cell_old, const int* owner_dev, const void* q, void* full,
+                        cudaStream_t s);
 struct ImplicitEngine;
 ImplicitEngine* implicit_create(const StepArgs& a, bool f32, const std::vector<int>& colors, cudaStream_t s);
 void implicit_destroy(ImplicitEngine* e);
@@ -297,6 +301,11 @@ struct afx_solver_s {
         if (ev1) cudaEventDestroy(ev1);
         if (stream) cudaStreamDestroy(stream);
     }
+
+    // grid sequencing (multigrid.h:99-178): centroids and areas of all cells
+    // (ghosts included, reference order), real-cell centroids in device order
+    std::vector<double> geo_cx, geo_cy, geo_area, dev_cx, dev_cy;
+    DevBuf d_geo, d_devc, d_owner, d_full;
 
     // implicit solver (solver.h:852-1213), when settings.solver == "implicit"
     ImplicitEngine* imp = nullptr;
@@ -854,6 +863,15 @@ static std::unique_ptr<afx_solver_s> make_solver(const HostMesh& m, const Device
             s->cell_old = L.cell_old;
             s->h_fcell = L.fcell;
             s->h_cslot = L.cslot;
+            s->geo_cx = m.cellsCentersX;
+            s->geo_cy = m.cellsCentersY;
+            s->geo_area = m.cellsAreas;
+            s->dev_cx.resize(L.n_cells);
+            s->dev_cy.resize(L.n_cells);
+            for (int i = 0; i < L.n_cells; ++i) {
+                s->dev_cx[i] = m.cellsCentersX[L.cell_old[i]];
+                s->dev_cy[i] = m.cellsCentersY[L.cell_old[i]];
+            }
         }
         s->fp64 = s->st.precision != "fp32-mixed";
         AFX_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
@@ -991,6 +1009,13 @@ static std::unique_ptr<afx_solver_s> make_solver(const HostMesh& m, const Device
             b.Rq = s->dalloc(N * 32);
             b.variant = 0;  // gather: no FP64 face buffers needed
             b.fflux = b.feL = nullptr;
+            if (implicit) {
+                // the implicit right-hand side is formed every chord step:
+                // the face-flux variant (one FP64 flux per face)
+                b.variant = 1;
+                b.fflux = s->dalloc(F * 32);
+                b.feL = s->dalloc(F * 8);
+            }
             b.corr = nullptr;
             b.ctrl = (Ctrl*)s->dalloc(sizeof(Ctrl));  // zeroed, never set to done
             s->R32buf = s->dalloc(N * 32);
@@ -1918,6 +1943,50 @@ int afx_adjoint_state(afx_solver s, double* lam, long long n) {
         enqueue_permute_out((int)N, (const int*)s->d_cell_old.p, J.lam[s->adj_parity].p, s->d_stage.p, s->stream);
         AFX_CUDA(cudaMemcpyAsync(lam, s->d_stage.p, N * 32, cudaMemcpyDefault, s->stream));
         AFX_CUDA(cudaStreamSynchronize(s->stream));
+    });
+}
+
+// multigrid::run's level transfer (multigrid.h:316-321): coarse ghosts from
+// their owners, fine state = mapper * coarse state, fine ghosts refilled.
+int afx_prolongate(afx_solver coarse, afx_solver fine) {
+    return guarded([&] {
+        if (!coarse || !fine) throw Error(AFX_ERR_ARG, "null argument");
+        afx_solver_s& c = *coarse;
+        afx_solver_s& f = *fine;
+        const int nc = (int)c.geo_area.size(), nr = c.a.n_cells, nb = nc - nr;
+        if (!c.d_geo.p) {
+            std::vector<double> g(3 * (size_t)nc);
+            std::copy(c.geo_cx.begin(), c.geo_cx.end(), g.begin());
+            std::copy(c.geo_cy.begin(), c.geo_cy.end(), g.begin() + nc);
+            std::copy(c.geo_area.begin(), c.geo_area.end(), g.begin() + 2 * (size_t)nc);
+            c.d_geo.upload(g.data(), g.size() * 8, c.stream);
+            std::vector<int> owner(std::max(nb, 1), 0);
+            for (int b = 0; b < nb; ++b) owner[b] = c.bedges[b].owner_dev;
+            c.d_owner.upload(owner.data(), owner.size() * sizeof(int), c.stream);
+            c.d_full.alloc((size_t)nc * 32);
+        }
+        if (!f.d_devc.p) {
+            std::vector<double> g(2 * f.dev_cx.size());
+            std::copy(f.dev_cx.begin(), f.dev_cx.end(), g.begin());
+            std::copy(f.dev_cy.begin(), f.dev_cy.end(), g.begin() + f.dev_cx.size());
+            f.d_devc.upload(g.data(), g.size() * 8, f.stream);
+        }
+        c.ensure_shadow();
+        enqueue_full_state(nr, nb, (const int*)c.d_cell_old.p, (const int*)c.d_owner.p, c.a.qm[c.parity], c.d_full.p,
+                           c.stream);
+        AFX_CUDA(cudaStreamSynchronize(c.stream));
+        AFX_CUDA(cudaStreamSynchronize(f.stream));
+        const double* geo = (const double*)c.d_geo.p;
+        const double* fc = (const double*)f.d_devc.p;
+        enqueue_prolong(nc, geo, geo + nc, geo + 2 * (size_t)nc, c.d_full.p, f.a.n_cells, fc, fc + f.a.n_cells,
+                        f.a.qm[f.parity], f.stream);
+        f.sync_shadow(f.parity);
+        f.shadow_stale = false;
+        f.reset_phase();
+        f.pending_last = -1;
+        f.refill_bcs();
+        AFX_CUDA(cudaStreamSynchronize(f.stream));
+        AFX_CUDA(cudaGetLastError());
     });
 }
 

@@ -31,7 +31,7 @@ ABI_SYMBOLS = [
     "afx_batch_set_state", "afx_batch_get_state", "afx_batch_iterate", "afx_batch_run_to_convergence",
     "afx_batch_case_history", "afx_batch_forces", "afx_batch_set_farfield", "afx_batch_autotune",
     "afx_batch_last_device_seconds", "afx_residual_vjp", "afx_boundary_states", "afx_adjoint_solve",
-    "afx_adjoint_state", "afx_linear_iterations",
+    "afx_adjoint_state", "afx_linear_iterations", "afx_prolongate",
 ]
 N_KERNEL_KINDS = 7
 
@@ -111,6 +111,7 @@ def lib():
         "afx_adjoint_solve": (i, [vp, cp, cp, d, i, vp, P(i), P(d)]),
         "afx_adjoint_state": (i, [vp, vp, ll]),
         "afx_linear_iterations": (i, [vp, P(i)]),
+        "afx_prolongate": (i, [vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -305,6 +306,11 @@ class Solver:
         ms = ctypes.c_double()
         _check(lib().afx_autotune(self.h, int(iters), buf, 16, ctypes.byref(blk), ctypes.byref(ms)))
         return dict(variant=buf.value.decode(), block=blk.value, ms_per_iter=ms.value)
+
+    def prolongate_from(self, coarse):
+        """Grid-sequencing transfer (multigrid.h:99-178, 316-321): this
+        solver's state from the coarse solver's."""
+        _check(lib().afx_prolongate(coarse.h, self.h))
 
     def linear_iterations(self):
         """Krylov iterations of the last implicit iteration (0: explicit solver)."""

@@ -169,6 +169,15 @@ int afx_autotune(afx_solver s, int iters, char* variant, int cap, int* block, do
  * array's address; make it before any stream capture. */
 int afx_residual_noalloc(afx_solver s, const double* q_dev, double* R_dev, long long n);
 
+/* Grid sequencing: multigrid::run's transfer between levels (multigrid.h:
+ * 316-321 with the mapper of gen_mapper, multigrid.h:99-178).  The fine
+ * solver's state becomes mapper * the coarse state (ghost cells taking their
+ * owner's state, bcs_from_internal, solver.h:276-287), and its ghost states
+ * are refilled from its boundary conditions.  The mapper weights every coarse
+ * cell j (ghosts included) within d^2 < 2 A_j of a fine cell by
+ * 1/max(0.1 sqrt(A_j), d), normalised.  Both solvers on the same device. */
+int afx_prolongate(afx_solver coarse, afx_solver fine);
+
 /* Implicit solver (settings solver = "implicit"): Krylov (GMRES)
  * iterations of the last implicit iteration, over its first solve and its
  * rhs_iterations chord solves (solver.h:1170-1213).  0 for the explicit

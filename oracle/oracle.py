@@ -51,6 +51,7 @@ def lib():
         L.orc_refill_bcs.argtypes = [vp]
         L.orc_set_farfield.argtypes = [vp, cp, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double]
         L.orc_set_q.argtypes = [vp, vp]
+        L.orc_prolongate.argtypes = [vp, vp]
         L.orc_get.restype = ctypes.c_longlong
         L.orc_get.argtypes = [vp, cp, vp]
         L.orc_residual.argtypes = [vp, vp]
@@ -183,6 +184,11 @@ class Solver:
     def set_farfield(self, patch, mach, angle, T=1.0, p=1.0):
         if lib().orc_set_farfield(self.h, patch.encode(), mach, angle, T, p):
             raise RuntimeError(lib().orc_last_error().decode())
+
+    def prolongate_from(self, coarse):
+        """Grid-sequencing transfer (multigrid.h:99-178, 295-363): this
+        solver's state from the coarse solver's."""
+        lib().orc_prolongate(coarse.h, self.h)
 
     def set_q(self, q):
         q = np.ascontiguousarray(q, np.float64).reshape(-1)

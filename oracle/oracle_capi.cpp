@@ -203,6 +203,8 @@ int orc_set_farfield(void* sp, const char* patch, double mach, double angle, dou
     }
 }
 
+void orc_prolongate(void* coarse, void* fine) { prolongate(*(ExplicitSolver*)coarse, *(ExplicitSolver*)fine); }
+
 void orc_set_q(void* sp, const double* q_real) {
     auto* s = (ExplicitSolver*)sp;
     std::memcpy(s->q.data(), q_real, 4 * (size_t)s->m.nRealCells * sizeof(double));

@@ -877,3 +877,42 @@ WallProfile get_wall_profile(const ExplicitSolver& s, const std::string& patch) 
 }
 
 }  // namespace oracle
+
+// ------------------------------------------------------ multigrid.h:99-178
+namespace oracle {
+void prolongate(ExplicitSolver& coarse, ExplicitSolver& fine) {
+    // bcs_from_internal (solver.h:276-287): ghost = its owner's state
+    for (size_t b = 0; b < coarse.m.boundaryEdges.size(); ++b) {
+        const uint e = coarse.m.boundaryEdges[b];
+        const uint c0 = coarse.m.edgesCells[e][0], c1 = coarse.m.edgesCells[e][1];
+        for (int k = 0; k < 4; ++k) coarse.q[4 * c1 + k] = coarse.q[4 * c0 + k];
+    }
+    const Mesh& cm = coarse.m;
+    const Mesh& fm = fine.m;
+    const size_t m = fm.cellsAreas.size(), n = cm.cellsAreas.size();
+    std::vector<double> out(4 * m, 0.);
+#pragma omp parallel for
+    for (long i = 0; i < (long)m; ++i) {
+        const double xi = fm.cellsCentersX[i], yi = fm.cellsCentersY[i];
+        double scale = 0;
+        for (size_t j = 0; j < n; ++j) {
+            const double xj = cm.cellsCentersX[j], yj = cm.cellsCentersY[j];
+            const double d2 = (xi - xj) * (xi - xj) + (yi - yj) * (yi - yj);
+            const double r2 = cm.cellsAreas[j];
+            if (d2 < 2 * r2) scale += 1 / std::max(0.1 * std::sqrt(r2), std::sqrt(d2));
+        }
+        // the mapper's column-major product adds the columns in order
+        for (size_t j = 0; j < n; ++j) {
+            const double xj = cm.cellsCentersX[j], yj = cm.cellsCentersY[j];
+            const double d2 = (xi - xj) * (xi - xj) + (yi - yj) * (yi - yj);
+            const double r2 = cm.cellsAreas[j];
+            if (d2 < 2 * r2) {
+                const double w = (1 / std::max(0.1 * std::sqrt(r2), std::sqrt(d2))) / scale;
+                for (int k = 0; k < 4; ++k) out[4 * i + k] += w * coarse.q[4 * j + k];
+            }
+        }
+    }
+    fine.q = out;
+    fine.refill_bcs();
+}
+}  // namespace oracle

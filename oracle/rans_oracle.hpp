@@ -170,6 +170,11 @@ struct WallProfile {
 };
 WallProfile get_wall_profile(const ExplicitSolver& s, const std::string& patch);  // post.h:301-387
 
+// Grid sequencing transfer (multigrid.h:99-178 gen_mapper, applied as in
+// multigrid::run, multigrid.h:295-363): coarse.bcs_from_internal(), fine.q =
+// mapper * coarse.q, fine.refill_bcs().
+void prolongate(ExplicitSolver& coarse, ExplicitSolver& fine);
+
 // Face-flux functors, physics.h:160-530.
 void internal_flux(const Gas& g, double nx, double ny, int viscous_type, const double qL[4],
                    const double qR[4], const double gx[4], const double gy[4], double f[4]);

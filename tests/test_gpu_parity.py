@@ -238,3 +238,29 @@ def test_nonfinite_flagged(afx):
     with pytest.raises(AfxError) as ei:
         g.iterate(50)
     assert ei.value.code == 4
+
+
+def test_prolongate_bitexact(afx, orc):
+    # multigrid::run's coarse -> fine transfer (multigrid.h:99-178, 316-321)
+    from aeroflex_gb300 import meshgen
+    from tests.cases import DEG
+    bcs = {"farfield": dict(type="farfield", T=1.0, mach=0.5, angle=1.25 * DEG, p=1.0),
+           "wall": dict(type="slip-wall")}
+    mc = meshgen.airfoil_omesh(32, 16, split=False)
+    mf = meshgen.airfoil_omesh(64, 32, split=False)
+    oc = oracle_solver(orc, mc, bcs)
+    oc.init()
+    oc.iterate(30)
+    of = oracle_solver(orc, mf, bcs)
+    of.init()
+    of.prolongate_from(oc)
+    gc = gpu_solver(afx, mc, bcs)
+    gc.init()
+    gc.set_q(oc.q())
+    gf = gpu_solver(afx, mf, bcs)
+    gf.init()
+    gf.prolongate_from(gc)
+    np.testing.assert_array_equal(gf.get_q(), of.q())
+    of.iterate(3)
+    gf.iterate(3)
+    np.testing.assert_array_equal(gf.get_q(), of.q())
