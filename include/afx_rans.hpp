@@ -6,13 +6,13 @@
 // tiny::config / Settings / mesh, tinyconfig.hpp:86-92, core.h:239, mesh.h:154).
 //
 // Differences from the reference, all deliberate:
-//  * the explicit solver runs on the GPU (the reference's default is its
-//    implicit Eigen solver, core.h:178); `solver = implicit` in the INI is
-//    accepted and run explicitly;
-//  * solve_airfoil solves on one mesh level (the reference sequences the
-//    _coarse and _mid meshes, rans.h:84-85, 99-102);
-//  * mesh paths come from the caller (rans.h:84 hard-codes
-//    "../../../../examples/rans/").
+//  * both solvers run on the GPU; `solver = implicit` (the reference's
+//    default, core.h:178) uses the library's block-Jacobian GMRES in place of
+//    Eigen's ILUT-preconditioned GMRES, so its iterates differ while its
+//    converged solution is the same;
+//  * mesh paths come from the caller (rans.h:84-85 hard-code
+//    "../../../../examples/rans/<name>_coarse.msh" and "_mid.msh"); pass
+//    both to solve_airfoil for the reference's two-level sequence.
 #pragma once
 
 #include <atomic>
@@ -136,6 +136,8 @@ class solver {
         afx_check(afx_set_farfield(h_, patch.c_str(), mach, angle, T, p));
     }
     void request_stop() { afx_request_stop(h_); }
+    // multigrid::run's level transfer (multigrid.h:316-321)
+    void prolongate_from(solver& coarse) { afx_check(afx_prolongate(coarse.h_, h_)); }
     afx_solver handle() const { return h_; }
 
   private:
@@ -174,31 +176,48 @@ class Rans {
             loaded_ = true;
         }
     }
-    // rans.h:78-106 / 116-123 on one level: the farfield angle is alpha * 0.01745
-    // (rans.h:88,94), the state carries over between angles (run(false)).
-    void solve_airfoil(const std::string& mesh_path, airfoil_db& db, const std::string& farfield = "farfield",
-                       const std::string& wall = "wall") {
+    // rans.h:78-106 / 116-123: the farfield angle is alpha * 0.01745
+    // (rans.h:88,94); for every angle the levels run in order, each finer
+    // level starting from the coarser one's solution (multigrid::run,
+    // multigrid.h:295-363), and every level keeps its own state from one
+    // angle to the next (run(false)).  The polar is read on the last level.
+    void solve_airfoil(const std::vector<std::string>& level_paths, airfoil_db& db,
+                       const std::string& farfield = "farfield", const std::string& wall = "wall") {
+        if (level_paths.empty()) throw std::runtime_error("[RANS] no mesh");
         iters = 0;
         if (alphas.empty()) compute_alphas();
-        mesh_.reset(new mesh(mesh_path));
-        solver s(*mesh_, settings);
+        levels_.clear();
+        meshes_.clear();
+        for (const auto& p : level_paths) {
+            meshes_.emplace_back(new mesh(p));
+            levels_.emplace_back(new solver(*meshes_.back(), settings));
+        }
         const std::vector<double> v = settings.bc_vars(farfield);  // T, mach, angle, p
-        s.set_farfield(farfield, v[1], alphas.front() * 0.01745, v[0], v[3]);
-        s.init();
+        levels_[0]->set_farfield(farfield, v[1], alphas.front() * 0.01745, v[0], v[3]);
+        levels_[0]->init();
         for (double a : alphas) {
-            s.set_farfield(farfield, v[1], a * 0.01745, v[0], v[3]);
-            iters += s.run_solver();
-            for (double r : s.residual_history()) residuals.push_back(r);
-            wallProfile wp = get_wall_profile(s, wall);
+            for (auto& s : levels_) s->set_farfield(farfield, v[1], a * 0.01745, v[0], v[3]);
+            for (size_t i = 0; i < levels_.size(); ++i) {
+                if (i > 0) levels_[i]->prolongate_from(*levels_[i - 1]);
+                iters += levels_[i]->run_solver();
+                for (double r : levels_[i]->residual_history()) residuals.push_back(r);
+            }
+            wallProfile wp = get_wall_profile(*levels_.back(), wall);
             db.alpha.push_back(a);
             db.cl.push_back(wp.cl);
             db.cd.push_back(wp.cd);
             db.cmy.push_back(wp.cm);
         }
     }
+    void solve_airfoil(const std::string& mesh_path, airfoil_db& db, const std::string& farfield = "farfield",
+                       const std::string& wall = "wall") {
+        solve_airfoil(std::vector<std::string>{mesh_path}, db, farfield, wall);
+    }
 
   private:
     std::unique_ptr<mesh> mesh_;
+    std::vector<std::unique_ptr<mesh>> meshes_;
+    std::vector<std::unique_ptr<solver>> levels_;
     bool loaded_ = false;
 };
 

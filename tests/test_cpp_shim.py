@@ -79,3 +79,30 @@ def test_cpp_polar_matches_python(afx, tmp_path):
         g.run_solver()
         w = afx.get_wall_profile(g, "wall")
         np.testing.assert_array_equal([cl, cd, cm], [w["cl"], w["cd"], w["cm"]])
+
+
+@pytest.mark.gpu
+def test_cpp_two_level_polar_matches_python(afx, tmp_path):
+    # the reference's coarse -> mid sequence (rans.h:84-85, multigrid.h:295-363)
+    exe = _build(afx, tmp_path)
+    paths = []
+    for k, (ns, nr) in enumerate(((24, 12), (48, 24))):
+        p = str(tmp_path / ("l%d.msh" % k))
+        meshgen.write_gmsh(p, meshgen.airfoil_omesh(ns, nr, split=False))
+        paths.append(p)
+    ini = tmp_path / "c.ini"
+    ini.write_text(INI)
+    out = subprocess.run([exe, str(ini)] + paths, capture_output=True, text=True, check=True).stdout.split("\n")
+    rows = [list(map(float, l.split())) for l in out if l and not l.startswith("iterations")]
+    st = afx.Settings.from_ini(str(ini))
+    lv = [afx.Solver(afx.mesh(p), st) for p in paths]
+    lv[0].set_farfield("farfield", 0.5, 0.0)
+    lv[0].init()
+    for a, cl, cd, cm in rows:
+        for g in lv:
+            g.set_farfield("farfield", 0.5, a * 0.01745)
+        lv[0].run_solver()
+        lv[1].prolongate_from(lv[0])
+        lv[1].run_solver()
+        w = afx.get_wall_profile(lv[1], "wall")
+        np.testing.assert_array_equal([cl, cd, cm], [w["cl"], w["cd"], w["cm"]])
