@@ -99,6 +99,14 @@ struct DevBuf {
         alloc(n);
         AFX_CUDA(cudaMemcpyAsync(p, src, n, cudaMemcpyHostToDevice, s));
     }
+    void reset() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
     ~DevBuf() {
         if (p) cudaFree(p);
     }
@@ -110,6 +118,9 @@ std::vector<T> cast_vec(const std::vector<double>& v) {
 }
 
 }  // namespace
+
+static void lsq_weights(const HostMesh& m, const DeviceLayout& L, std::vector<double>& lsqw64,
+                        std::vector<int>& code);
 
 struct afx_solver_s {
     Settings st;
@@ -254,6 +265,17 @@ struct afx_solver_s {
     };
     std::unique_ptr<AdjointBufs> adj;
     int adj_parity = 0;  // lam[adj_parity] holds the last adjoint solution
+    std::string adj_patch, adj_objective;  // what the last adjoint solution is of
+    // inverse-distance deformation of one boundary patch (afx_deform_patch)
+    struct PatchDeform {
+        std::string patch;
+        double power = 0;
+        std::vector<int> pnodes;      // the patch's nodes, ascending
+        std::vector<double> pnx, pny; // their unit normals (undeformed mesh)
+        std::vector<char> role;       // per node: 0 volume, 1 on the patch, 2 on another boundary (fixed)
+        std::vector<double> W;        // per volume node: sum of the inverse-distance weights
+    };
+    std::unique_ptr<PatchDeform> pdef;
     AdjointBufs& adjoint() {
         if (!fp64) throw Error(AFX_ERR_CONFIG, "the adjoint needs an fp64 solver");
         if (a.visc != 0) throw Error(AFX_ERR_CONFIG, "the adjoint covers the inviscid flux only");
@@ -300,6 +322,69 @@ struct afx_solver_s {
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (stream) cudaStreamDestroy(stream);
+    }
+
+    // host copies of the mesh and its device layout (the geometry can be
+    // deformed: afx_deform_patch)
+    HostMesh hm;
+    DeviceLayout hl;
+    std::vector<double> nodes0x, nodes0y;  // undeformed node coordinates
+
+    // geometry kept on the host: boundary edges for the forces, centroids for
+    // grid sequencing
+    void host_geometry() {
+        const HostMesh& m = hm;
+        const DeviceLayout& L = hl;
+        bedges.clear();
+        for (size_t b = 0; b < m.boundaryEdges.size(); ++b) {
+            const uint32_t e = m.boundaryEdges[b];
+            bedges.push_back({m.boundaryEdgesPhysicals[b], L.cell_new[m.edgesCells[e][0]], m.edgesCentersX[e],
+                              m.edgesCentersY[e], m.edgesNormalsX[e], m.edgesNormalsY[e], m.edgesLengths[e]});
+        }
+        patches.clear();
+        geo_cx = m.cellsCentersX;
+        geo_cy = m.cellsCentersY;
+        geo_area = m.cellsAreas;
+        dev_cx.resize(L.n_cells);
+        dev_cy.resize(L.n_cells);
+        for (int i = 0; i < L.n_cells; ++i) {
+            dev_cx[i] = m.cellsCentersX[L.cell_old[i]];
+            dev_cy[i] = m.cellsCentersY[L.cell_old[i]];
+        }
+        d_geo.reset();
+        d_devc.reset();
+    }
+
+    // new node coordinates: metrics, device geometry, host geometry
+    void set_nodes(const double* x, const double* y) {
+        hm.update_nodes(x, y);
+        fill_layout_geometry(hm, hl);
+        auto put = [&](const void* dst, const std::vector<double>& v, bool f32) {
+            if (f32) {
+                std::vector<float> f(v.begin(), v.end());
+                AFX_CUDA(cudaMemcpyAsync((void*)dst, f.data(), f.size() * 4, cudaMemcpyHostToDevice, stream));
+                AFX_CUDA(cudaStreamSynchronize(stream));
+            } else {
+                AFX_CUDA(cudaMemcpyAsync((void*)dst, v.data(), v.size() * 8, cudaMemcpyHostToDevice, stream));
+            }
+        };
+        std::vector<double> lw;
+        std::vector<int> code;
+        if (a.lsq) lsq_weights(hm, hl, lw, code);
+        for (StepArgs* m : {&a, &a64}) {
+            if (!m->fn) continue;
+            const bool f32 = (m == &a) && !fp64;
+            if (m == &a64 && a64.fn == a.fn) continue;
+            put(m->area, hl.area, f32);
+            put(m->fn, hl.fn, f32);
+            put(m->fLg, hl.fLg, f32);
+            put(m->fd0, hl.fd0, f32);
+            put(m->fd1, hl.fd1, f32);
+            put(m->ft, hl.ft, f32);
+            if (m->lsq && m->lsqw) put(m->lsqw, lw, f32);
+        }
+        AFX_CUDA(cudaStreamSynchronize(stream));
+        host_geometry();  // (captured iteration graphs read the arrays in place)
     }
 
     // grid sequencing (multigrid.h:99-178): centroids and areas of all cells
@@ -843,6 +928,47 @@ void afx_config_free(afx_config c) { delete c; }
 // ---------------------------------------------------------------- solver
 }  // extern "C"
 
+// Least-squares gradient weights (solver.h:402-422) per real cell, over its
+// local edges in their own order: M = (d^T d)^-1 (closed form), weights M d_j,
+// and the cslot slot of each local edge.
+static void lsq_weights(const HostMesh& m, const DeviceLayout& L, std::vector<double>& lsqw64,
+                        std::vector<int>& code) {
+    const size_t N = L.n_cells;
+    std::vector<int> face_of_edge(L.n_faces);
+    for (int f = 0; f < L.n_faces; ++f) face_of_edge[L.face_edge[f]] = f;
+    lsqw64.assign(8 * N, 0.0);
+    code.assign(N, 0);
+    for (size_t i = 0; i < N; ++i) {
+        const uint32_t c = (uint32_t)L.cell_old[i];
+        const uint32_t nj = m.cellsIsTriangle[c] ? 3 : 4;
+        double dx[4], dy[4], a00 = 0, a01 = 0, a11 = 0;
+        int cd = (int)nj << 8;
+        for (uint32_t j = 0; j < nj; ++j) {
+            const uint32_t e = m.cellsEdges[c][j];
+            const uint32_t cn = m.edgesCells[e][0] == c ? m.edgesCells[e][1] : m.edgesCells[e][0];
+            dx[j] = m.cellsCentersX[cn] - m.cellsCentersX[c];
+            dy[j] = m.cellsCentersY[cn] - m.cellsCentersY[c];
+            a00 += dx[j] * dx[j];
+            a01 += dx[j] * dy[j];
+            a11 += dy[j] * dy[j];
+            int slot = -1;
+            for (int sl = 0; sl < 4; ++sl) {
+                const int v = L.cslot[4 * i + sl];
+                if (v != 0 && (v > 0 ? v : -v) - 1 == face_of_edge[e]) slot = sl;
+            }
+            if (slot < 0) throw Error(AFX_ERR_MESH, "least squares: cell edge not among its faces");
+            cd |= slot << (2 * j);
+        }
+        const double invdet = 1.0 / (a00 * a11 - a01 * a01);
+        const double M0 = a11 * invdet, M1 = -a01 * invdet, M2 = -a01 * invdet, M3 = a00 * invdet;
+        for (uint32_t j = 0; j < nj; ++j) {
+            lsqw64[8 * i + 2 * j] = M0 * dx[j] + M1 * dy[j];
+            lsqw64[8 * i + 2 * j + 1] = M2 * dx[j] + M3 * dy[j];
+        }
+        code[i] = cd;
+    }
+}
+
 // The device solver of one mesh (a single case, or the union of a batch's
 // cases) with settings `st`.
 static std::unique_ptr<afx_solver_s> make_solver(const HostMesh& m, const DeviceLayout& L, const Settings& st0) {
@@ -854,25 +980,12 @@ static std::unique_ptr<afx_solver_s> make_solver(const HostMesh& m, const Device
         s->st = st0;
         if (s->st.viscosity_code() == VISC_SA)
             throw Error(AFX_ERR_CONFIG, "spalart-allmaras is not available in this build");
-        {
-            for (size_t b = 0; b < m.boundaryEdges.size(); ++b) {
-                const uint32_t e = m.boundaryEdges[b];
-                s->bedges.push_back({m.boundaryEdgesPhysicals[b], L.cell_new[m.edgesCells[e][0]], m.edgesCentersX[e],
-                                     m.edgesCentersY[e], m.edgesNormalsX[e], m.edgesNormalsY[e], m.edgesLengths[e]});
-            }
-            s->cell_old = L.cell_old;
-            s->h_fcell = L.fcell;
-            s->h_cslot = L.cslot;
-            s->geo_cx = m.cellsCentersX;
-            s->geo_cy = m.cellsCentersY;
-            s->geo_area = m.cellsAreas;
-            s->dev_cx.resize(L.n_cells);
-            s->dev_cy.resize(L.n_cells);
-            for (int i = 0; i < L.n_cells; ++i) {
-                s->dev_cx[i] = m.cellsCentersX[L.cell_old[i]];
-                s->dev_cy[i] = m.cellsCentersY[L.cell_old[i]];
-            }
-        }
+        s->hm = m;
+        s->hl = L;
+        s->host_geometry();
+        s->cell_old = L.cell_old;
+        s->h_fcell = L.fcell;
+        s->h_cslot = L.cslot;
         s->fp64 = s->st.precision != "fp32-mixed";
         AFX_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
         AFX_CUDA(cudaEventCreate(&s->ev0));
@@ -920,41 +1033,8 @@ static std::unique_ptr<afx_solver_s> make_solver(const HostMesh& m, const Device
         a.limiter = st.limiter == "michalak" ? 1 : 0;
         std::vector<double> lsqw64;
         if (st.gradient == "least-squares") {
-            // solver.h:402-422 per real cell, over its local edges in their
-            // own order: M = (d^T d)^-1 (closed form), weights M d_j
-            std::vector<int> face_of_edge(L.n_faces);
-            for (int f = 0; f < L.n_faces; ++f) face_of_edge[L.face_edge[f]] = f;
-            lsqw64.assign(8 * N, 0.0);
-            std::vector<int> code(N);
-            for (size_t i = 0; i < N; ++i) {
-                const uint32_t c = (uint32_t)L.cell_old[i];
-                const uint32_t nj = m.cellsIsTriangle[c] ? 3 : 4;
-                double dx[4], dy[4], a00 = 0, a01 = 0, a11 = 0;
-                int cd = (int)nj << 8;
-                for (uint32_t j = 0; j < nj; ++j) {
-                    const uint32_t e = m.cellsEdges[c][j];
-                    const uint32_t cn = m.edgesCells[e][0] == c ? m.edgesCells[e][1] : m.edgesCells[e][0];
-                    dx[j] = m.cellsCentersX[cn] - m.cellsCentersX[c];
-                    dy[j] = m.cellsCentersY[cn] - m.cellsCentersY[c];
-                    a00 += dx[j] * dx[j];
-                    a01 += dx[j] * dy[j];
-                    a11 += dy[j] * dy[j];
-                    int slot = -1;
-                    for (int sl = 0; sl < 4; ++sl) {
-                        const int v = L.cslot[4 * i + sl];
-                        if (v != 0 && (v > 0 ? v : -v) - 1 == face_of_edge[e]) slot = sl;
-                    }
-                    if (slot < 0) throw Error(AFX_ERR_MESH, "least squares: cell edge not among its faces");
-                    cd |= slot << (2 * j);
-                }
-                const double invdet = 1.0 / (a00 * a11 - a01 * a01);
-                const double M0 = a11 * invdet, M1 = -a01 * invdet, M2 = -a01 * invdet, M3 = a00 * invdet;
-                for (uint32_t j = 0; j < nj; ++j) {
-                    lsqw64[8 * i + 2 * j] = M0 * dx[j] + M1 * dy[j];
-                    lsqw64[8 * i + 2 * j + 1] = M2 * dx[j] + M3 * dy[j];
-                }
-                code[i] = cd;
-            }
+            std::vector<int> code;
+            lsq_weights(m, L, lsqw64, code);
             a.lsq = 1;
             a.lsqw = s->fp64 ? s->dupload(lsqw64) : s->dupload(cast_vec<float>(lsqw64));
             a.lsqs = (const int*)s->dupload(code);
@@ -1844,8 +1924,12 @@ int afx_adjoint_solve(afx_solver s, const char* patch, const char* objective, do
         ForceArgs f = force_args(s, patch, vf);
         AFX_CUDA(cudaMemsetAsync(J.g.p, 0, N * 32, s->stream));
         enqueue_objective_grad(f, cx, cy, J.g.p, s->stream);
-        // gradients, limiter and local time step of the converged state
-        enqueue_adjoint_prep(a, p, true, s->stream);
+        // gradients, limiter and local time step of the converged state; an
+        // implicit solver's CFL is not an explicit one: the pseudo-time steps
+        // then use CFL 1
+        StepArgs ap = a;
+        if (s->imp) ap.cfl = 1.0;
+        enqueue_adjoint_prep(ap, p, true, s->stream);
         // pseudo-time iteration lam <- lam + relax*dt*(J^T lam + dJ/dq) with
         // the solver's three stages (alpha = 1/4, 1/2, 1), from lam = 0
         AFX_CUDA(cudaMemsetAsync(J.lam[0].p, 0, N * 32, s->stream));
@@ -1905,6 +1989,8 @@ int afx_adjoint_solve(afx_solver s, const char* patch, const char* objective, do
         AFX_CUDA(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
         s->last_sec = ms * 1e-3;
         s->adj_parity = q;
+        s->adj_patch = patch;
+        s->adj_objective = obj;
         if (iters) *iters = it;
         if (res) *res = r / r0;
         // dJ/dalpha, dJ/dM = explicit terms + lam . dR/dbq . dbq/d(alpha, M)
@@ -1931,6 +2017,163 @@ int afx_adjoint_solve(afx_solver s, const char* patch, const char* objective, do
             s->stop.store(0);
             throw Error(AFX_ERR_STOPPED, "stopped by request");
         }
+    });
+}
+
+// Inverse-distance deformation data of `patch` with weights d^-power: the
+// patch nodes (normals from the undeformed mesh), the nodes of the other
+// boundary patches (held fixed), and each volume node's weight sum.
+static afx_solver_s::PatchDeform& patch_deform(afx_solver_s* s, const std::string& patch, double power) {
+    if (s->pdef && s->pdef->patch == patch && s->pdef->power == power) return *s->pdef;
+    const HostMesh& m = s->hm;
+    if (s->nodes0x.empty()) {
+        s->nodes0x = m.nodesX;
+        s->nodes0y = m.nodesY;
+    }
+    const std::vector<double>&X = s->nodes0x, &Y = s->nodes0y;
+    auto d = std::make_unique<afx_solver_s::PatchDeform>();
+    d->patch = patch;
+    d->power = power;
+    const size_t V = X.size();
+    d->role.assign(V, 0);
+    std::vector<double> nx(V, 0.), ny(V, 0.);
+    // undeformed edge normals: the metrics of the undeformed nodes
+    HostMesh m0 = m;
+    m0.update_nodes(X.data(), Y.data());
+    for (size_t b = 0; b < m0.boundaryEdges.size(); ++b) {
+        const uint32_t e = m0.boundaryEdges[b];
+        const bool on = m0.boundaryEdgesPhysicals[b] == patch;
+        for (int k = 0; k < 2; ++k) {
+            const uint32_t v = m0.edgesNodes[e][k];
+            if (on) {
+                d->role[v] = 1;
+                nx[v] += m0.edgesNormalsX[e];
+                ny[v] += m0.edgesNormalsY[e];
+            } else if (d->role[v] != 1) {
+                d->role[v] = 2;
+            }
+        }
+    }
+    std::vector<int> fixed;
+    for (size_t v = 0; v < V; ++v) {
+        if (d->role[v] == 1) {
+            const double l = std::sqrt(nx[v] * nx[v] + ny[v] * ny[v]);
+            d->pnodes.push_back((int)v);
+            d->pnx.push_back(nx[v] / l);
+            d->pny.push_back(ny[v] / l);
+        } else if (d->role[v] == 2) {
+            fixed.push_back((int)v);
+        }
+    }
+    if (d->pnodes.empty()) throw Error(AFX_ERR_ARG, "no boundary edges on patch '" + patch + "'");
+    d->W.assign(V, 0.);
+#pragma omp parallel for
+    for (long v = 0; v < (long)V; ++v) {
+        if (d->role[v] != 0) continue;
+        double w = 0;
+        for (int k : d->pnodes) w += std::pow(std::hypot(X[v] - X[k], Y[v] - Y[k]), -power);
+        for (int f : fixed) w += std::pow(std::hypot(X[v] - X[f], Y[v] - Y[f]), -power);
+        d->W[v] = w;
+    }
+    s->pdef = std::move(d);
+    return *s->pdef;
+}
+
+// Node displacement of a unit normal displacement of patch node k (index
+// into pnodes), added with factor c to (x, y)
+static void add_patch_mode(const afx_solver_s* s, const afx_solver_s::PatchDeform& d, int k, double c,
+                           std::vector<double>& x, std::vector<double>& y) {
+    const std::vector<double>&X = s->nodes0x, &Y = s->nodes0y;
+    const int vk = d.pnodes[k];
+    const double nxk = d.pnx[k], nyk = d.pny[k], p = d.power;
+    const long V = (long)X.size();
+#pragma omp parallel for
+    for (long v = 0; v < V; ++v) {
+        if (d.role[v] != 0) continue;
+        const double w = std::pow(std::hypot(X[v] - X[vk], Y[v] - Y[vk]), -p) / d.W[v];
+        x[v] += c * w * nxk;
+        y[v] += c * w * nyk;
+    }
+    x[vk] += c * nxk;
+    y[vk] += c * nyk;
+}
+
+int afx_patch_nodes(afx_solver s, const char* patch, long long* ids, double* nx, double* ny, int cap, int* n) {
+    return guarded([&] {
+        if (!s || !patch || !n) throw Error(AFX_ERR_ARG, "null argument");
+        const auto& d = patch_deform(s, patch, s->pdef ? s->pdef->power : 2.0);
+        *n = (int)d.pnodes.size();
+        for (int k = 0; k < *n && k < cap; ++k) {
+            if (ids) ids[k] = d.pnodes[k];
+            if (nx) nx[k] = d.pnx[k];
+            if (ny) ny[k] = d.pny[k];
+        }
+    });
+}
+
+int afx_deform_patch(afx_solver s, const char* patch, const double* a, int n, double power) {
+    return guarded([&] {
+        if (!s || !patch || !a) throw Error(AFX_ERR_ARG, "null argument");
+        if (power <= 0) power = 2.0;
+        const auto& d = patch_deform(s, patch, power);
+        if (n != (int)d.pnodes.size())
+            throw Error(AFX_ERR_ARG, "expected " + std::to_string(d.pnodes.size()) + " patch-node displacements");
+        std::vector<double> x = s->nodes0x, y = s->nodes0y;
+        for (int k = 0; k < n; ++k)
+            if (a[k] != 0) add_patch_mode(s, d, k, a[k], x, y);
+        s->materialize_qW();
+        s->set_nodes(x.data(), y.data());
+    });
+}
+
+int afx_adjoint_patch(afx_solver s, const char* patch, const char* objective, double power, double h, double* dJ,
+                      int n) {
+    return guarded([&] {
+        if (!s || !patch || !objective || !dJ) throw Error(AFX_ERR_ARG, "null argument");
+        if (s->adj_patch != patch || s->adj_objective != objective)
+            throw Error(AFX_ERR_ARG, "afx_adjoint_patch needs afx_adjoint_solve of the same patch and objective first");
+        if (power <= 0) power = 2.0;
+        if (h <= 0) h = 1e-7;
+        const auto& d = patch_deform(s, patch, power);
+        if (n != (int)d.pnodes.size())
+            throw Error(AFX_ERR_ARG, "expected room for " + std::to_string(d.pnodes.size()) + " sensitivities");
+        auto& J = s->adjoint();
+        const size_t N = s->a.n_cells;
+        s->materialize_qW();
+        // lambda (device order) to the host
+        std::vector<double> lam(4 * N), R(4 * N);
+        AFX_CUDA(cudaMemcpyAsync(lam.data(), J.lam[s->adj_parity].p, N * 32, cudaMemcpyDeviceToHost, s->stream));
+        AFX_CUDA(cudaStreamSynchronize(s->stream));
+        const std::vector<double> xc = s->hm.nodesX, yc = s->hm.nodesY;
+        const FarfieldVars vf = s->freestream();
+        const bool cl_obj = std::string(objective) == "cl";
+        StepArgs r = s->a;
+        r.Rq = J.u.p;  // scratch: the solver's qW stays
+        // J(q; X) + lambda . R(q; X) at the current state for nodes (x, y)
+        auto lagr = [&](const std::vector<double>& x, const std::vector<double>& y) {
+            s->set_nodes(x.data(), y.data());
+            s->set_ctrl(0, 0, 0);
+            r.area = s->a.area;
+            enqueue_residual_f64(r, s->parity, s->stream);
+            AFX_CUDA(cudaMemcpyAsync(R.data(), J.u.p, N * 32, cudaMemcpyDeviceToHost, s->stream));
+            double cl = 0, cd = 0;
+            forces_impl(s, patch, vf, &cl, &cd, nullptr, nullptr, 0, nullptr);
+            double lr = 0;
+            for (size_t i = 0; i < 4 * N; ++i) lr += lam[i] * R[i];
+            return (cl_obj ? cl : cd) + lr;
+        };
+        try {
+            for (int k = 0; k < n; ++k) {
+                std::vector<double> xp = xc, yp = yc, xm = xc, ym = yc;
+                add_patch_mode(s, d, k, h, xp, yp);
+                add_patch_mode(s, d, k, -h, xm, ym);
+                dJ[k] = (lagr(xp, yp) - lagr(xm, ym)) / (2 * h);
+            }
+        } catch (...) {
+            s->set_nodes(xc.data(), yc.data());
+            throw;
+        }
+        s->set_nodes(xc.data(), yc.data());
     });
 }
 

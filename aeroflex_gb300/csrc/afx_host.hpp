@@ -90,6 +90,8 @@ struct HostMesh {
     std::vector<std::string> bndName;
 
     void finalize();  // edges, metrics, ghosts (mesh.h:843-884)
+    void compute_metrics();  // mesh.h:378-453 for the real cells
+    void update_nodes(const double* x, const double* y);  // new coordinates, same topology
 };
 
 HostMesh load_gmsh(const std::string& path);
@@ -111,5 +113,8 @@ struct DeviceLayout {
 };
 
 DeviceLayout build_layout(const HostMesh& m);
+// The geometric face and cell records of L (fn, fLg, fd0, fd1, ft, area) from
+// the metrics of m, keeping L's numbering.
+void fill_layout_geometry(const HostMesh& m, DeviceLayout& L);
 
 }  // namespace afx

@@ -232,6 +232,85 @@ void radix_sort(std::vector<uint64_t>& key, std::vector<uint32_t>& val, int key_
 
 }  // namespace
 
+// Cell and edge metrics of the real cells from the node coordinates
+// (mesh.h:378-453); the cell arrays hold the real cells afterwards.
+void HostMesh::compute_metrics() {
+    const uint32_t N = nRealCells;
+    const uint32_t E = (uint32_t)edgesNodes.size();
+    cellsAreas.assign(N, 0.);
+    cellsCentersX.assign(N, 0.);
+    cellsCentersY.assign(N, 0.);
+    edgesLengths.assign(E, 0.);
+    edgesNormalsX.assign(E, 0.);
+    edgesNormalsY.assign(E, 0.);
+    edgesCentersX.assign(E, 0.);
+    edgesCentersY.assign(E, 0.);
+#pragma omp parallel for
+    for (long i = 0; i < (long)N; ++i) {
+        double cx = 0., cy = 0.;
+        uint32_t n = cellsIsTriangle[i] ? 3 : 4;
+        for (uint32_t j = 0; j < n; ++j) {
+            cx += nodesX[cellsNodes[i][j]] / ((double)n);
+            cy += nodesY[cellsNodes[i][j]] / ((double)n);
+        }
+        cellsCentersX[i] = cx;
+        cellsCentersY[i] = cy;
+    }
+#pragma omp parallel for
+    for (long i = 0; i < (long)E; ++i) {
+        const uint32_t a = edgesNodes[i][0], b = edgesNodes[i][1];
+        edgesCentersX[i] = (nodesX[b] + nodesX[a]) * 0.5;
+        edgesCentersY[i] = (nodesY[b] + nodesY[a]) * 0.5;
+        double dex = nodesX[b] - nodesX[a];
+        double dey = nodesY[b] - nodesY[a];
+        double l = std::sqrt(dex * dex + dey * dey);
+        edgesLengths[i] = l;
+        edgesNormalsX[i] = -dey / l;
+        edgesNormalsY[i] = dex / l;
+        double dot = edgesNormalsX[i] * (edgesCentersX[i] - cellsCentersX[edgesCells[i][0]]) +
+                     edgesNormalsY[i] * (edgesCentersY[i] - cellsCentersY[edgesCells[i][0]]);
+        if (dot < 0) {
+            edgesNormalsX[i] *= -1.;
+            edgesNormalsY[i] *= -1.;
+        }
+    }
+#pragma omp parallel for
+    for (long i = 0; i < (long)N; ++i) {
+        const auto& n = cellsNodes[i];
+        double x1 = nodesX[n[0]], x2 = nodesX[n[1]], x3 = nodesX[n[2]];
+        double y1 = nodesY[n[0]], y2 = nodesY[n[1]], y3 = nodesY[n[2]];
+        if (cellsIsTriangle[i]) {
+            cellsAreas[i] = 0.5 * std::fabs(x1 * (y2 - y3) + x2 * (y3 - y1) + x3 * (y1 - y2));
+        } else {
+            double x4 = nodesX[n[3]], y4 = nodesY[n[3]];
+            cellsAreas[i] = 0.5 * std::fabs(x1 * (y2 - y3) + x2 * (y3 - y1) + x3 * (y1 - y2)) +
+                            0.5 * std::fabs(x1 * (y3 - y4) + x3 * (y4 - y1) + x4 * (y1 - y3));
+        }
+    }
+
+}
+
+// New node coordinates, same topology: metrics and ghost-cell geometry
+// (mesh.h:744-787) recomputed with the formulas of finalize().
+void HostMesh::update_nodes(const double* x, const double* y) {
+    std::copy(x, x + nodesX.size(), nodesX.begin());
+    std::copy(y, y + nodesY.size(), nodesY.begin());
+    compute_metrics();
+    for (size_t b = 0; b < boundaryEdges.size(); ++b) {
+        const uint32_t e = boundaryEdges[b];
+        const uint32_t cell = edgesCells[e][0];
+        double area = cellsAreas[cell];
+        double dx = edgesCentersX[e] - cellsCentersX[cell];
+        double dy = edgesCentersY[e] - cellsCentersY[cell];
+        double dist = std::sqrt(dx * dx + dy * dy);
+        double cx = edgesCentersX[e] + dist * edgesNormalsX[e];
+        double cy = edgesCentersY[e] + dist * edgesNormalsY[e];
+        cellsAreas.push_back(area);
+        cellsCentersX.push_back(cx);
+        cellsCentersY.push_back(cy);
+    }
+}
+
 void HostMesh::finalize() {
     const uint32_t N = (uint32_t)cellsNodes.size();
     const uint64_t NN = nodesX.size();
@@ -298,57 +377,7 @@ void HostMesh::finalize() {
         s = t;
     }
 
-    // metrics (mesh.h:378-453)
-    cellsAreas.assign(N, 0.);
-    cellsCentersX.assign(N, 0.);
-    cellsCentersY.assign(N, 0.);
-    edgesLengths.assign(E, 0.);
-    edgesNormalsX.assign(E, 0.);
-    edgesNormalsY.assign(E, 0.);
-    edgesCentersX.assign(E, 0.);
-    edgesCentersY.assign(E, 0.);
-#pragma omp parallel for
-    for (long i = 0; i < (long)N; ++i) {
-        double cx = 0., cy = 0.;
-        uint32_t n = cellsIsTriangle[i] ? 3 : 4;
-        for (uint32_t j = 0; j < n; ++j) {
-            cx += nodesX[cellsNodes[i][j]] / ((double)n);
-            cy += nodesY[cellsNodes[i][j]] / ((double)n);
-        }
-        cellsCentersX[i] = cx;
-        cellsCentersY[i] = cy;
-    }
-#pragma omp parallel for
-    for (long i = 0; i < (long)E; ++i) {
-        const uint32_t a = edgesNodes[i][0], b = edgesNodes[i][1];
-        edgesCentersX[i] = (nodesX[b] + nodesX[a]) * 0.5;
-        edgesCentersY[i] = (nodesY[b] + nodesY[a]) * 0.5;
-        double dex = nodesX[b] - nodesX[a];
-        double dey = nodesY[b] - nodesY[a];
-        double l = std::sqrt(dex * dex + dey * dey);
-        edgesLengths[i] = l;
-        edgesNormalsX[i] = -dey / l;
-        edgesNormalsY[i] = dex / l;
-        double dot = edgesNormalsX[i] * (edgesCentersX[i] - cellsCentersX[edgesCells[i][0]]) +
-                     edgesNormalsY[i] * (edgesCentersY[i] - cellsCentersY[edgesCells[i][0]]);
-        if (dot < 0) {
-            edgesNormalsX[i] *= -1.;
-            edgesNormalsY[i] *= -1.;
-        }
-    }
-#pragma omp parallel for
-    for (long i = 0; i < (long)N; ++i) {
-        const auto& n = cellsNodes[i];
-        double x1 = nodesX[n[0]], x2 = nodesX[n[1]], x3 = nodesX[n[2]];
-        double y1 = nodesY[n[0]], y2 = nodesY[n[1]], y3 = nodesY[n[2]];
-        if (cellsIsTriangle[i]) {
-            cellsAreas[i] = 0.5 * std::fabs(x1 * (y2 - y3) + x2 * (y3 - y1) + x3 * (y1 - y2));
-        } else {
-            double x4 = nodesX[n[3]], y4 = nodesY[n[3]];
-            cellsAreas[i] = 0.5 * std::fabs(x1 * (y2 - y3) + x2 * (y3 - y1) + x3 * (y1 - y2)) +
-                            0.5 * std::fabs(x1 * (y3 - y4) + x3 * (y4 - y1) + x4 * (y1 - y3));
-        }
-    }
+    compute_metrics();
 
     // ghost cells (mesh.h:744-787)
     std::vector<uint64_t> skey(ukey);
@@ -491,18 +520,30 @@ DeviceLayout build_layout(const HostMesh& m) {
 
     // face records
     L.fcell.assign(2 * (size_t)E, 0);
+    L.bface.assign(B, 0);
+    for (int f = 0; f < E; ++f) {
+        const uint32_t e = L.face_edge[f];
+        const uint32_t i = m.edgesCells[e][0], j = m.edgesCells[e][1];
+        L.fcell[2 * f] = L.cell_new[i];
+        L.fcell[2 * f + 1] = j < (uint32_t)N ? L.cell_new[j] : -(bnd_of_edge[e] + 1);
+    }
+    for (int b = 0; b < B; ++b) L.bface[b] = face_of_edge[m.boundaryEdges[b]];
+    fill_layout_geometry(m, L);
+    return L;
+}
+
+void fill_layout_geometry(const HostMesh& m, DeviceLayout& L) {
+    const long E = L.n_faces;
+    const int N = L.n_cells;
     L.fn.assign(2 * (size_t)E, 0.);
     L.fLg.assign(2 * (size_t)E, 0.);
     L.fd0.assign(2 * (size_t)E, 0.);
     L.fd1.assign(2 * (size_t)E, 0.);
     L.ft.assign(4 * (size_t)E, 0.);
-    L.bface.assign(B, 0);
 #pragma omp parallel for
-    for (long f = 0; f < (long)E; ++f) {
+    for (long f = 0; f < E; ++f) {
         const uint32_t e = L.face_edge[f];
         const uint32_t i = m.edgesCells[e][0], j = m.edgesCells[e][1];
-        L.fcell[2 * f] = L.cell_new[i];
-        L.fcell[2 * f + 1] = j < (uint32_t)N ? L.cell_new[j] : -(bnd_of_edge[e] + 1);
         L.fn[2 * f] = m.edgesNormalsX[e];
         L.fn[2 * f + 1] = m.edgesNormalsY[e];
         // Green-Gauss face weight, solver.h:436-444
@@ -529,10 +570,8 @@ DeviceLayout build_layout(const HostMesh& m) {
         L.ft[4 * f + 1] = t1;
         L.ft[4 * f + 2] = lij;
     }
-    for (int b = 0; b < B; ++b) L.bface[b] = face_of_edge[m.boundaryEdges[b]];
     L.area.assign(N, 0.);
     for (int i = 0; i < N; ++i) L.area[i] = m.cellsAreas[L.cell_old[i]];
-    return L;
 }
 
 }  // namespace afx

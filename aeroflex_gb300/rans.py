@@ -31,7 +31,8 @@ ABI_SYMBOLS = [
     "afx_batch_set_state", "afx_batch_get_state", "afx_batch_iterate", "afx_batch_run_to_convergence",
     "afx_batch_case_history", "afx_batch_forces", "afx_batch_set_farfield", "afx_batch_autotune",
     "afx_batch_last_device_seconds", "afx_residual_vjp", "afx_boundary_states", "afx_adjoint_solve",
-    "afx_adjoint_state", "afx_linear_iterations", "afx_prolongate",
+    "afx_adjoint_state", "afx_linear_iterations", "afx_prolongate", "afx_patch_nodes", "afx_deform_patch",
+    "afx_adjoint_patch",
 ]
 N_KERNEL_KINDS = 7
 
@@ -112,6 +113,9 @@ def lib():
         "afx_adjoint_state": (i, [vp, vp, ll]),
         "afx_linear_iterations": (i, [vp, P(i)]),
         "afx_prolongate": (i, [vp, vp]),
+        "afx_patch_nodes": (i, [vp, cp, vp, vp, vp, i, P(i)]),
+        "afx_deform_patch": (i, [vp, cp, vp, i, d]),
+        "afx_adjoint_patch": (i, [vp, cp, cp, d, d, vp, i]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -344,6 +348,28 @@ class Solver:
         _check(lib().afx_adjoint_solve(self.h, patch.encode(), objective.encode(), float(tol), int(max_it), _ptr(dJ),
                                        ctypes.byref(it), ctypes.byref(res)))
         return (float(dJ[0]), float(dJ[1])), it.value, res.value
+
+    def patch_nodes(self, patch="wall"):
+        """(node ids, unit normals nx, ny) of a boundary patch."""
+        n = ctypes.c_int()
+        _check(lib().afx_patch_nodes(self.h, patch.encode(), None, None, None, 0, ctypes.byref(n)))
+        ids = np.empty(n.value, np.int64)
+        nx = np.empty(n.value, np.float64)
+        ny = np.empty(n.value, np.float64)
+        _check(lib().afx_patch_nodes(self.h, patch.encode(), _ptr(ids), _ptr(nx), _ptr(ny), n.value, ctypes.byref(n)))
+        return ids, nx, ny
+
+    def deform_patch(self, a, patch="wall", power=2.0):
+        a = np.ascontiguousarray(a, np.float64)
+        _check(lib().afx_deform_patch(self.h, patch.encode(), _ptr(a), a.size, float(power)))
+
+    def adjoint_patch(self, patch="wall", objective="cl", power=2.0, h=0.0):
+        """dJ/da_k for every patch node (after adjoint_solve of the same J)."""
+        n = len(self.patch_nodes(patch)[0])
+        out = np.empty(n, np.float64)
+        _check(lib().afx_adjoint_patch(self.h, patch.encode(), objective.encode(), float(power), float(h), _ptr(out),
+                                       n))
+        return out
 
     def adjoint_state(self):
         lam = np.empty(4 * self.n_real, np.float64)

@@ -203,7 +203,7 @@ int afx_boundary_states(afx_solver s, double* bq, long long n);
 /* Sensitivities of a force coefficient J ("cl" or "cd" over `patch`,
  * post.h:301-387) at the solver's (converged) state: solves
  * (dR/dq)^T lam = -(dJ/dq)^T by pseudo-time iteration with the solver's own
- * local time step and three stages, until ||(dR/dq)^T lam + dJ/dq|| falls
+ * local time step (CFL 1 for an implicit solver) and three stages, until ||(dR/dq)^T lam + dJ/dq|| falls
  * below tol * ||dJ/dq|| (tol <= 0: 1e-10) or max_it iterations
  * (<= 0: 100000).  dJ[0] = dJ/d(angle) per radian of the farfield angle,
  * dJ[1] = dJ/d(Mach), both for every farfield-type boundary together.
@@ -212,6 +212,26 @@ int afx_adjoint_solve(afx_solver s, const char* patch, const char* objective, do
                       int* iters, double* res);
 /* The adjoint state lam of the last afx_adjoint_solve (reference order). */
 int afx_adjoint_state(afx_solver s, double* lam, long long n);
+
+/* ---- Shape deformation and surface sensitivities.  No counterpart in the
+ * reference.  A boundary patch (e.g. "wall") deforms by a normal
+ * displacement a_k of each of its nodes (unit normals of the undeformed mesh:
+ * the mean of the adjacent patch-edge normals, pointing out of the flow
+ * domain); every other node moves by inverse-distance weighting
+ * (weights d^-power) of the patch displacements, with the nodes of the other
+ * boundary patches held fixed.  Displacements are relative to the
+ * undeformed mesh (a = 0 restores it); the state is kept. */
+/* The patch's nodes (ascending node index) and their unit normals. */
+int afx_patch_nodes(afx_solver s, const char* patch, long long* ids, double* nx, double* ny, int cap, int* n);
+/* Deform: n == number of patch nodes; power <= 0: 2. */
+int afx_deform_patch(afx_solver s, const char* patch, const double* a, int n, double power);
+/* dJ/da_k for every patch node k, J the objective of the last
+ * afx_adjoint_solve on the same patch (call it first, at the converged
+ * state): dJ/da_k = dJ/da_k|_q + lam . dR/da_k|_q, the geometric partials by
+ * central differences of the residual and the forces with step h
+ * (h <= 0: 1e-7), no re-convergence.  FP64 solvers, inviscid. */
+int afx_adjoint_patch(afx_solver s, const char* patch, const char* objective, double power, double h, double* dJ,
+                      int n);
 
 /* ---- Batched load cases.  No single counterpart in the reference: its
  * polar sweep runs one case after another (src/rans/include/rans/rans.h:

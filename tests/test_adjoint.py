@@ -148,3 +148,50 @@ def test_adjoint_alpha_mach_sensitivities_match_fd(afx):
             fd = (get_wall_profile(gp, "wall")[obj] - get_wall_profile(gm, "wall")[obj]) / (2 * h)
             ad = out[obj][k]
             assert abs(ad - fd) <= 1e-6 * abs(fd) + 1e-9, (obj, k, ad, fd)
+
+
+def _implicit(afx, m, bcs, a=None, **kw):
+    g = gpu_solver(afx, m, bcs, solver="implicit", start_cfl=40.0, slope_cfl=50.0, max_cfl=100.0, **kw)
+    g.init()
+    if a is not None:
+        g.deform_patch(a, "wall", 2.0)
+    it, err = g.run_solver(1e-13, 600)
+    assert err <= 1e-12, (it, err)
+    return g
+
+
+@pytest.mark.parametrize("order,steps,rtol", [
+    # first order: smooth in the shape, steps of 1e-6
+    ("first", (2e-6, 1e-6), 1e-6),
+    # second order: the limiter (min over faces of min(1, .)) switches within
+    # displacements of ~1e-6, so the check takes the step 1e-7; the converged
+    # C_L is good to ~1e-13, which bounds the difference's accuracy near 1e-6
+    ("second", (2e-7, 1e-7), 1e-5),
+])
+def test_adjoint_surface_sensitivities_match_fd(afx, order, steps, rtol):
+    # dJ/da for the normal displacements a of the wall nodes (displacement
+    # spread into the volume by inverse-distance weighting), against central
+    # differences of converged solutions (to 1e-13) on deformed meshes
+    from aeroflex_gb300 import meshgen
+    from aeroflex_gb300.rans import get_wall_profile
+    m = meshgen.airfoil_omesh(32, 24, split=False, m=0.02, p=0.4, t=0.12)
+    bcs = {"farfield": dict(type="farfield", T=1.0, mach=0.5, angle=2.0 * DEG, p=1.0), "wall": dict(type="slip-wall")}
+    kw = dict(second_order=(order == "second"))
+    g = _implicit(afx, m, bcs, **kw)
+    ids, nx, ny = g.patch_nodes("wall")
+    assert len(ids) == 32 and np.allclose(np.hypot(nx, ny), 1.0)
+    rng = np.random.default_rng(3)
+    c = rng.standard_normal(len(ids))
+    dirs = [c / np.linalg.norm(c)]
+    for obj in ("cl", "cd"):
+        g.adjoint_solve("wall", obj, tol=1e-13, max_it=400000)
+        dJ = g.adjoint_patch("wall", obj)
+        for c in dirs:
+            pred = float(c @ dJ)
+            fds = []
+            for eps in steps:
+                Jp = get_wall_profile(_implicit(afx, m, bcs, eps * c, **kw), "wall")[obj]
+                Jm = get_wall_profile(_implicit(afx, m, bcs, -eps * c, **kw), "wall")[obj]
+                fds.append((Jp - Jm) / (2 * eps))
+            fd, unc = 0.5 * (fds[0] + fds[1]), abs(fds[0] - fds[1])
+            assert abs(pred - fd) <= rtol * abs(fd) + unc + 1e-9, (obj, pred, fd, unc)
