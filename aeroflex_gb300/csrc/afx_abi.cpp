@@ -1224,6 +1224,50 @@ int afx_residual(afx_solver s, double* R, long long n) {
 static int implicit_run(afx_solver_s* s, int n, int run_mode, double tol, double* last) {
     s->ensure_shadow();
     s->materialize_qW();
+    if (s->a.n_cases > 0) {
+        // batch: every case follows run_solver on its own (per-case err_0,
+        // err/err_0, tolerance, iteration limit); the right-hand-side rows
+        // of a case that has stopped are zero, so its state holds
+        s->set_ctrl(run_mode, n, tol);
+        StepArgs A = s->A64();
+        A.ctrl = s->a.ctrl;
+        if (run_mode == 1) {
+            double qf[4] = {0, 0, 0, 0};
+            enqueue_uniform_f64(A, s->parity, qf, s->stream);
+        }
+        AFX_CUDA(cudaEventRecord(s->ev0, s->stream));
+        double cfl = s->st.start_cfl;
+        int i = 0;
+        bool stopped = false;
+        while (i < n) {
+            if (s->stop.load()) {
+                stopped = true;
+                break;
+            }
+            const double e = s->implicit_iteration(cfl, 0.0);
+            if (e < 0) {
+                s->imp_sync();
+                throw Error(AFX_ERR_DIVERGED, "implicit solve failed (singular diagonal block)");
+            }
+            enqueue_case_control(A, s->stream);  // per-case norms of the last right-hand side
+            cfl = std::min(s->st.start_cfl + (i + 1) * s->st.slope_cfl, s->st.max_cfl);
+            ++i;
+            s->read_ctrl();
+            if (s->h_ctrl->done) break;
+        }
+        AFX_CUDA(cudaEventRecord(s->ev1, s->stream));
+        AFX_CUDA(cudaEventSynchronize(s->ev1));
+        float ms = 0;
+        AFX_CUDA(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+        s->last_sec = ms * 1e-3;
+        s->imp_sync();
+        if (last) *last = 0;
+        if (stopped) {
+            s->stop.store(0);
+            throw Error(AFX_ERR_STOPPED, "stopped by request");
+        }
+        return i;
+    }
     s->set_ctrl(0, 0, 0);
     StepArgs& A = s->A64();
     if (A.ctrl != s->a.ctrl) AFX_CUDA(cudaMemsetAsync(A.ctrl, 0, sizeof(Ctrl), s->stream));
@@ -1708,6 +1752,18 @@ int afx_batch_create(int n_cases, const afx_mesh* meshes, const afx_config* conf
         a.cctrl = (CaseCtrl*)b->cctrl.p;
         a.chist = (double*)b->chist.p;
         a.qfar_case = (const double*)b->qfar.p;
+        if (s.a64.fn) {  // the FP64 machine (implicit right-hand sides) sees the cases too
+            for (StepArgs* x : {&s.a64, &s.a64it}) {
+                x->n_cases = a.n_cases;
+                x->case_of = a.case_of;
+                x->case_off = a.case_off;
+                x->case_done = a.case_done;
+                x->cell_sq = a.cell_sq;
+                x->cctrl = a.cctrl;
+                x->chist = a.chist;
+                x->qfar_case = a.qfar_case;
+            }
+        }
         AFX_CUDA(cudaMemsetAsync(b->cell_sq.p, 0, u.nRealCells * sizeof(double), s.stream));
         s.set_ctrl(0, 0, 0);
         b->set_freestream();
@@ -1776,8 +1832,13 @@ int afx_batch_iterate(afx_batch b, int n_iters, double* res_norms) {
     return guarded([&] {
         if (!b || n_iters < 0) throw Error(AFX_ERR_ARG, "bad argument");
         afx_solver_s& s = *b->s;
-        s.set_ctrl(0, n_iters, 0);
-        const int done = s.run(n_iters, 0, 0);
+        int done = 0;
+        if (s.imp) {
+            implicit_run(&s, n_iters, 0, 0, nullptr);
+        } else {
+            s.set_ctrl(0, n_iters, 0);
+            done = s.run(n_iters, 0, 0);
+        }
         AFX_CUDA(cudaGetLastError());
         b->read_cases();
         bool bad = false;
@@ -1796,12 +1857,17 @@ int afx_batch_run_to_convergence(afx_batch b, double tol, int max_it, int* iters
         afx_solver_s& s = *b->s;
         if (tol <= 0) tol = s.st.tolerance;
         if (max_it <= 0) max_it = s.st.max_iterations;
-        s.set_ctrl(1, max_it, tol);
-        // get_uniform_residual per case: each cell's case freestream
-        double qf[4] = {0, 0, 0, 0};
-        if (s.fp64) enqueue_uniform_f64(s.a, s.parity, qf, s.stream);
-        else enqueue_uniform_f32(s.a, s.parity, qf, s.stream);
-        const int done = s.run(max_it, 1, tol);
+        int done = 0;
+        if (s.imp) {
+            implicit_run(&s, max_it, 1, tol, nullptr);
+        } else {
+            s.set_ctrl(1, max_it, tol);
+            // get_uniform_residual per case: each cell's case freestream
+            double qf[4] = {0, 0, 0, 0};
+            if (s.fp64) enqueue_uniform_f64(s.a, s.parity, qf, s.stream);
+            else enqueue_uniform_f32(s.a, s.parity, qf, s.stream);
+            done = s.run(max_it, 1, tol);
+        }
         AFX_CUDA(cudaGetLastError());
         b->read_cases();
         for (int c = 0; c < b->n; ++c) {

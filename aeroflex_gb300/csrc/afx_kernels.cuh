@@ -420,11 +420,14 @@ __device__ __forceinline__ void stage_epilogue(const StageOut<T, S>& o, const in
             st4(&o.Rq[i], Rd);
         } else if (o.mode == 3) {
             // implicit right-hand side: the face sums, not divided by the area
-            // (solver.h:1079-1152), and their squared norm
+            // (solver.h:1079-1152), and their squared norm; in a batch, the
+            // rows of a case that has stopped are zero (its update is zero)
             double Rd[4] = {(double)Rsum[0], (double)Rsum[1], (double)Rsum[2], (double)Rsum[3]};
+            if (o.case_done && __ldg(&o.case_done[__ldg(&o.case_of[i])])) Rd[0] = Rd[1] = Rd[2] = Rd[3] = 0.0;
             st4(&o.Rq[i], Rd);
 #pragma unroll
             for (int k = 0; k < 4; ++k) sq += Rd[k] * Rd[k];
+            if (o.cell_sq) o.cell_sq[i] = sq;
         } else if (sizeof(T) == 4) {
             stage_epilogue_mixed<S>(o, i, R, dti, sq);
         } else {

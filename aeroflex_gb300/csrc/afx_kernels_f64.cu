@@ -10,6 +10,11 @@ namespace afx {
 void enqueue_iteration_f64(const StepArgs& a, int p, cudaStream_t s) { dev::iteration<double, double, false>(a, p, s); }
 void enqueue_residual_f64(const StepArgs& a, int p, cudaStream_t s) { dev::residual<double, double>(a, p, s); }
 void enqueue_rhs_f64(const StepArgs& a, int p, cudaStream_t s) { dev::rhs<double, double>(a, p, s); }
+void enqueue_case_control(const StepArgs& a, cudaStream_t s) {
+    dev::k_case_control<<<a.n_cases, 256, 0, s>>>(a.cell_sq, a.case_off, a.cctrl, a.case_done, a.chist, a.ctrl,
+                                                  a.n_cases, 0);
+    dev::k_batch_finalize<<<1, 1, 0, s>>>(a.ctrl, a.n_cases);
+}
 void enqueue_last_stage_residual_f64(const StepArgs& a, int p, cudaStream_t s) {
     dev::last_stage_residual<double, double>(a, p, s);
 }

@@ -129,6 +129,9 @@ void enqueue_residual_f32(const StepArgs& a, int p, cudaStream_t s);
 // Implicit right-hand side (face sums, not divided by the area) of parity p
 // -> Rq, with ||.||^2 block partials (nblocks(n_cells, block) of them).
 void enqueue_rhs_f64(const StepArgs& a, int p, cudaStream_t s);
+// Batch: per-case norms of cell_sq and run_solver control (k_case_control),
+// then the run's iteration count and stop flag.
+void enqueue_case_control(const StepArgs& a, cudaStream_t s);
 // Re-form qW of the last RK stage of the iteration that read parity p.
 void enqueue_last_stage_residual_f64(const StepArgs& a, int p, cudaStream_t s);
 void enqueue_last_stage_residual_f32(const StepArgs& a, int p, cudaStream_t s);

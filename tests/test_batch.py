@@ -144,3 +144,31 @@ def test_batch_rejects_mixed_schemes(afx):
     with pytest.raises(afx.AfxError) as ei:
         afx.Batch(meshes, sets)
     assert ei.value.code == 2
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32-mixed"])
+def test_batch_implicit_polar_converges_per_case(afx, precision):
+    # an implicit batch (FP32-mixed: FP32 Jacobians and Krylov vectors, FP64
+    # right-hand side) reaches each case's FP64 fixed point: converged C_L /
+    # C_D of every case within 1e-8 of the same case solved alone in FP64
+    from aeroflex_gb300 import meshgen
+    imp = dict(solver="implicit", start_cfl=40.0, slope_cfl=50.0, max_cfl=100.0)
+    cases = []
+    for ns, nr, mach, aoa, kw in [(32, 24, 0.5, 1.25, {}), (40, 20, 0.3, 4.0, dict(m=0.04)),
+                                  (24, 24, 0.6, -2.0, dict(t=0.15))]:
+        m = meshgen.airfoil_omesh(ns, nr, split=False, **kw)
+        bcs = {"farfield": dict(type="farfield", T=1.0, mach=mach, angle=aoa * DEG, p=1.0),
+               "wall": dict(type="slip-wall")}
+        cases.append((m, bcs))
+    b = _batch(afx, cases, precision, **imp)
+    b.init()
+    it, err, st = b.run_solver(1e-11, 300)
+    assert (st == 0).all() and (err <= 1e-11).all(), (it, err)
+    for c, (m, bcs) in enumerate(cases):
+        g = gpu_solver(afx, m, bcs, "fp64", **imp)
+        g.init()
+        g.run_solver(1e-11, 300)
+        wg = afx.get_wall_profile(g, "wall")
+        fb = b.forces(c, "wall")
+        for k in ("cl", "cd"):
+            assert abs(fb[k] - wg[k]) <= 1e-8 * max(abs(wg[k]), 1e-3), (c, k, fb[k], wg[k])
