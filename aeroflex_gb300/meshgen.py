@@ -42,7 +42,8 @@ def naca4_surface(n_surf, m=0.0, p=0.4, t=0.12):
     return x, y
 
 
-def airfoil_omesh(n_surf=128, n_rad=64, r_far=20.0, growth=None, first=2e-3, m=0.0, p=0.4, t=0.12, split=True):
+def airfoil_omesh(n_surf=128, n_rad=64, r_far=20.0, growth=None, first=2e-3, m=0.0, p=0.4, t=0.12, split=True,
+                  fade=1):
     """O-mesh around a NACA 4-digit airfoil of chord 1.
 
     ``n_surf`` distinct surface nodes, ``n_rad + 1`` node layers whose
@@ -50,9 +51,11 @@ def airfoil_omesh(n_surf=128, n_rad=64, r_far=20.0, growth=None, first=2e-3, m=0
     centred at mid-chord; the ratio is ``growth`` if given, else the one that
     makes the first layer ``first`` chords thick.  Grid lines leave the
     surface along its normal and blend linearly (in the layer coordinate)
-    into uniformly spaced points on the far-field circle.  Each quad is split
-    into two triangles along a fixed diagonal when ``split``.  Patches:
-    "wall" (airfoil) and "farfield" (outer circle).
+    into uniformly spaced points on the far-field circle; the normal offset
+    fades as (1 - s)^fade in the layer coordinate s (fade = 2 keeps the
+    outer layers of fine meshes from folding).  Each quad is split into two
+    triangles along a fixed diagonal when ``split``.  Patches: "wall"
+    (airfoil) and "farfield" (outer circle).
     """
     sx, sy = naca4_surface(n_surf, m, p, t)
     ang = 2.0 * np.pi * np.arange(n_surf) / n_surf
@@ -74,8 +77,13 @@ def airfoil_omesh(n_surf=128, n_rad=64, r_far=20.0, growth=None, first=2e-3, m=0
     k = np.arange(n_rad + 1)
     s = (growth ** k - 1.0) / (growth ** n_rad - 1.0)
     S = s[:, None]
-    X = (1.0 - S) * (sx[None, :] + r_far * S * nx_[None, :]) + S * fx[None, :]
-    Y = (1.0 - S) * (sy[None, :] + r_far * S * ny_[None, :]) + S * fy[None, :]
+    if fade == 1:
+        X = (1.0 - S) * (sx[None, :] + r_far * S * nx_[None, :]) + S * fx[None, :]
+        Y = (1.0 - S) * (sy[None, :] + r_far * S * ny_[None, :]) + S * fy[None, :]
+    else:
+        F = (1.0 - S) ** fade * r_far * S
+        X = (1.0 - S) * sx[None, :] + F * nx_[None, :] + S * fx[None, :]
+        Y = (1.0 - S) * sy[None, :] + F * ny_[None, :] + S * fy[None, :]
     x = X.reshape(-1)
     y = Y.reshape(-1)
 
@@ -261,6 +269,6 @@ def polar_sweep_cases(n_cases=256, seed=4, n_min=5000, n_max=200000, split=False
         mach = rng.uniform(0.1, 0.7)
         n_rad = max(8, int(round(math.sqrt(n / (4.0 if split else 2.0)))))
         n_surf = 2 * n_rad
-        mesh = airfoil_omesh(n_surf=n_surf, n_rad=n_rad, m=m, p=p, t=t, split=split)
+        mesh = airfoil_omesh(n_surf=n_surf, n_rad=n_rad, m=m, p=p, t=t, split=split, fade=2)
         out.append(dict(mesh=mesh, m=m, t=t, p=p, aoa_deg=aoa, mach=mach, n_cells=len(mesh["cells"])))
     return out

@@ -415,6 +415,60 @@ def batch_sweep(n_cases=256, K=100, K64=10, warmup=3):
     return out
 
 
+def batch_converge(n_cases=16, tol=1e-10, max_it=200):
+    """Polar sweep to convergence: ``n_cases`` cases of the batched polar-sweep
+    generator (seed 4) solved to err/err_0 <= tol by the implicit solver, as
+    one FP32-mixed batch (FP32 Jacobians and Krylov vectors, FP64 residual)
+    and as the FP64 per-case loop.  Reports both device times and the largest
+    C_L / C_D difference between them (the FP32-mixed batch converges to the
+    FP64 fixed point of every case)."""
+    from aeroflex_gb300 import meshgen, rans
+
+    # the subsonic, moderate-angle cases (M <= 0.5, AoA <= 8 deg): the
+    # explicit scheme's transonic high-angle cases do not reach a steady state
+    cases = [c for c in meshgen.polar_sweep_cases(256, seed=4) if c["mach"] <= 0.5 and c["aoa_deg"] <= 8.0][:n_cases]
+    meshes = [rans.mesh.from_arrays(c["mesh"]) for c in cases]
+
+    def settings(c, prec):
+        st = rans.Settings().set("solver", "implicit").set("precision", prec).set("start_cfl", 40.0)
+        st.set("slope_cfl", 50.0).set("max_cfl", 100.0)
+        st.set_bc("farfield", "farfield", 1.0, c["mach"], c["aoa_deg"] * 0.01745, 1.0).set_bc("wall", "slip-wall")
+        return st
+
+    t0 = time.time()
+    b = rans.Batch(meshes, [settings(c, "fp32-mixed") for c in cases])
+    b.init()
+    it_b, err_b, st_b = b.run_solver(tol, max_it)
+    t_batch = b.last_device_seconds()
+    fb = [b.forces(k, "wall") for k in range(n_cases)]
+    del b
+    t64, dcl, dcd, conv = 0.0, 0.0, 0.0, 0
+    its64 = []
+    for k, (c, m) in enumerate(zip(cases, meshes)):
+        s = rans.Solver(m, settings(c, "fp64"))
+        s.init()
+        try:
+            n, e = s.run_solver(tol, max_it)
+        except rans.AfxError:
+            n, e = max_it, float("nan")
+        t64 += s.last_device_seconds()
+        its64.append(n)
+        w = rans.get_wall_profile(s, "wall")
+        if e <= tol and err_b[k] <= tol:
+            conv += 1
+            dcl = max(dcl, abs(w["cl"] - fb[k]["cl"]))
+            dcd = max(dcd, abs(w["cd"] - fb[k]["cd"]))
+        del s
+    return {"cases": n_cases, "cells_total": int(sum(m.nRealCells for m in meshes)), "tolerance": tol,
+            "workload": "first %d cases with M <= 0.5 and AoA <= 8 deg of the polar-sweep generator (seed 4), "
+                        "implicit solver, CFL 40 -> 100" % n_cases,
+            "batch_fp32_mixed_s": t_batch, "per_case_fp64_s": t64,
+            "speedup_batch_fp32_mixed_vs_per_case_fp64": t64 / t_batch if t_batch > 0 else None,
+            "converged_both": conv, "max_abs_dcl": dcl, "max_abs_dcd": dcd,
+            "batch_iterations": [int(x) for x in it_b], "per_case_iterations": its64,
+            "wall_s": time.time() - t0}
+
+
 def cpu_baseline(budget_s=12.0):
     """The oracle (plain-C++ restatement of the reference's explicit solver)
     on a 512 x 256 sample of the same generator, all host threads."""
@@ -475,6 +529,9 @@ def main():
     ap.add_argument("--no-cl", action="store_true", help="skip the time-to-C_L leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched polar-sweep leg")
     ap.add_argument("--batch-cases", type=int, default=256)
+    ap.add_argument("--batch-converge", action="store_true",
+                    help="also solve 16 polar-sweep cases to convergence (implicit FP32-mixed batch vs FP64 per case; "
+                         "about 12 minutes)")
     ap.add_argument("--nx", type=int, default=NX)
     ap.add_argument("--ny", type=int, default=NY)
     ap.add_argument("--lean", action="store_true", help="warm-up + timed iterations only (for ncu)")
@@ -540,6 +597,8 @@ def main():
         line["time_to_cl"] = time_to_cl()
     if not args.no_batch:
         line["batch"] = batch_sweep(args.batch_cases)
+    if args.batch_converge:
+        line["batch_converge"] = batch_converge()
     print(json.dumps(line))
 
 
