@@ -33,6 +33,8 @@ void enqueue_prolong(int nc, const double* cx, const double* cy, const double* c
                      const double* fx, const double* fy, void* fine_q, cudaStream_t s);
 void enqueue_full_state(int n, int nb, const int* cell_old, const int* owner_dev, const void* q, void* full,
                         cudaStream_t s);
+void enqueue_wall_dist(int nc, const double* cx, const double* cy, int nw, const double* wx, const double* wy,
+                       double* out, cudaStream_t s);
 struct ImplicitEngine;
 ImplicitEngine* implicit_create(const StepArgs& a, bool f32, const std::vector<int>& colors, cudaStream_t s);
 void implicit_destroy(ImplicitEngine* e);
@@ -2296,6 +2298,37 @@ int afx_prolongate(afx_solver coarse, afx_solver fine) {
         f.refill_bcs();
         AFX_CUDA(cudaStreamSynchronize(f.stream));
         AFX_CUDA(cudaGetLastError());
+    });
+}
+
+// mesh::compute_wall_dist (mesh.h:794-830) with the solver's boundary
+// conditions: every cell (ghosts included, reference order).
+int afx_wall_distance(afx_solver s, double* out, long long n) {
+    return guarded([&] {
+        if (!s || !out) throw Error(AFX_ERR_ARG, "null argument");
+        const int nc = (int)s->geo_area.size();
+        if (n != nc) throw Error(AFX_ERR_ARG, "size must be n_real_cells + n_boundary_edges");
+        std::vector<double> w;  // wall edge centres in boundary order, then x / y
+        std::vector<double> wy;
+        for (size_t b = 0; b < s->bedges.size(); ++b)
+            if (s->boundary_type[b] == BC_WALL || s->boundary_type[b] == BC_SLIP_WALL) {
+                w.push_back(s->bedges[b].ex);
+                wy.push_back(s->bedges[b].ey);
+            }
+        const int nw = (int)w.size();
+        w.insert(w.end(), wy.begin(), wy.end());
+        std::vector<double> c(2 * (size_t)nc);
+        std::copy(s->geo_cx.begin(), s->geo_cx.end(), c.begin());
+        std::copy(s->geo_cy.begin(), s->geo_cy.end(), c.begin() + nc);
+        DevBuf dc, dw, dout;
+        dc.upload(c.data(), c.size() * 8, s->stream);
+        dw.upload(w.data(), std::max<size_t>(w.size(), 1) * 8, s->stream);
+        dout.alloc((size_t)nc * 8);
+        const double* pc = (const double*)dc.p;
+        const double* pw = (const double*)dw.p;
+        enqueue_wall_dist(nc, pc, pc + nc, nw, pw, pw + nw, (double*)dout.p, s->stream);
+        AFX_CUDA(cudaMemcpyAsync(out, dout.p, (size_t)nc * 8, cudaMemcpyDeviceToHost, s->stream));
+        AFX_CUDA(cudaStreamSynchronize(s->stream));
     });
 }
 

@@ -97,7 +97,48 @@ __global__ void k_full_ghosts(const int n, const int nb, const int* __restrict__
     }
 }
 
+// mesh::compute_wall_dist (mesh.h:794-830): for every cell, the least
+// distance from its centroid to a wall / slip-wall edge centre, scanning the
+// edges in boundary order (std::min), 1 if there is no wall.
+__global__ void __launch_bounds__(256) k_wall_dist(const int nc, const double* __restrict__ cx,
+                                                   const double* __restrict__ cy, const int nw,
+                                                   const double* __restrict__ wx, const double* __restrict__ wy,
+                                                   double* __restrict__ out) {
+    __shared__ double sx[PT], sy[PT];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool act = i < nc;
+    const double xi = act ? cx[i] : 0.0, yi = act ? cy[i] : 0.0;
+    double mind = 1;
+    bool first = true;
+    for (int t0 = 0; t0 < nw; t0 += PT) {
+        const int tn = min(PT, nw - t0);
+        __syncthreads();
+        for (int t = threadIdx.x; t < tn; t += blockDim.x) {
+            sx[t] = wx[t0 + t];
+            sy[t] = wy[t0 + t];
+        }
+        __syncthreads();
+        if (act)
+            for (int t = 0; t < tn; ++t) {
+                const double dx = xi - sx[t], dy = yi - sy[t];
+                const double d = sqrt(dx * dx + dy * dy);
+                if (first) {
+                    mind = d;
+                    first = false;
+                } else {
+                    mind = (d < mind) ? d : mind;
+                }
+            }
+    }
+    if (act) out[i] = mind;
+}
+
 }  // namespace dev
+
+void enqueue_wall_dist(int nc, const double* cx, const double* cy, int nw, const double* wx, const double* wy,
+                       double* out, cudaStream_t s) {
+    dev::k_wall_dist<<<(nc + 255) / 256, 256, 0, s>>>(nc, cx, cy, nw, wx, wy, out);
+}
 
 void enqueue_prolong(int nc, const double* cx, const double* cy, const double* ca, const void* coarse_full, int nf,
                      const double* fx, const double* fy, void* fine_q, cudaStream_t s) {

@@ -32,7 +32,7 @@ ABI_SYMBOLS = [
     "afx_batch_case_history", "afx_batch_forces", "afx_batch_set_farfield", "afx_batch_autotune",
     "afx_batch_last_device_seconds", "afx_residual_vjp", "afx_boundary_states", "afx_adjoint_solve",
     "afx_adjoint_state", "afx_linear_iterations", "afx_prolongate", "afx_patch_nodes", "afx_deform_patch",
-    "afx_adjoint_patch",
+    "afx_adjoint_patch", "afx_wall_distance",
 ]
 N_KERNEL_KINDS = 7
 
@@ -116,6 +116,7 @@ def lib():
         "afx_patch_nodes": (i, [vp, cp, vp, vp, vp, i, P(i)]),
         "afx_deform_patch": (i, [vp, cp, vp, i, d]),
         "afx_adjoint_patch": (i, [vp, cp, cp, d, d, vp, i]),
+        "afx_wall_distance": (i, [vp, vp, ll]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -310,6 +311,12 @@ class Solver:
         ms = ctypes.c_double()
         _check(lib().afx_autotune(self.h, int(iters), buf, 16, ctypes.byref(blk), ctypes.byref(ms)))
         return dict(variant=buf.value.decode(), block=blk.value, ms_per_iter=ms.value)
+
+    def wall_distance(self):
+        """mesh::compute_wall_dist (mesh.h:794-830) on the GPU: all cells."""
+        out = np.empty(self.n_real + self.n_boundary, np.float64)
+        _check(lib().afx_wall_distance(self.h, _ptr(out), out.size))
+        return out
 
     def prolongate_from(self, coarse):
         """Grid-sequencing transfer (multigrid.h:99-178, 316-321): this

@@ -470,8 +470,12 @@ def batch_converge(n_cases=16, tol=1e-10, max_it=200):
 
 
 def cpu_baseline(budget_s=12.0):
-    """The oracle (plain-C++ restatement of the reference's explicit solver)
-    on a 512 x 256 sample of the same generator, all host threads."""
+    """The oracle (plain-C++ restatement of the reference's explicit solver:
+    serial face loops, OpenMP per-cell loops as the reference) on a 512 x 256
+    sample of the same generator, with all host threads and with one thread,
+    plus its time per iteration on the 128 x 128 airfoil case, from which the
+    CPU time to C_L within 1e-6 is extrapolated with the FP64 GPU path's
+    iteration count (same arithmetic, so the same iterations)."""
     from aeroflex_gb300 import meshgen
     from oracle import oracle
 
@@ -480,15 +484,33 @@ def cpu_baseline(budget_s=12.0):
         "farfield": dict(type="farfield", T=1.0, mach=MACH, angle=0.0, p=1.0), "wall": dict(type="slip-wall")})
     s.init()
     s.set_q(meshgen.density_bump_state(marr, mach=MACH))
-    s.time_iterations(1)
-    its, sec = 0, 0.0
-    while sec < budget_s:
-        sec += s.time_iterations(1)
-        its += 1
     n = SAMPLE_NX * SAMPLE_NY * 2
-    return dict(value=n * 3 * its / sec, unit="cell-residual evals/s", cores=os.cpu_count(), kind="port",
-                sample="%d explicit iterations on the %dx%d channel (%d cells), OMP_NUM_THREADS=%s" %
-                       (its, SAMPLE_NX, SAMPLE_NY, n, os.environ.get("OMP_NUM_THREADS", str(os.cpu_count()))))
+    out = {}
+    for threads, budget in ((0, budget_s), (1, budget_s / 2)):
+        oracle.set_threads(threads)
+        s.time_iterations(1)
+        its, sec = 0, 0.0
+        while sec < budget:
+            sec += s.time_iterations(1)
+            its += 1
+        out[threads] = (n * 3 * its / sec, its)
+    # the airfoil case of the time-to-C_L leg
+    am = meshgen.airfoil_omesh(128, 128, split=False)
+    a = oracle.Solver(oracle.Mesh.from_arrays(am), oracle.default_settings(cfl=1.5), {
+        "farfield": dict(type="farfield", T=1.0, mach=0.5, angle=1.25 * 0.01745, p=1.0), "wall": dict(type="slip-wall")})
+    a.init()
+    oracle.set_threads(0)
+    a.time_iterations(2)
+    t_it = a.time_iterations(20) / 20
+    oracle.set_threads(0)
+    return {"value": out[0][0], "unit": "cell-residual evals/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": "%d explicit iterations on the %dx%d channel (%d cells), all %d host threads" %
+                      (out[0][1], SAMPLE_NX, SAMPLE_NY, n, os.cpu_count()),
+            "one_thread": {"value": out[1][0], "iterations": out[1][1]},
+            "airfoil_ms_per_iteration": t_it * 1e3,
+            "airfoil_time_to_cl_1e-6_s_extrapolated": t_it * 35000,
+            "airfoil_note": "128x128 quad O-mesh, CFL 1.5: 35,000 iterations to C_L within 1e-6 (the FP64 GPU "
+                            "path's count, bit-identical arithmetic) x the measured time per iteration"}
 
 
 def run_reference(args):

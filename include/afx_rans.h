@@ -178,6 +178,14 @@ int afx_residual_noalloc(afx_solver s, const double* q_dev, double* R_dev, long 
  * 1/max(0.1 sqrt(A_j), d), normalised.  Both solvers on the same device. */
 int afx_prolongate(afx_solver coarse, afx_solver fine);
 
+/* mesh::compute_wall_dist (mesh.h:794-830) on the GPU with the solver's
+ * boundary conditions: for every cell (real then ghost, reference order) the
+ * least distance from its centroid to the centre of a wall or slip-wall
+ * boundary edge; 1 when the mesh has none.  n = n_real_cells +
+ * n_boundary_edges.  (The reference computes it for its Spalart-Allmaras
+ * model, which it does not implement.) */
+int afx_wall_distance(afx_solver s, double* out, long long n);
+
 /* Implicit solver (settings solver = "implicit"): Krylov (GMRES)
  * iterations of the last implicit iteration, over its first solve and its
  * rhs_iterations chord solves (solver.h:1170-1213).  0 for the explicit

@@ -52,6 +52,9 @@ def lib():
         L.orc_set_farfield.argtypes = [vp, cp, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double]
         L.orc_set_q.argtypes = [vp, vp]
         L.orc_prolongate.argtypes = [vp, vp]
+        L.orc_set_threads.argtypes = [ip]
+        L.orc_wall_distance.restype = ctypes.c_longlong
+        L.orc_wall_distance.argtypes = [vp, vp]
         L.orc_get.restype = ctypes.c_longlong
         L.orc_get.argtypes = [vp, cp, vp]
         L.orc_residual.argtypes = [vp, vp]
@@ -185,6 +188,13 @@ class Solver:
         if lib().orc_set_farfield(self.h, patch.encode(), mach, angle, T, p):
             raise RuntimeError(lib().orc_last_error().decode())
 
+    def wall_distance(self):
+        """mesh::compute_wall_dist (mesh.h:794-830), all cells."""
+        n = lib().orc_wall_distance(self.h, None)
+        out = np.empty(n, np.float64)
+        lib().orc_wall_distance(self.h, _ptr(out))
+        return out
+
     def prolongate_from(self, coarse):
         """Grid-sequencing transfer (multigrid.h:99-178, 295-363): this
         solver's state from the coarse solver's."""
@@ -242,3 +252,8 @@ class Solver:
 
     def time_residuals(self, n):
         return lib().orc_time_residuals(self.h, n)
+
+
+def set_threads(n):
+    """OpenMP threads of the oracle's per-cell loops (0: all host threads)."""
+    lib().orc_set_threads(int(n))

@@ -3,6 +3,7 @@
 // restatement through ctypes.  Errors are reported by a null handle or a
 // non-zero return and a message in orc_last_error().
 #include <chrono>
+#include <omp.h>
 #include <cstring>
 #include <string>
 
@@ -203,7 +204,21 @@ int orc_set_farfield(void* sp, const char* patch, double mach, double angle, dou
     }
 }
 
+// OpenMP threads of the restated per-cell loops (the reference's own loops
+// are OpenMP-parallel the same way); 0 or less: all host threads.
+void orc_set_threads(int n) { omp_set_num_threads(n > 0 ? n : omp_get_num_procs()); }
+
 void orc_prolongate(void* coarse, void* fine) { prolongate(*(ExplicitSolver*)coarse, *(ExplicitSolver*)fine); }
+
+// mesh::compute_wall_dist (mesh.h:794-830) with the solver's boundary
+// conditions, as multigrid's constructor calls it (multigrid.h:72); all
+// cells, ghosts included.
+long long orc_wall_distance(void* sp, double* out) {
+    auto* s = (ExplicitSolver*)sp;
+    s->m.compute_wall_dist(s->st.bcs);
+    if (out) std::memcpy(out, s->m.wall_dist.data(), s->m.wall_dist.size() * sizeof(double));
+    return (long long)s->m.wall_dist.size();
+}
 
 void orc_set_q(void* sp, const double* q_real) {
     auto* s = (ExplicitSolver*)sp;

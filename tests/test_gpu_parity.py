@@ -264,3 +264,15 @@ def test_prolongate_bitexact(afx, orc):
     of.iterate(3)
     gf.iterate(3)
     np.testing.assert_array_equal(gf.get_q(), of.q())
+
+
+@pytest.mark.parametrize("case", ["omesh", "channel"])
+def test_wall_distance_bitexact(afx, orc, case):
+    # mesh::compute_wall_dist (mesh.h:794-830), ghosts included
+    if case == "omesh":
+        m, bcs = omesh_case(48, 24)
+    else:
+        m, bcs, _ = channel_case(64, 32)
+    so = oracle_solver(orc, m, bcs)
+    g = gpu_solver(afx, m, bcs)
+    np.testing.assert_array_equal(g.wall_distance(), so.wall_distance())
