@@ -15,9 +15,10 @@
 //     K for row c0 and -J for row c1), never a general sparse matrix;
 //   * face Jacobians by the reference's one-sided differences
 //     (physics.h:533-578: step max(1e-6, 1e-6 |q|)), one thread per face;
-//   * preconditioner: one symmetric multicolour block Gauss-Seidel sweep
-//     (cells coloured so no two neighbours share a colour; forward then
-//     backward over the colours), a fixed linear operator, so right
+//   * preconditioner: block ILU(0) in a multicolour ordering (cells
+//     coloured so no two neighbours share a colour; the factor's diagonal
+//     blocks formed colour by colour), applied as a forward then a backward
+//     sweep over the colours -- a fixed linear operator, so right
 //     preconditioned GMRES applies unchanged;
 //   * Krylov vectors and matrix blocks in T = double (FP64 path) or float
 //     (FP32-mixed path: the right-hand side, the update and the norms stay
@@ -218,6 +219,105 @@ __global__ void __launch_bounds__(128) k_imp_diag(const KM<double> m, const doub
     T* Io = dinv + 16 * (size_t)i;
 #pragma unroll
     for (int k = 0; k < 16; ++k) Io[k] = (T)I[k];
+}
+
+// Block ILU(0) in the colour ordering: for the cells of colour c,
+//     D~_i = D_i - sum_{neighbours o of a lower colour} O_io D~_o^-1 O_oi,
+// inverted into dinv (colour 0 keeps D^-1).  With these inverses the
+// symmetric multicolour Gauss-Seidel sweep below applies the ILU(0) factors
+// (D~ + L) D~^-1 (D~ + U) exactly.
+__device__ __forceinline__ void inv4(const double* A, double* I, int* singular) {
+    double D[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+        D[k] = A[k];
+        I[k] = (k % 5 == 0) ? 1.0 : 0.0;
+    }
+    for (int c = 0; c < 4; ++c) {
+        int p = c;
+        double best = fabs(D[4 * c + c]);
+        for (int r = c + 1; r < 4; ++r)
+            if (fabs(D[4 * r + c]) > best) {
+                best = fabs(D[4 * r + c]);
+                p = r;
+            }
+        if (!(best > 0)) {
+            *singular = 1;
+            return;
+        }
+        if (p != c)
+            for (int k = 0; k < 4; ++k) {
+                double t = D[4 * c + k];
+                D[4 * c + k] = D[4 * p + k];
+                D[4 * p + k] = t;
+                t = I[4 * c + k];
+                I[4 * c + k] = I[4 * p + k];
+                I[4 * p + k] = t;
+            }
+        const double inv = 1.0 / D[4 * c + c];
+        for (int k = 0; k < 4; ++k) {
+            D[4 * c + k] *= inv;
+            I[4 * c + k] *= inv;
+        }
+        for (int r = 0; r < 4; ++r) {
+            if (r == c) continue;
+            const double fct = D[4 * r + c];
+            for (int k = 0; k < 4; ++k) {
+                D[4 * r + k] -= fct * D[4 * c + k];
+                I[4 * r + k] -= fct * I[4 * c + k];
+            }
+        }
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(128) k_imp_ilu(const KM<double> m, const T* __restrict__ jf,
+                                                 const T* __restrict__ dblk, const int* __restrict__ cells,
+                                                 const int n, const int color, const unsigned char* __restrict__ col,
+                                                 T* __restrict__ dinv, int* __restrict__ singular) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int i = __ldg(&cells[t]);
+    double D[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) D[k] = (double)dblk[16 * (size_t)i + k];
+    const int4 sl = __ldg(&m.cslot[i]);
+    const int4 nb = __ldg(&m.cnbr[i]);
+#pragma unroll 1
+    for (int s = 0; s < 4; ++s) {
+        const int fs = pick(sl, s);
+        const int o = pick(nb, s);
+        if (fs == 0 || o < 0 || (int)__ldg(&col[o]) >= color) continue;
+        const int f = (fs > 0 ? fs : -fs) - 1;
+        const T* J = jf + 32 * (size_t)f;
+        const T* Oio = J + (fs > 0 ? 16 : 0);  // row i, column o
+        const T* Ooi = J + (fs > 0 ? 0 : 16);  // row o, column i
+        const double sio = fs > 0 ? 1.0 : -1.0, soi = -sio;
+        const T* Dinv_o = dinv + 16 * (size_t)o;
+        double Y[16];  // D~_o^-1 O_oi
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                double acc = 0;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) acc += (double)Dinv_o[4 * r + k] * (double)Ooi[4 * k + c];
+                Y[4 * r + c] = soi * acc;
+            }
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                double acc = 0;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) acc += (double)Oio[4 * r + k] * Y[4 * k + c];
+                D[4 * r + c] -= sio * acc;
+            }
+    }
+    double I[16];
+    inv4(D, I, singular);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) dinv[16 * (size_t)i + k] = (T)I[k];
 }
 
 // --------------------------------------------------------- linear algebra
@@ -535,6 +635,7 @@ struct ImplicitEngine {
     void* dblk = nullptr;
     void* dinv = nullptr;
     int* color_cells = nullptr;
+    unsigned char* color_of = nullptr;  // colour of each cell
     int* singular = nullptr;
     void* V = nullptr;     // (GM_M+1) x 4N
     void* w = nullptr;     // 4N
@@ -591,6 +692,13 @@ ImplicitEngine* implicit_create(const StepArgs& a, bool f32, const std::vector<i
     chk(cudaMalloc((void**)&e->ctl, sizeof(dev::GmresCtl)));
     chk(cudaHostAlloc((void**)&e->h_ctl, sizeof(dev::GmresCtl), cudaHostAllocDefault));
     chk(cudaMemcpyAsync(e->color_cells, cells.data(), cells.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    {
+        if (nc > 255) throw Error(7, "implicit solver: too many colours");
+        std::vector<unsigned char> col(colors.begin(), colors.end());
+        chk(cudaMalloc((void**)&e->color_of, std::max<size_t>(col.size(), 1)));
+        chk(cudaMemcpyAsync(e->color_of, col.data(), col.size(), cudaMemcpyHostToDevice, s));
+        chk(cudaStreamSynchronize(s));
+    }
     chk(cudaMemsetAsync(e->jf, 0, (size_t)e->F * 32 * T, s));
     chk(cudaStreamSynchronize(s));
     return e;
@@ -602,6 +710,7 @@ void implicit_destroy(ImplicitEngine* e) {
         if (e->cyc[k]) cudaGraphExecDestroy(e->cyc[k]);
     if (e->s2) cudaStreamDestroy(e->s2);
     if (e->s3) cudaStreamDestroy(e->s3);
+    if (e->color_of) cudaFree(e->color_of);
     for (void* p : {e->jf, e->dblk, e->dinv, (void*)e->color_cells, (void*)e->singular, e->V, e->w, e->z, e->t,
                     (void*)e->x, (void*)e->part, (void*)e->small, (void*)e->ctl, (void*)e->counter})
         if (p) cudaFree(p);
@@ -631,6 +740,13 @@ void implicit_fill(ImplicitEngine* e, const StepArgs& a0, int p, cudaStream_t s)
                                                    a.ctrl);
         k_imp_diag<float><<<nc, 128, 0, s>>>(m, (const double*)a.dt, (const float*)e->jf, (float*)e->dblk,
                                              (float*)e->dinv, e->singular, a.ctrl);
+        for (int c = 1; c < e->n_colors; ++c) {
+            const int c0 = e->color_ptr[c], cn = e->color_ptr[c + 1] - c0;
+            if (cn > 0)
+                k_imp_ilu<float><<<nb_(cn, 128), 128, 0, s>>>(m, (const float*)e->jf, (const float*)e->dblk,
+                                                              e->color_cells + c0, cn, c, e->color_of,
+                                                              (float*)e->dinv, e->singular);
+        }
     } else {
         if (a.visc == 1)
             k_imp_jac<double, 1><<<nf, 128, 0, s>>>(m, a.n_faces, q, (const d4*)a.gx, (const d4*)a.gy,
@@ -640,6 +756,13 @@ void implicit_fill(ImplicitEngine* e, const StepArgs& a0, int p, cudaStream_t s)
                                                     (double*)e->jf, a.ctrl);
         k_imp_diag<double><<<nc, 128, 0, s>>>(m, (const double*)a.dt, (const double*)e->jf, (double*)e->dblk,
                                               (double*)e->dinv, e->singular, a.ctrl);
+        for (int c = 1; c < e->n_colors; ++c) {
+            const int c0 = e->color_ptr[c], cn = e->color_ptr[c + 1] - c0;
+            if (cn > 0)
+                k_imp_ilu<double><<<nb_(cn, 128), 128, 0, s>>>(m, (const double*)e->jf, (const double*)e->dblk,
+                                                               e->color_cells + c0, cn, c, e->color_of,
+                                                               (double*)e->dinv, e->singular);
+        }
     }
 }
 
