@@ -171,6 +171,18 @@ def run_lean(args):
     marr = meshgen.channel(args.nx, args.ny, jitter=0.2, seed=1, shuffle_seed=2)
     q0 = meshgen.density_bump_state(marr, mach=MACH)
     m = rans.mesh.from_arrays(marr)
+    if args.adjoint:
+        # transpose-Jacobian products of the FP64 residual (afx_residual_vjp)
+        g = _setup_gpu("fp64", m, q0, "face", args.block)
+        v = np.random.default_rng(1).standard_normal(4 * m.nRealCells)
+        for _ in range(args.warmup):
+            g.residual_vjp(v)
+        t = time.perf_counter()
+        for _ in range(args.steps):
+            g.residual_vjp(v)
+        print(json.dumps({"adjoint_vjp": True, "cells": m.nRealCells, "steps": args.steps,
+                          "ms_per_vjp_host": (time.perf_counter() - t) / args.steps * 1e3}))
+        return
     for precision in args.precision.split(","):
         g = _setup_gpu(precision, m, q0, args.variant, args.block)
         g.iterate(args.warmup)
@@ -560,6 +572,7 @@ def main():
     ap.add_argument("--precision", default="fp32-mixed", help="--lean: comma-separated precisions")
     ap.add_argument("--variant", default="auto", help="--lean: residual kernel variant (auto|gather|face|tile)")
     ap.add_argument("--block", type=int, default=0, help="--lean: threads per block (0: the library's default)")
+    ap.add_argument("--adjoint", action="store_true", help="--lean: FP64 residual vJP calls instead of iterations")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank = int(os.environ.get("RANK", "0"))
