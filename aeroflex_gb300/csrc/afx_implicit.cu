@@ -58,24 +58,25 @@ template <class T> struct B4;
 template <> struct B4<double> { using type = d4; };
 template <> struct B4<float> { using type = float4; };
 
-__device__ __forceinline__ void ldb(const d4* p, double* v) { ld4(p, v); }
-__device__ __forceinline__ void ldb(const float4* p, double* v) {
+// Krylov-side vectors in their own precision T: FP32 arithmetic stays in the
+// FP32 pipes (a float-to-double conversion per operand would run on GB300's
+// FP64 pipe, at ~1/64 of the FP32 rate)
+__device__ __forceinline__ void ldt(const d4* p, double* v) { ld4(p, v); }
+__device__ __forceinline__ void ldt(const float4* p, float* v) {
     const float4 a = *p;
     v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
 }
-__device__ __forceinline__ void stb(d4* p, const double* v) { st4(p, v); }
-__device__ __forceinline__ void stb(float4* p, const double* v) {
-    *p = make_float4((float)v[0], (float)v[1], (float)v[2], (float)v[3]);
-}
+__device__ __forceinline__ void stt(d4* p, const double* v) { st4(p, v); }
+__device__ __forceinline__ void stt(float4* p, const float* v) { *p = make_float4(v[0], v[1], v[2], v[3]); }
 
-// 4x4 block (row-major, T) times a 4-vector, accumulated in double
+// y += sgn * B x for a 4x4 block (row-major) in T
 template <class T>
-__device__ __forceinline__ void bmv_add(const T* __restrict__ B, const double* x, double* y, const double sgn) {
+__device__ __forceinline__ void bmv_add(const T* __restrict__ B, const T* x, T* y, const T sgn) {
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-        double s = 0;
+        T s = 0;
 #pragma unroll
-        for (int c = 0; c < 4; ++c) s += (double)B[4 * r + c] * x[c];
+        for (int c = 0; c < 4; ++c) s += B[4 * r + c] * x[c];
         y[r] += sgn * s;
     }
 }
@@ -329,9 +330,9 @@ __global__ void __launch_bounds__(256) k_imp_spmv(const KM<double> m, const T* _
     if (stop && *stop) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m.n_cells) return;
-    double xi[4], yi[4] = {0, 0, 0, 0};
-    ldb(&x[i], xi);
-    bmv_add(dblk + 16 * (size_t)i, xi, yi, 1.0);
+    T xi[4], yi[4] = {0, 0, 0, 0};
+    ldt(&x[i], xi);
+    bmv_add<T>(dblk + 16 * (size_t)i, xi, yi, T(1));
     const int4 sl = __ldg(&m.cslot[i]);
     const int4 nb = __ldg(&m.cnbr[i]);
 #pragma unroll
@@ -340,12 +341,12 @@ __global__ void __launch_bounds__(256) k_imp_spmv(const KM<double> m, const T* _
         const int o = pick(nb, s);
         if (fs == 0 || o < 0) continue;
         const int f = (fs > 0 ? fs : -fs) - 1;
-        double xo[4];
-        ldb(&x[o], xo);
+        T xo[4];
+        ldt(&x[o], xo);
         // row c0: K x_c1; row c1: -J x_c0
-        bmv_add(jf + 32 * (size_t)f + (fs > 0 ? 16 : 0), xo, yi, fs > 0 ? 1.0 : -1.0);
+        bmv_add<T>(jf + 32 * (size_t)f + (fs > 0 ? 16 : 0), xo, yi, fs > 0 ? T(1) : T(-1));
     }
-    stb(&y[i], yi);
+    stt(&y[i], yi);
 }
 
 // One colour of a block Gauss-Seidel sweep: x_i = D_i^-1 (r_i - sum O x_n).
@@ -362,8 +363,8 @@ __global__ void __launch_bounds__(256) k_imp_gs(const KM<double> m, const T* __r
     const typename B4<T>::type* r =
         reinterpret_cast<const typename B4<T>::type*>(rbase + (rk ? (long long)*rk * stride : 0));
     const int i = __ldg(&cells[t]);
-    double s[4];
-    ldb(&r[i], s);
+    T s[4];
+    ldt(&r[i], s);
     const int4 sl = __ldg(&m.cslot[i]);
     const int4 nb = __ldg(&m.cnbr[i]);
 #pragma unroll
@@ -372,13 +373,13 @@ __global__ void __launch_bounds__(256) k_imp_gs(const KM<double> m, const T* __r
         const int o = pick(nb, k);
         if (fs == 0 || o < 0) continue;
         const int f = (fs > 0 ? fs : -fs) - 1;
-        double xo[4];
-        ldb(&x[o], xo);
-        bmv_add(jf + 32 * (size_t)f + (fs > 0 ? 16 : 0), xo, s, fs > 0 ? -1.0 : 1.0);
+        T xo[4];
+        ldt(&x[o], xo);
+        bmv_add<T>(jf + 32 * (size_t)f + (fs > 0 ? 16 : 0), xo, s, fs > 0 ? T(-1) : T(1));
     }
-    double xi[4] = {0, 0, 0, 0};
-    bmv_add(dinv + 16 * (size_t)i, s, xi, 1.0);
-    stb(&x[i], xi);
+    T xi[4] = {0, 0, 0, 0};
+    bmv_add<T>(dinv + 16 * (size_t)i, s, xi, T(1));
+    stt(&x[i], xi);
 }
 
 template <class T>
@@ -402,20 +403,21 @@ __global__ void __launch_bounds__(DOT_THREADS) k_imp_dots(const int n, int nv, c
     if (stop && *stop) return;
     if (nvk) nv = *nvk + 1;  // v_0 .. v_k of the current Arnoldi step
     // one pass over w and the nv vectors, nv accumulators per thread
-    double acc[GM_M + 1];
+    // per-thread partial sums in T (a few elements each), then double
+    T acc[GM_M + 1];
 #pragma unroll
     for (int j = 0; j <= GM_M; ++j) acc[j] = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const double wi = (double)w[i];
+        const T wi = w[i];
 #pragma unroll
         for (int j = 0; j <= GM_M; ++j)
-            if (j < nv) acc[j] += (double)V[(size_t)j * n + i] * wi;
+            if (j < nv) acc[j] += V[(size_t)j * n + i] * wi;
     }
     const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
 #pragma unroll
     for (int j = 0; j <= GM_M; ++j) {
         if (j >= nv) break;
-        double v = acc[j];
+        double v = (double)acc[j];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
         if (lane == 0) sh[wp][j] = v;
@@ -448,13 +450,16 @@ template <class T>
 __global__ void __launch_bounds__(256) k_imp_orth(const int n, int nv, const int* __restrict__ nvk,
                                                   const T* __restrict__ V, const double* __restrict__ h,
                                                   T* __restrict__ w, const int* __restrict__ stop) {
+    __shared__ T hs[GM_M + 1];
     if (stop && *stop) return;
     if (nvk) nv = *nvk + 1;
+    if ((int)threadIdx.x < nv) hs[threadIdx.x] = (T)h[threadIdx.x];
+    __syncthreads();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    double s = (double)w[i];
-    for (int j = 0; j < nv; ++j) s -= h[j] * (double)V[(size_t)j * n + i];
-    w[i] = (T)s;
+    T s = w[i];
+    for (int j = 0; j < nv; ++j) s -= hs[j] * V[(size_t)j * n + i];
+    w[i] = s;
 }
 
 // v = w * scale[0] (scale read from the device)
@@ -466,7 +471,8 @@ __global__ void __launch_bounds__(256) k_imp_scale(const int n, const T* __restr
     if (stop && *stop) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (vk) v += (long long)*vk * n;
-    if (i < n) v[i] = (T)((double)w[i] * scale[0]);
+    const T sc = (T)scale[0];
+    if (i < n) v[i] = w[i] * sc;
 }
 
 // Arnoldi step j = c->k, classical Gram-Schmidt twice: h1 (first pass) and
@@ -548,11 +554,15 @@ __global__ void __launch_bounds__(32) k_imp_solve_y(GmresCtl* c) {
 template <class T>
 __global__ void __launch_bounds__(256) k_imp_lincomb(const int n, const T* __restrict__ V, const GmresCtl* __restrict__ c,
                                                      T* __restrict__ t) {
+    __shared__ T ys[GM_M];
+    const int k = c->k;
+    if ((int)threadIdx.x < k) ys[threadIdx.x] = (T)c->y[threadIdx.x];
+    __syncthreads();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    double s = 0;
-    for (int j = 0; j < c->k; ++j) s += c->y[j] * (double)V[(size_t)j * n + i];
-    t[i] = (T)s;
+    T s = 0;
+    for (int j = 0; j < k; ++j) s += ys[j] * V[(size_t)j * n + i];
+    t[i] = s;
 }
 
 // x (double) += z;  r = b - y  (b double), both 4N long
