@@ -692,7 +692,7 @@ struct TileView {
 };
 
 template <class T, class S, int VISC, bool SECOND, bool EIG>
-__global__ void __launch_bounds__(256) k_resid_tile(const KM<T> m, const TileView tv, const V4<S>* __restrict__ qk,
+__global__ void __launch_bounds__(256, 8) k_resid_tile(const KM<T> m, const TileView tv, const V4<S>* __restrict__ qk,
                                                     const V4<S>* __restrict__ qmem, const V4<T>* __restrict__ gx,
                                                     const V4<T>* __restrict__ gy, const V4<T>* __restrict__ phi,
                                                     const StageOut<T, S> o, const Ctrl* __restrict__ ctrl) {
