@@ -766,6 +766,15 @@ int afx_mesh_boundary_name(afx_mesh mp, int b, char* out, int cap) {
     });
 }
 
+int afx_mesh_set_nodes(afx_mesh mp, const double* x, const double* y, long long n) {
+    return guarded([&] {
+        if (!mp || !x || !y) throw Error(AFX_ERR_ARG, "null argument");
+        if (n != (long long)mp->m.nodesX.size()) throw Error(AFX_ERR_ARG, "node count mismatch");
+        mp->m.update_nodes(x, y);
+        if (mp->has_layout) fill_layout_geometry(mp->m, mp->L);
+    });
+}
+
 void afx_mesh_free(afx_mesh m) { delete m; }
 
 // ---------------------------------------------------------------- config

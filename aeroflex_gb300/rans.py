@@ -32,7 +32,7 @@ ABI_SYMBOLS = [
     "afx_batch_case_history", "afx_batch_forces", "afx_batch_set_farfield", "afx_batch_autotune",
     "afx_batch_last_device_seconds", "afx_residual_vjp", "afx_boundary_states", "afx_adjoint_solve",
     "afx_adjoint_state", "afx_linear_iterations", "afx_prolongate", "afx_patch_nodes", "afx_deform_patch",
-    "afx_adjoint_patch", "afx_wall_distance",
+    "afx_adjoint_patch", "afx_wall_distance", "afx_mesh_set_nodes",
 ]
 N_KERNEL_KINDS = 7
 
@@ -117,6 +117,7 @@ def lib():
         "afx_deform_patch": (i, [vp, cp, vp, i, d]),
         "afx_adjoint_patch": (i, [vp, cp, cp, d, d, vp, i]),
         "afx_wall_distance": (i, [vp, vp, ll]),
+        "afx_mesh_set_nodes": (i, [vp, vp, vp, ll]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -173,6 +174,12 @@ class mesh:
         out = np.empty(n.value, np.int64)
         _check(lib().afx_mesh_get_int(self.h, what.encode(), _ptr(out), n.value, ctypes.byref(n)))
         return out
+
+    def set_nodes(self, x, y):
+        """New node coordinates, same topology: metrics re-formed."""
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.ascontiguousarray(y, np.float64)
+        _check(lib().afx_mesh_set_nodes(self.h, _ptr(x), _ptr(y), x.size))
 
     def boundary_names(self):
         buf = ctypes.create_string_buffer(256)

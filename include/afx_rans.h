@@ -67,6 +67,11 @@ int afx_mesh_get(afx_mesh m, const char* what, double* out, long long cap, long 
 int afx_mesh_get_int(afx_mesh m, const char* what, long long* out, long long cap, long long* n);
 /* Physical name of boundary edge b (mesh.h:783-785). */
 int afx_mesh_boundary_name(afx_mesh m, int b, char* out, int cap);
+/* New node coordinates for the same topology (a deformed shape): the
+ * metrics and ghost cells are re-formed with the formulas of mesh.h:378-453,
+ * 744-787.  Solvers created afterwards see the new geometry; a solver
+ * deforms its own copy with afx_deform_patch.  n = number of nodes. */
+int afx_mesh_set_nodes(afx_mesh m, const double* x, const double* y, long long n);
 void afx_mesh_free(afx_mesh m);
 
 /* ----------------------------------------------------------- config ---- */

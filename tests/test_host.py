@@ -186,3 +186,29 @@ def test_batch_checks_schemes_then_fails_loudly_without_gpu(afx):
     with pytest.raises(afx.AfxError) as e:
         afx.Batch(meshes, [afx.Settings(), afx.Settings()])
     assert e.value.code == 7
+
+
+def test_mesh_set_nodes_matches_a_fresh_mesh(afx):
+    # deformed coordinates on an existing mesh give exactly the metrics of a
+    # mesh built from the deformed coordinates
+    m0 = meshgen.airfoil_omesh(24, 12, split=False, m=0.02)
+    rng = np.random.default_rng(7)
+    x = m0["x"] * (1 + 1e-3 * rng.standard_normal(m0["x"].size))
+    y = m0["y"] * (1 + 1e-3 * rng.standard_normal(m0["y"].size))
+    a = afx.mesh.from_arrays(m0)
+    a.set_nodes(x, y)
+    b = afx.mesh.from_arrays(dict(m0, x=x, y=y))
+    for what in ("cx", "cy", "area", "ex", "ey", "nx", "ny", "L"):
+        np.testing.assert_array_equal(a.get(what), b.get(what), err_msg=what)
+    with pytest.raises(afx.AfxError):
+        a.set_nodes(x[:-1], y[:-1])
+
+
+def test_polar_sweep_meshes_do_not_fold():
+    # every cell of the 256 polar-sweep O-meshes keeps the orientation of
+    # the mesh (no folded cell near the far field)
+    for c in meshgen.polar_sweep_cases(256, seed=4):
+        m = c["mesh"]
+        X, Y = m["x"][m["cells"]], m["y"][m["cells"]]
+        sa = 0.5 * sum(X[:, k] * Y[:, (k + 1) % 4] - X[:, (k + 1) % 4] * Y[:, k] for k in range(4))
+        assert (sa < 0).all() or (sa > 0).all(), (c["n_cells"], int((sa > 0).sum()))
