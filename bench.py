@@ -171,6 +171,20 @@ def run_lean(args):
     marr = meshgen.channel(args.nx, args.ny, jitter=0.2, seed=1, shuffle_seed=2)
     q0 = meshgen.density_bump_state(marr, mach=MACH)
     m = rans.mesh.from_arrays(marr)
+    if args.implicit:
+        # two implicit iterations on the 128 x 128 airfoil O-mesh from freestream, CFL 40
+        am = rans.mesh.from_arrays(meshgen.airfoil_omesh(128, 128, split=False))
+        for precision in args.precision.split(","):
+            st = rans.Settings().set("solver", "implicit").set("precision", precision).set("start_cfl", 40.0)
+            st.set_bc("farfield", "farfield", 1.0, 0.5, 1.25 * 0.01745, 1.0).set_bc("wall", "slip-wall")
+            g = rans.Solver(am, st)
+            g.init()
+            g.iterate(args.steps)
+            print(json.dumps({"implicit": precision, "cells": am.nRealCells, "iterations": args.steps,
+                              "krylov_last_iteration": g.linear_iterations(),
+                              "device_s": g.last_device_seconds()}))
+            del g
+        return
     if args.adjoint:
         # transpose-Jacobian products of the FP64 residual (afx_residual_vjp)
         g = _setup_gpu("fp64", m, q0, "face", args.block)
@@ -573,6 +587,8 @@ def main():
     ap.add_argument("--variant", default="auto", help="--lean: residual kernel variant (auto|gather|face|tile)")
     ap.add_argument("--block", type=int, default=0, help="--lean: threads per block (0: the library's default)")
     ap.add_argument("--adjoint", action="store_true", help="--lean: FP64 residual vJP calls instead of iterations")
+    ap.add_argument("--implicit", action="store_true",
+                    help="--lean: implicit iterations on the 128x128 airfoil O-mesh (--steps of them)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank = int(os.environ.get("RANK", "0"))
