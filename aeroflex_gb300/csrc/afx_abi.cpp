@@ -407,6 +407,13 @@ struct afx_solver_s {
         StepArgs r = A64();
         r.Rq = imp_b;
         enqueue_rhs_f64(r, p, stream);
+        if (r.n_cases > 0) {
+            // a batch stops a case whose right-hand side is not finite; the
+            // norm below is not used by the batch loop
+            r.ctrl = a.ctrl;
+            enqueue_case_nonfinite(r, imp_b, stream);
+            return 0.0;
+        }
         const int nb = (r.n_cells + r.block - 1) / r.block;
         std::vector<double> parts(nb);
         AFX_CUDA(cudaMemcpyAsync(parts.data(), r.partials, nb * 8, cudaMemcpyDeviceToHost, stream));
@@ -422,6 +429,7 @@ struct afx_solver_s {
     double implicit_iteration(double cfl, double tol_abs) {
         StepArgs m = A64();
         m.cfl = cfl;
+        if (a.n_cases > 0) m.ctrl = a.ctrl;  // a case stopped during the fill is counted on the run's control block
         implicit_fill(imp, m, parity, stream);
         imp_lin_iters = 0;
         auto solve_update = [&]() {
@@ -430,16 +438,21 @@ struct afx_solver_s {
             imp_lin_iters += it;
             return true;
         };
+        const bool batch = a.n_cases > 0;  // per-case control instead of the global early exits
         double err = imp_rhs(parity);
-        if (!(err == err)) return err;
-        if (err < tol_abs) return err;
+        if (!batch) {
+            if (!(err == err)) return err;
+            if (err < tol_abs) return err;
+        }
         const double err_ini = err;
         if (!solve_update()) return -1;
         for (int i = 0; i < st.rhs_iterations; ++i) {
             err = imp_rhs(parity);
-            if (!(err == err)) return err;
-            if (err < tol_abs) return err;
-            if (err > 10 * err_ini) return err;
+            if (!batch) {
+                if (!(err == err)) return err;
+                if (err < tol_abs) return err;
+                if (err > 10 * err_ini) return err;
+            }
             if (!solve_update()) return -1;
         }
         return imp_rhs(parity);

@@ -81,6 +81,25 @@ __device__ __forceinline__ void bmv_add(const T* __restrict__ B, const T* x, T* 
     }
 }
 
+// Batch: a cell of a case that has stopped takes no part in the linear
+// solve (its rows and unknowns are zero), so a case that went non-finite
+// cannot spread into the others
+__device__ __forceinline__ bool held(const int* case_of, const int* case_done, const int i) {
+    return case_done && ((volatile const int*)case_done)[__ldg(&case_of[i])];
+}
+
+// A batch case whose diagonal block cannot be inverted stops (status 4)
+// instead of failing the whole batch; the first cell to find it stops it.
+__device__ __forceinline__ void stop_case(const int* case_of, int* case_done, CaseCtrl* cctrl, Ctrl* ctrl,
+                                          const int i) {
+    const int c = __ldg(&case_of[i]);
+    if (atomicCAS(&case_done[c], 0, 1) == 0) {
+        cctrl[c].status = 4;
+        cctrl[c].done = 1;
+        atomicAdd(&ctrl->ndone, 1);
+    }
+}
+
 // ------------------------------------------------------------- assembly
 // F of face f for the cell states (no reconstruction; the ghost side is the
 // stored boundary state), as the reference's flux functor evaluates it.
@@ -157,10 +176,19 @@ template <class T>
 __global__ void __launch_bounds__(128) k_imp_diag(const KM<double> m, const double* __restrict__ dt,
                                                   const T* __restrict__ jf, T* __restrict__ dblk,
                                                   T* __restrict__ dinv, int* __restrict__ singular,
-                                                  const Ctrl* __restrict__ ctrl) {
+                                                  Ctrl* __restrict__ ctrl, const int* __restrict__ case_of,
+                                                  int* __restrict__ case_done, CaseCtrl* __restrict__ cctrl) {
     if (ctrl->done) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m.n_cells) return;
+    if (held(case_of, case_done, i)) {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            dblk[16 * (size_t)i + k] = T((k % 5 == 0) ? 1 : 0);
+            dinv[16 * (size_t)i + k] = T((k % 5 == 0) ? 1 : 0);
+        }
+        return;
+    }
     double D[16];
     const double ad = __ldg(&m.area[i]) / __ldg(&dt[i]);
 #pragma unroll
@@ -191,7 +219,13 @@ __global__ void __launch_bounds__(128) k_imp_diag(const KM<double> m, const doub
                 p = r;
             }
         if (!(best > 0)) {
-            *singular = 1;
+            if (case_done) {
+                stop_case(case_of, case_done, cctrl, ctrl, i);
+#pragma unroll
+                for (int k = 0; k < 16; ++k) dinv[16 * (size_t)i + k] = T((k % 5 == 0) ? 1 : 0);
+            } else {
+                *singular = 1;
+            }
             return;
         }
         if (p != c)
@@ -275,10 +309,13 @@ template <class T>
 __global__ void __launch_bounds__(128) k_imp_ilu(const KM<double> m, const T* __restrict__ jf,
                                                  const T* __restrict__ dblk, const int* __restrict__ cells,
                                                  const int n, const int color, const unsigned char* __restrict__ col,
-                                                 T* __restrict__ dinv, int* __restrict__ singular) {
+                                                 T* __restrict__ dinv, int* __restrict__ singular,
+                                                 const int* __restrict__ case_of, int* __restrict__ case_done,
+                                                 CaseCtrl* __restrict__ cctrl, Ctrl* __restrict__ ctrl) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     const int i = __ldg(&cells[t]);
+    if (held(case_of, case_done, i)) return;
     double D[16];
 #pragma unroll
     for (int k = 0; k < 16; ++k) D[k] = (double)dblk[16 * (size_t)i + k];
@@ -316,7 +353,16 @@ __global__ void __launch_bounds__(128) k_imp_ilu(const KM<double> m, const T* __
             }
     }
     double I[16];
-    inv4(D, I, singular);
+    int sing = 0;
+    inv4(D, I, &sing);
+    if (sing) {
+        if (case_done) {
+            stop_case(case_of, case_done, cctrl, ctrl, i);
+        } else {
+            *singular = 1;
+        }
+        return;
+    }
 #pragma unroll
     for (int k = 0; k < 16; ++k) dinv[16 * (size_t)i + k] = (T)I[k];
 }
@@ -326,10 +372,16 @@ __global__ void __launch_bounds__(128) k_imp_ilu(const KM<double> m, const T* __
 template <class T>
 __global__ void __launch_bounds__(256) k_imp_spmv(const KM<double> m, const T* __restrict__ jf,
                                                   const T* __restrict__ dblk, const typename B4<T>::type* __restrict__ x,
-                                                  typename B4<T>::type* __restrict__ y, const int* __restrict__ stop) {
+                                                  typename B4<T>::type* __restrict__ y, const int* __restrict__ stop,
+                                                  const int* __restrict__ case_of, const int* __restrict__ case_done) {
     if (stop && *stop) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m.n_cells) return;
+    if (held(case_of, case_done, i)) {
+        const T z[4] = {0, 0, 0, 0};
+        stt(&y[i], z);
+        return;
+    }
     T xi[4], yi[4] = {0, 0, 0, 0};
     ldt(&x[i], xi);
     bmv_add<T>(dblk + 16 * (size_t)i, xi, yi, T(1));
@@ -356,13 +408,19 @@ __global__ void __launch_bounds__(256) k_imp_gs(const KM<double> m, const T* __r
                                                 const T* __restrict__ dinv, const int* __restrict__ cells,
                                                 const int n, const T* __restrict__ rbase, const int* __restrict__ rk,
                                                 const long long stride, typename B4<T>::type* __restrict__ x,
-                                                const int* __restrict__ stop) {
+                                                const int* __restrict__ stop, const int* __restrict__ case_of,
+                                                const int* __restrict__ case_done) {
     if (stop && *stop) return;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     const typename B4<T>::type* r =
         reinterpret_cast<const typename B4<T>::type*>(rbase + (rk ? (long long)*rk * stride : 0));
     const int i = __ldg(&cells[t]);
+    if (held(case_of, case_done, i)) {
+        const T z[4] = {0, 0, 0, 0};
+        stt(&x[i], z);
+        return;
+    }
     T s[4];
     ldt(&r[i], s);
     const int4 sl = __ldg(&m.cslot[i]);
@@ -749,13 +807,15 @@ void implicit_fill(ImplicitEngine* e, const StepArgs& a0, int p, cudaStream_t s)
             k_imp_jac<float, 0><<<nf, 128, 0, s>>>(m, a.n_faces, q, (const d4*)a.gx, (const d4*)a.gy, (float*)e->jf,
                                                    a.ctrl);
         k_imp_diag<float><<<nc, 128, 0, s>>>(m, (const double*)a.dt, (const float*)e->jf, (float*)e->dblk,
-                                             (float*)e->dinv, e->singular, a.ctrl);
+                                             (float*)e->dinv, e->singular, a.ctrl, a.case_of, a.case_done,
+                                             a.cctrl);
         for (int c = 1; c < e->n_colors; ++c) {
             const int c0 = e->color_ptr[c], cn = e->color_ptr[c + 1] - c0;
             if (cn > 0)
                 k_imp_ilu<float><<<nb_(cn, 128), 128, 0, s>>>(m, (const float*)e->jf, (const float*)e->dblk,
                                                               e->color_cells + c0, cn, c, e->color_of,
-                                                              (float*)e->dinv, e->singular);
+                                                              (float*)e->dinv, e->singular, a.case_of,
+                                                              a.case_done, a.cctrl, a.ctrl);
         }
     } else {
         if (a.visc == 1)
@@ -765,13 +825,15 @@ void implicit_fill(ImplicitEngine* e, const StepArgs& a0, int p, cudaStream_t s)
             k_imp_jac<double, 0><<<nf, 128, 0, s>>>(m, a.n_faces, q, (const d4*)a.gx, (const d4*)a.gy,
                                                     (double*)e->jf, a.ctrl);
         k_imp_diag<double><<<nc, 128, 0, s>>>(m, (const double*)a.dt, (const double*)e->jf, (double*)e->dblk,
-                                              (double*)e->dinv, e->singular, a.ctrl);
+                                              (double*)e->dinv, e->singular, a.ctrl, a.case_of,
+                                              a.case_done, a.cctrl);
         for (int c = 1; c < e->n_colors; ++c) {
             const int c0 = e->color_ptr[c], cn = e->color_ptr[c + 1] - c0;
             if (cn > 0)
                 k_imp_ilu<double><<<nb_(cn, 128), 128, 0, s>>>(m, (const double*)e->jf, (const double*)e->dblk,
                                                                e->color_cells + c0, cn, c, e->color_of,
-                                                               (double*)e->dinv, e->singular);
+                                                               (double*)e->dinv, e->singular, a.case_of,
+                                                               a.case_done, a.cctrl, a.ctrl);
         }
     }
 }
@@ -790,7 +852,7 @@ struct Ops {
     int* stop() const { return &e->ctl->stop; }
     void spmv(const T* x, T* y, const int* st) const {
         dev::k_imp_spmv<T><<<nb_(e->N, 256), 256, 0, s>>>(m, (const T*)e->jf, (const T*)e->dblk, (const V4*)x, (V4*)y,
-                                                          st);
+                                                          st, a.case_of, a.case_done);
     }
     // one symmetric multicolour block Gauss-Seidel sweep from x = 0; the
     // input is r, or the current Krylov vector V + k*n when rk is given
@@ -803,7 +865,7 @@ struct Ops {
                 if (cn == 0) continue;
                 dev::k_imp_gs<T><<<nb_(cn, 256), 256, 0, s>>>(m, (const T*)e->jf, (const T*)e->dinv,
                                                               e->color_cells + c0, cn, r, rk, (long long)e->n4,
-                                                              (V4*)x, st);
+                                                              (V4*)x, st, a.case_of, a.case_done);
             }
     }
     void dots(int nv, const int* nvk, const T* V, const T* w, double* out, const int* st) const {

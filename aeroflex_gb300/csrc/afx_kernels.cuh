@@ -939,6 +939,36 @@ static __global__ void __launch_bounds__(256) k_case_control(const double* __res
     }
 }
 
+// Implicit batches, right after a right-hand side: a case whose face sums
+// are not finite stops (status 4) and its right-hand-side rows are zeroed
+// before the linear solve, so it cannot spread into the other cases.
+static __global__ void __launch_bounds__(256) k_case_nonfinite(const double* __restrict__ cell_sq,
+                                                               const int* __restrict__ case_off, CaseCtrl* cctrl,
+                                                               int* case_done, Ctrl* ctrl, d4* __restrict__ b) {
+    __shared__ double sh[32];
+    __shared__ int bad;
+    const int c = blockIdx.x;
+    if (cctrl[c].done) return;
+    const int b0 = case_off[c], b1 = case_off[c + 1];
+    double v = 0;
+    for (int k = b0 + threadIdx.x; k < b1; k += blockDim.x) v += cell_sq[k];
+    const double t = block_sum(v, sh);
+    if (threadIdx.x == 0) {
+        bad = !(t == t) || t > 1.7976931348623157e308;
+        if (bad) {
+            cctrl[c].status = 4;
+            cctrl[c].done = 1;
+            case_done[c] = 1;
+            atomicAdd(&ctrl->ndone, 1);
+        }
+    }
+    __syncthreads();
+    if (bad) {
+        const double z[4] = {0, 0, 0, 0};
+        for (int k = b0 + threadIdx.x; k < b1; k += blockDim.x) st4(&b[k], z);
+    }
+}
+
 // After k_case_control: count the iteration and stop the run once every
 // case has stopped (a separate launch, so no block of k_case_control sees
 // the run's flag change under it).

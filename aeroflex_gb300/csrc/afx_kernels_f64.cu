@@ -10,6 +10,10 @@ namespace afx {
 void enqueue_iteration_f64(const StepArgs& a, int p, cudaStream_t s) { dev::iteration<double, double, false>(a, p, s); }
 void enqueue_residual_f64(const StepArgs& a, int p, cudaStream_t s) { dev::residual<double, double>(a, p, s); }
 void enqueue_rhs_f64(const StepArgs& a, int p, cudaStream_t s) { dev::rhs<double, double>(a, p, s); }
+void enqueue_case_nonfinite(const StepArgs& a, void* b, cudaStream_t s) {
+    dev::k_case_nonfinite<<<a.n_cases, 256, 0, s>>>(a.cell_sq, a.case_off, a.cctrl, a.case_done, a.ctrl,
+                                                    (dev::d4*)b);
+}
 void enqueue_case_control(const StepArgs& a, cudaStream_t s) {
     dev::k_case_control<<<a.n_cases, 256, 0, s>>>(a.cell_sq, a.case_off, a.cctrl, a.case_done, a.chist, a.ctrl,
                                                   a.n_cases, 0);

@@ -132,6 +132,8 @@ void enqueue_rhs_f64(const StepArgs& a, int p, cudaStream_t s);
 // Batch: per-case norms of cell_sq and run_solver control (k_case_control),
 // then the run's iteration count and stop flag.
 void enqueue_case_control(const StepArgs& a, cudaStream_t s);
+// Implicit batch: cases with a non-finite right-hand side b stop and get zero rows.
+void enqueue_case_nonfinite(const StepArgs& a, void* b, cudaStream_t s);
 // Re-form qW of the last RK stage of the iteration that read parity p.
 void enqueue_last_stage_residual_f64(const StepArgs& a, int p, cudaStream_t s);
 void enqueue_last_stage_residual_f32(const StepArgs& a, int p, cudaStream_t s);

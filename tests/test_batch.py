@@ -172,3 +172,31 @@ def test_batch_implicit_polar_converges_per_case(afx, precision):
         fb = b.forces(c, "wall")
         for k in ("cl", "cd"):
             assert abs(fb[k] - wg[k]) <= 1e-8 * max(abs(wg[k]), 1e-3), (c, k, fb[k], wg[k])
+
+
+def test_batch_implicit_isolates_a_failed_case(afx):
+    # a case whose state is not finite stops with status NONFINITE; the other
+    # cases of the implicit batch still reach their own fixed points
+    from aeroflex_gb300 import meshgen
+    imp = dict(solver="implicit", start_cfl=40.0, slope_cfl=50.0, max_cfl=100.0)
+    cases = []
+    for ns, nr, mach, aoa in [(32, 24, 0.5, 1.25), (24, 16, 0.4, 3.0), (40, 20, 0.3, -1.0)]:
+        m = meshgen.airfoil_omesh(ns, nr, split=False)
+        bcs = {"farfield": dict(type="farfield", T=1.0, mach=mach, angle=aoa * DEG, p=1.0),
+               "wall": dict(type="slip-wall")}
+        cases.append((m, bcs))
+    b = _batch(afx, cases, "fp32-mixed", **imp)
+    b.init()
+    q = b.get_q(1)
+    q[::4] = np.nan
+    b.set_q(1, q)
+    it, err, st = b.run_solver(1e-11, 300)
+    assert st[1] == 4 and st[0] == 0 and st[2] == 0, (it, err, st)
+    for c in (0, 2):
+        m, bcs = cases[c]
+        g = gpu_solver(afx, m, bcs, "fp64", **imp)
+        g.init()
+        g.run_solver(1e-11, 300)
+        wg = afx.get_wall_profile(g, "wall")
+        fb = b.forces(c, "wall")
+        assert abs(fb["cl"] - wg["cl"]) <= 1e-8 * max(abs(wg["cl"]), 1e-3), (c, fb, wg)
