@@ -280,7 +280,7 @@ struct afx_solver_s {
     std::unique_ptr<PatchDeform> pdef;
     AdjointBufs& adjoint() {
         if (!fp64) throw Error(AFX_ERR_CONFIG, "the adjoint needs an fp64 solver");
-        if (a.visc != 0) throw Error(AFX_ERR_CONFIG, "the adjoint covers the inviscid flux only");
+        if (a.visc > 1) throw Error(AFX_ERR_CONFIG, "the adjoint covers the inviscid and laminar fluxes");
         if (a.lsq) throw Error(AFX_ERR_CONFIG, "the adjoint covers the Green-Gauss gradient only");
         if (!adj) {
             const size_t N = a.n_cells, F = a.n_faces, B = std::max(a.n_bnd, 1);
@@ -288,7 +288,7 @@ struct afx_solver_s {
             for (DevBuf* d : {&b->v, &b->gbx, &b->gby, &b->qbar, &b->u, &b->g, &b->q, &b->lam[0], &b->lam[1],
                               &b->ls[0], &b->ls[1]})
                 d->alloc(N * 32);
-            b->fbar.alloc(F * 64);
+            b->fbar.alloc(F * (a.visc == 1 ? 256 : 64));
             b->lw.alloc(N * 64);
             b->lt.alloc(N * 32);
             b->bqbar.alloc(B * 32);

@@ -16,8 +16,10 @@
 //   k_adj_final  per cell: adds the limiter pairs that target it and the
 //                Green-Gauss gradient's reverse over its faces, and writes
 //                the boundary-state adjoint of its boundary faces.
-// Face Jacobians are never stored.  Inviscid flux only (Roe + entropy fix
-// with every boundary type); first or second order; both limiters.
+// Face Jacobians are never stored.  Roe flux with the entropy fix and every
+// boundary type, and the laminar term (then 16 directions per face: the
+// face gradient's inputs too, reversed through average_gradients);
+// first or second order; both limiters.
 #include "afx_dual.cuh"
 #include "afx_kernels_impl.cuh"
 
@@ -29,10 +31,12 @@ constexpr int ADJ_NONE = (int)0x80000000;  // limiter target: none / the cell it
 __device__ __forceinline__ int pick4(const int4 v, const int k) { return pick(v, k); }
 
 // sum_m dF_m/d(dir) * w_m of the face flux, for input direction `dir`
-// (0-3: left state, 4-7: right state, or the boundary state when one-sided)
-__device__ __forceinline__ double face_flux_dir(const int bt, const double gamma, const double nx, const double ny,
-                                                const double* qL, const double* qR, const int dir,
-                                                const double* w) {
+// (0-3: left state, 4-7: right state, or the boundary state when one-sided;
+// with the laminar term, 8-11 / 12-15: the face gradient's x / y parts)
+template <int VISC>
+__device__ __forceinline__ double face_flux_dir(const KM<double>& m, const int bt, const double nx, const double ny,
+                                                const double* qL, const double* qR, const double* fgx,
+                                                const double* fgy, const int dir, const double* w) {
     Dual dL[4], dR[4], F[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
@@ -40,11 +44,21 @@ __device__ __forceinline__ double face_flux_dir(const int bt, const double gamma
         dR[k] = Dual(qR[k], dir == k + 4 ? 1.0 : 0.0);
     }
     if (two_sided(bt)) {
-        roe_flux<Dual>(Dual(gamma), Dual(nx), Dual(ny), dL, dR, F);
+        roe_flux<Dual>(Dual(m.gamma), Dual(nx), Dual(ny), dL, dR, F);
+        if (VISC == 1) {
+            Dual gxd[4], gyd[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                gxd[k] = Dual(fgx[k], dir == k + 8 ? 1.0 : 0.0);
+                gyd[k] = Dual(fgy[k], dir == k + 12 ? 1.0 : 0.0);
+            }
+            laminar_flux<Dual>(Dual(m.gamma), Dual(m.R), Dual(m.mu), Dual(m.kheat), Dual(nx), Dual(ny), dL, dR,
+                               gxd, gyd, F);
+        }
     } else {
         Dual qb[4];
-        ghost_state<Dual>(bt, Dual(gamma), Dual(nx), Dual(ny), dL, dR, qb);
-        roe_flux<Dual>(Dual(gamma), Dual(nx), Dual(ny), dL, qb, F);
+        ghost_state<Dual>(bt, Dual(m.gamma), Dual(nx), Dual(ny), dL, dR, qb);
+        roe_flux<Dual>(Dual(m.gamma), Dual(nx), Dual(ny), dL, qb, F);
     }
     return F[0].d * w[0] + F[1].d * w[1] + F[2].d * w[2] + F[3].d * w[3];
 }
@@ -62,22 +76,30 @@ __device__ __forceinline__ double ghost_dir(const int bt, const double gamma, co
     return g[0].d * w[0] + g[1].d * w[1] + g[2].d * w[2] + g[3].d * w[3];
 }
 
-template <bool SECOND>
+// Per face, FB = 2 (inviscid) or 8 (laminar) 4-vectors of fbar:
+// [qL_bar, qR_bar (or the boundary state's), and with the laminar term
+//  gxa_bar, gya_bar, qa_bar, gxb_bar, gyb_bar, qb_bar] -- a/b: the face's
+// cells as the face gradient sees them (solver.h:359-398)
+template <bool SECOND, int VISC>
 __global__ void __launch_bounds__(128) k_adj_face(const KM<double> m, const int n_faces, const d4* __restrict__ q,
                                                   const d4* __restrict__ gx, const d4* __restrict__ gy,
                                                   const d4* __restrict__ phi, const d4* __restrict__ v,
                                                   d4* __restrict__ fbar) {
+    constexpr int FB = VISC == 1 ? 8 : 2;
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= n_faces) return;
     const int2 cc = __ldg(&m.fcell[f]);
     const double2 n = __ldg(&m.fn[f]);
     const double L = __ldg(&m.fLg[f]).x;
-    double q0[4], qL[4], qR[4], w[4], v0[4];
+    double q0[4], q1[4], qL[4], qR[4], w[4], v0[4];
+    double g0x[4] = {0, 0, 0, 0}, g0y[4] = {0, 0, 0, 0}, g1x[4] = {0, 0, 0, 0}, g1y[4] = {0, 0, 0, 0};
     ld4(&q[cc.x], q0);
-    if (SECOND) {
-        double g0x[4], g0y[4], p0[4];
+    if (SECOND || VISC == 1) {
         ld4(&gx[cc.x], g0x);
         ld4(&gy[cc.x], g0y);
+    }
+    if (SECOND) {
+        double p0[4];
         ld4(&phi[cc.x], p0);
         const double2 d0 = __ldg(&m.fd0[f]);
         reconstruct(q0, g0x, g0y, p0, d0.x, d0.y, qL);
@@ -89,12 +111,14 @@ __global__ void __launch_bounds__(128) k_adj_face(const KM<double> m, const int 
     const double A0 = __ldg(&m.area[cc.x]);
     int bt = BT_INTERNAL;
     if (cc.y >= 0) {
-        double q1[4], v1[4];
+        double v1[4];
         ld4(&q[cc.y], q1);
-        if (SECOND) {
-            double g1x[4], g1y[4], p1[4];
+        if (SECOND || VISC == 1) {
             ld4(&gx[cc.y], g1x);
             ld4(&gy[cc.y], g1y);
+        }
+        if (SECOND) {
+            double p1[4];
             ld4(&phi[cc.y], p1);
             const double2 d1 = __ldg(&m.fd1[f]);
             reconstruct(q1, g1x, g1y, p1, d1.x, d1.y, qR);
@@ -109,23 +133,62 @@ __global__ void __launch_bounds__(128) k_adj_face(const KM<double> m, const int 
         for (int k = 0; k < 4; ++k) w[k] = L * (v1[k] / A1 - v0[k] / A0);
     } else {
         bt = __ldg(&m.btype[-cc.y - 1]);
-        ld4(&m.bq[-cc.y - 1], qR);
+        ld4(&m.bq[-cc.y - 1], q1);
 #pragma unroll
-        for (int k = 0; k < 4; ++k) w[k] = -L * (v0[k] / A0);
+        for (int k = 0; k < 4; ++k) {
+            qR[k] = q1[k];
+            w[k] = -L * (v0[k] / A0);
+        }
     }
-    double out[8];
+    // the face gradient of the laminar term (member states, cell gradients;
+    // a boundary side has zero gradient)
+    const bool lam = VISC == 1 && two_sided(bt);
+    double fgx[4] = {0, 0, 0, 0}, fgy[4] = {0, 0, 0, 0};
+    double4 t = make_double4(0, 0, 1, 0);  // (t0, t1, lij): zero adjoint on a face without the term
+    if (lam) {
+        const d4 tt = ldv4d(&m.ft[f]);
+        t = make_double4(tt.x, tt.y, tt.z, tt.w);
+        face_gradient(q0, q1, g0x, g0y, g1x, g1y, tt, fgx, fgy);
+    }
+    constexpr int ND = VISC == 1 ? 16 : 8;
+    double out[ND];
 #pragma unroll 1
-    for (int dir = 0; dir < 8; ++dir) out[dir] = face_flux_dir(bt, m.gamma, n.x, n.y, qL, qR, dir, w);
-    st4(&fbar[2 * (size_t)f], out);
-    st4(&fbar[2 * (size_t)f + 1], out + 4);
+    for (int dir = 0; dir < ND; ++dir)
+        out[dir] = (dir < 8 || lam) ? face_flux_dir<VISC>(m, bt, n.x, n.y, qL, qR, fgx, fgy, dir, w) : 0.0;
+    d4* fb = fbar + (size_t)FB * f;
+    st4(&fb[0], out);
+    st4(&fb[1], out + 4);
+    if (VISC == 1) {
+        // reverse of face_gradient (solver.h:359-398), component by component:
+        // fg = gbar - ((gbar . t) - (qa - qb)/lij) t, gbar the mean gradient
+        double ga_x[4], ga_y[4], qa_b[4], gb_x[4], gb_y[4], qb_b[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const double fx = out[8 + k], fy = out[12 + k];
+            const double e = -(t.x * fx + t.y * fy);  // adjoint of grad_dot - grad_dir
+            const double mx = fx + e * t.x, my = fy + e * t.y;
+            ga_x[k] = gb_x[k] = 0.5 * mx;
+            ga_y[k] = gb_y[k] = 0.5 * my;
+            qa_b[k] = -e / t.z;
+            qb_b[k] = e / t.z;
+        }
+        st4(&fb[2], ga_x);
+        st4(&fb[3], ga_y);
+        st4(&fb[4], qa_b);
+        st4(&fb[5], gb_x);
+        st4(&fb[6], gb_y);
+        st4(&fb[7], qb_b);
+    }
 }
 
-template <bool SECOND>
+template <bool SECOND, int VISC>
 __global__ void __launch_bounds__(128) k_adj_cell(const KM<double> m, const d4* __restrict__ q,
                                                   const d4* __restrict__ gx, const d4* __restrict__ gy,
                                                   const d4* __restrict__ phi, const d4* __restrict__ fbar,
                                                   d4* __restrict__ qbar, d4* __restrict__ gbx, d4* __restrict__ gby,
                                                   d4* __restrict__ lw, int4* __restrict__ lt) {
+    constexpr int FB = VISC == 1 ? 8 : 2;
+    constexpr bool GRAD = SECOND || VISC == 1;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m.n_cells) return;
     const int4 sl = __ldg(&m.cslot[i]);
@@ -146,9 +209,23 @@ __global__ void __launch_bounds__(128) k_adj_cell(const KM<double> m, const d4* 
         const bool own0 = fs > 0;
         const int f = (own0 ? fs : -fs) - 1;
         double side[4];
-        ld4(&fbar[2 * (size_t)f + (own0 ? 0 : 1)], side);
+        const d4* fb = fbar + (size_t)FB * f;
+        ld4(&fb[own0 ? 0 : 1], side);
 #pragma unroll
         for (int k = 0; k < 4; ++k) qb[k] += side[k];
+        if (VISC == 1) {
+            // the face gradient's use of this cell's member state and gradient
+            double sgx[4], sgy[4], sq[4];
+            ld4(&fb[own0 ? 2 : 5], sgx);
+            ld4(&fb[own0 ? 3 : 6], sgy);
+            ld4(&fb[own0 ? 4 : 7], sq);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                qb[k] += sq[k];
+                bx[k] += sgx[k];
+                by[k] += sgy[k];
+            }
+        }
         if (SECOND) {
             const double2 d = own0 ? __ldg(&m.fd0[f]) : __ldg(&m.fd1[f]);
             dxs[s] = d.x;
@@ -241,18 +318,22 @@ __global__ void __launch_bounds__(128) k_adj_cell(const KM<double> m, const d4* 
         st4(&lw[2 * (size_t)i + 1], wmn);
         lt[2 * (size_t)i] = make_int4(tmx[0], tmx[1], tmx[2], tmx[3]);
         lt[2 * (size_t)i + 1] = make_int4(tmn[0], tmn[1], tmn[2], tmn[3]);
+    }
+    if (GRAD) {
         st4(&gbx[i], bx);
         st4(&gby[i], by);
     }
     st4(&qbar[i], qb);
 }
 
-template <bool SECOND>
+template <bool SECOND, int VISC>
 __global__ void __launch_bounds__(128) k_adj_final(const KM<double> m, const d4* __restrict__ q,
                                                    const d4* __restrict__ fbar, const d4* __restrict__ qbar,
                                                    const d4* __restrict__ gbx, const d4* __restrict__ gby,
                                                    const d4* __restrict__ lw, const int4* __restrict__ lt,
                                                    d4* __restrict__ u, d4* __restrict__ bqbar) {
+    constexpr int FB = VISC == 1 ? 8 : 2;
+    constexpr bool GRAD = SECOND || VISC == 1;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= m.n_cells) return;
     const int4 sl = __ldg(&m.cslot[j]);
@@ -261,7 +342,7 @@ __global__ void __launch_bounds__(128) k_adj_final(const KM<double> m, const d4*
     ld4(&qbar[j], uj);
     double bxj[4], byj[4], qj[4];
     const double Aj = __ldg(&m.area[j]);
-    if (SECOND) {
+    if (GRAD) {
         ld4(&gbx[j], bxj);
         ld4(&gby[j], byj);
         ld4(&q[j], qj);
@@ -276,17 +357,19 @@ __global__ void __launch_bounds__(128) k_adj_final(const KM<double> m, const d4*
         const double2 n = __ldg(&m.fn[f]);
         const double2 Lg = __ldg(&m.fLg[f]);
         if (o >= 0) {
-            if (!SECOND) continue;
-            // limiter terms of the neighbour that point at this cell
-            double wx[4], wn[4];
-            ld4(&lw[2 * (size_t)o], wx);
-            ld4(&lw[2 * (size_t)o + 1], wn);
-            const int4 tx = __ldg(&lt[2 * (size_t)o]);
-            const int4 tn = __ldg(&lt[2 * (size_t)o + 1]);
+            if (!GRAD) continue;
+            if (SECOND) {
+                // limiter terms of the neighbour that point at this cell
+                double wx[4], wn[4];
+                ld4(&lw[2 * (size_t)o], wx);
+                ld4(&lw[2 * (size_t)o + 1], wn);
+                const int4 tx = __ldg(&lt[2 * (size_t)o]);
+                const int4 tn = __ldg(&lt[2 * (size_t)o + 1]);
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                if (pick4(tx, k) == j) uj[k] += wx[k];
-                if (pick4(tn, k) == j) uj[k] += wn[k];
+                for (int k = 0; k < 4; ++k) {
+                    if (pick4(tx, k) == j) uj[k] += wx[k];
+                    if (pick4(tn, k) == j) uj[k] += wn[k];
+                }
             }
             // Green-Gauss face value (q_c0 (1-g) + (q_c0 + q_c1)/2 g) L, added
             // to cell 0's sum and subtracted from cell 1's
@@ -307,7 +390,14 @@ __global__ void __launch_bounds__(128) k_adj_final(const KM<double> m, const d4*
             // boundary face b of this cell (always its cell 0)
             const int b = -o - 1;
             double bb[4];
-            ld4(&fbar[2 * (size_t)f + 1], bb);
+            ld4(&fbar[(size_t)FB * f + 1], bb);
+            if (VISC == 1) {
+                // a two-sided boundary's face gradient reads the boundary state
+                double qbb[4];
+                ld4(&fbar[(size_t)FB * f + 7], qbb);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) bb[k] += qbb[k];
+            }
             if (SECOND) {
                 double wx[4], wn[4];
                 ld4(&lw[2 * (size_t)j], wx);
@@ -319,6 +409,8 @@ __global__ void __launch_bounds__(128) k_adj_final(const KM<double> m, const d4*
                     if (pick4(tx, k) == o) bb[k] += wx[k];
                     if (pick4(tn, k) == o) bb[k] += wn[k];
                 }
+            }
+            if (GRAD) {
                 // face value (q_j (1-g) + ghost(q_j, bq) g) L
                 const int bt = __ldg(&m.btype[b]);
                 double qbc[4], fb[4];
@@ -404,7 +496,9 @@ void enqueue_adjoint_prep(const StepArgs& a0, int p, bool with_dt, cudaStream_t 
     dev::launch_prep<double, double>(a, m, (const dev::d4*)a.qm[p], s);
 }
 
-void enqueue_vjp(const StepArgs& a, int p, const AdjArgs& j, cudaStream_t s) {
+namespace {
+template <bool SECOND, int VISC>
+void vjp_launch(const StepArgs& a, int p, const AdjArgs& j, cudaStream_t s) {
     using namespace dev;
     const KM<double> m = make_km<double>(a);
     const d4* q = (const d4*)a.qm[p];
@@ -413,20 +507,22 @@ void enqueue_vjp(const StepArgs& a, int p, const AdjArgs& j, cudaStream_t s) {
     const d4* ph = (const d4*)a.phi;
     const int B = 128;
     const int nf = nblocks(a.n_faces, B), nc = nblocks(a.n_cells, B);
-    if (a.second) {
-        k_adj_face<true><<<nf, B, 0, s>>>(m, a.n_faces, q, gx, gy, ph, (const d4*)j.v, (d4*)j.fbar);
-        k_adj_cell<true><<<nc, B, 0, s>>>(m, q, gx, gy, ph, (const d4*)j.fbar, (d4*)j.qbar, (d4*)j.gbx, (d4*)j.gby,
-                                          (d4*)j.lw, (int4*)j.lt);
-        k_adj_final<true><<<nc, B, 0, s>>>(m, q, (const d4*)j.fbar, (const d4*)j.qbar, (const d4*)j.gbx,
-                                           (const d4*)j.gby, (const d4*)j.lw, (const int4*)j.lt, (d4*)j.u,
-                                           (d4*)j.bqbar);
+    k_adj_face<SECOND, VISC><<<nf, B, 0, s>>>(m, a.n_faces, q, gx, gy, ph, (const d4*)j.v, (d4*)j.fbar);
+    k_adj_cell<SECOND, VISC><<<nc, B, 0, s>>>(m, q, gx, gy, ph, (const d4*)j.fbar, (d4*)j.qbar, (d4*)j.gbx,
+                                              (d4*)j.gby, (d4*)j.lw, (int4*)j.lt);
+    k_adj_final<SECOND, VISC><<<nc, B, 0, s>>>(m, q, (const d4*)j.fbar, (const d4*)j.qbar, (const d4*)j.gbx,
+                                               (const d4*)j.gby, (const d4*)j.lw, (const int4*)j.lt, (d4*)j.u,
+                                               (d4*)j.bqbar);
+}
+}  // namespace
+
+void enqueue_vjp(const StepArgs& a, int p, const AdjArgs& j, cudaStream_t s) {
+    if (a.visc == 1) {
+        if (a.second) vjp_launch<true, 1>(a, p, j, s);
+        else vjp_launch<false, 1>(a, p, j, s);
     } else {
-        k_adj_face<false><<<nf, B, 0, s>>>(m, a.n_faces, q, gx, gy, ph, (const d4*)j.v, (d4*)j.fbar);
-        k_adj_cell<false><<<nc, B, 0, s>>>(m, q, gx, gy, ph, (const d4*)j.fbar, (d4*)j.qbar, (d4*)j.gbx,
-                                           (d4*)j.gby, (d4*)j.lw, (int4*)j.lt);
-        k_adj_final<false><<<nc, B, 0, s>>>(m, q, (const d4*)j.fbar, (const d4*)j.qbar, (const d4*)j.gbx,
-                                            (const d4*)j.gby, (const d4*)j.lw, (const int4*)j.lt, (d4*)j.u,
-                                            (d4*)j.bqbar);
+        if (a.second) vjp_launch<true, 0>(a, p, j, s);
+        else vjp_launch<false, 0>(a, p, j, s);
     }
 }
 

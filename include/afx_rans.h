@@ -202,9 +202,10 @@ int afx_linear_iterations(afx_solver s, int* n);
  * has no adjoint).  R(q) is the residual afx_residual returns (first-stage
  * semantics: gradients and limiter formed from q, solver.h:745-799); bq are
  * the boundary states of the boundary edges (core.h:73-83 for farfield
- * patches).  Inviscid flux only; first or second order; Venkatakrishnan or
- * Michalak limiter (the derivative of the active branch: min/max and limiter
- * cases follow the state).  FP64 solvers only (AFX_ERR_CONFIG otherwise).
+ * patches).  Inviscid or laminar flux; first or second order; Green-Gauss
+ * gradient; Venkatakrishnan or Michalak limiter (the derivative of the
+ * active branch: min/max and limiter cases follow the state).  FP64 solvers
+ * only (AFX_ERR_CONFIG otherwise).
  *
  * u = (dR/dq)^T v and, if bq_bar != NULL, bq_bar = (dR/dbq)^T v (4 per
  * boundary edge, boundary order).  q: the state to linearise about, or NULL
@@ -242,7 +243,7 @@ int afx_deform_patch(afx_solver s, const char* patch, const double* a, int n, do
  * afx_adjoint_solve on the same patch (call it first, at the converged
  * state): dJ/da_k = dJ/da_k|_q + lam . dR/da_k|_q, the geometric partials by
  * central differences of the residual and the forces with step h
- * (h <= 0: 1e-7), no re-convergence.  FP64 solvers, inviscid. */
+ * (h <= 0: 1e-7), no re-convergence.  FP64 solvers. */
 int afx_adjoint_patch(afx_solver s, const char* patch, const char* objective, double power, double h, double* dJ,
                       int n);
 

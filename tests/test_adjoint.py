@@ -40,7 +40,8 @@ def _vR(orc_s, q, e, v):
     return f
 
 
-@pytest.mark.parametrize("variant", [dict(), dict(limiter="michalak"), dict(second_order=False)])
+@pytest.mark.parametrize("variant", [dict(), dict(limiter="michalak"), dict(second_order=False),
+                                     dict(viscosity="laminar"), dict(viscosity="laminar", second_order=False)])
 def test_vjp_matches_oracle_finite_differences(afx, orc, variant):
     m, bcs = omesh_case(48, 24)
     so = oracle_solver(orc, m, bcs, **variant)
