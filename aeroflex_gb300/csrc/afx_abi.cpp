@@ -36,7 +36,8 @@ void enqueue_full_state(int n, int nb, const int* cell_old, const int* owner_dev
 void enqueue_wall_dist(int nc, const double* cx, const double* cy, int nw, const double* wx, const double* wy,
                        double* out, cudaStream_t s);
 struct ImplicitEngine;
-ImplicitEngine* implicit_create(const StepArgs& a, bool f32, const std::vector<int>& colors, cudaStream_t s);
+ImplicitEngine* implicit_create(const StepArgs& a, bool f32, bool graph, const std::vector<int>& colors,
+                                cudaStream_t s);
 void implicit_destroy(ImplicitEngine* e);
 void implicit_fill(ImplicitEngine* e, const StepArgs& a, int p, cudaStream_t s);
 int implicit_solve_update(ImplicitEngine* e, const StepArgs& a, int p, const double* b, double relax,
@@ -854,6 +855,8 @@ int afx_config_set_double(afx_config c, const char* key, double v) {
             c->s.fp64_correction_interval = (int)v;
         } else if (k == "fp64_finish") {
             c->s.fp64_finish = v != 0;
+        } else if (k == "krylov_graph") {
+            c->s.krylov_graph = v != 0;
         }
         else if (k == "second_order") c->s.second_order = v != 0;
         else if (double* p = dfield(c->s, k)) *p = v;
@@ -870,6 +873,7 @@ int afx_config_get_double(afx_config c, const char* key, double* v) {
         else if (k == "block_size") *v = c->s.block_size;
         else if (k == "fp64_correction_interval") *v = c->s.fp64_correction_interval;
         else if (k == "fp64_finish") *v = c->s.fp64_finish ? 1 : 0;
+        else if (k == "krylov_graph") *v = c->s.krylov_graph ? 1 : 0;
         else if (k == "second_order") *v = c->s.second_order ? 1 : 0;
         else if (double* p = dfield(c->s, k)) *v = *p;
         else throw Error(AFX_ERR_ARG, "unknown numeric setting '" + k + "'");
@@ -1160,7 +1164,7 @@ static std::unique_ptr<afx_solver_s> make_solver(const HostMesh& m, const Device
                 color[i] = c;
             }
             s->imp_b = s->dalloc(N * 32);
-            s->imp = implicit_create(s->A64(), !s->fp64, color, s->stream);
+            s->imp = implicit_create(s->A64(), !s->fp64, st.krylov_graph, color, s->stream);
         }
         s->d_stage.alloc(N * 32);
         AFX_CUDA(cudaHostAlloc((void**)&s->h_stage, N * 32, cudaHostAllocDefault));
@@ -1950,6 +1954,14 @@ int afx_batch_last_device_seconds(afx_batch b, double* sec) {
     return guarded([&] {
         if (!b || !sec) throw Error(AFX_ERR_ARG, "null argument");
         *sec = b->s->last_sec;
+    });
+}
+
+int afx_batch_linear_iterations(afx_batch b, int* iters, int n_cases) {
+    return guarded([&] {
+        if (!b || !iters) throw Error(AFX_ERR_ARG, "null argument");
+        if (n_cases != b->n) throw Error(AFX_ERR_ARG, "n_cases must be the batch's case count");
+        for (int c = 0; c < b->n; ++c) iters[c] = b->s->imp ? b->s->imp_lin_iters : 0;
     });
 }
 

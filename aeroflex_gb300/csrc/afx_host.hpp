@@ -57,6 +57,10 @@ struct Settings {
     // FP32-mixed only: run_to_convergence switches to FP64 iterations once the
     // FP32 residual stops falling
     bool fp64_finish = false;
+    // implicit solver: run each GMRES solve as one CUDA graph with device-side
+    // loops (true), or drive the same kernels from a host loop (false: every
+    // kernel is a plain launch that a profiler can list)
+    bool krylov_graph = true;
 
     int viscosity_code() const;
     static int bc_code(const std::string& t);

@@ -45,7 +45,7 @@ struct GmresCtl {
     int iters;   // Krylov iterations of this solve
     int halt;    // no further restart cycle
     int max_iters;
-    int pad;
+    int graph;   // launched inside the solve graph: set the WHILE conditions
     cudaGraphConditionalHandle hin, hout;  // WHILE conditions: Arnoldi steps, restart cycles
     double tol;  // absolute residual target
     double res;  // current residual estimate
@@ -69,14 +69,39 @@ __device__ __forceinline__ void ldt(const float4* p, float* v) {
 __device__ __forceinline__ void stt(d4* p, const double* v) { st4(p, v); }
 __device__ __forceinline__ void stt(float4* p, const float* v) { *p = make_float4(v[0], v[1], v[2], v[3]); }
 
-// y += sgn * B x for a 4x4 block (row-major) in T
+// y += sgn * B x for a 4x4 block (row-major) in T.  Blocks start on a
+// 16-byte boundary (16 T per block, buffers from cudaMalloc), so each row is
+// read with 16-byte vector loads: a cell's block is then 4 (FP32) or 8 (FP64)
+// load instructions, not 16 scattered scalar ones.
 template <class T>
-__device__ __forceinline__ void bmv_add(const T* __restrict__ B, const T* x, T* y, const T sgn) {
+__device__ __forceinline__ void bmv_add(const T* __restrict__ B, const T* x, T* y, const T sgn);
+template <>
+__device__ __forceinline__ void bmv_add<float>(const float* __restrict__ B, const float* x, float* y,
+                                               const float sgn) {
+    const float4* b = reinterpret_cast<const float4*>(B);
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-        T s = 0;
+        const float4 row = __ldg(&b[r]);
+        float s = 0;
+        s += row.x * x[0];
+        s += row.y * x[1];
+        s += row.z * x[2];
+        s += row.w * x[3];
+        y[r] += sgn * s;
+    }
+}
+template <>
+__device__ __forceinline__ void bmv_add<double>(const double* __restrict__ B, const double* x, double* y,
+                                                const double sgn) {
+    const double2* b = reinterpret_cast<const double2*>(B);
 #pragma unroll
-        for (int c = 0; c < 4; ++c) s += B[4 * r + c] * x[c];
+    for (int r = 0; r < 4; ++r) {
+        const double2 u = __ldg(&b[2 * r]), v = __ldg(&b[2 * r + 1]);
+        double s = 0;
+        s += u.x * x[0];
+        s += u.y * x[1];
+        s += v.x * x[2];
+        s += v.y * x[3];
         y[r] += sgn * s;
     }
 }
@@ -403,13 +428,16 @@ __global__ void __launch_bounds__(256) k_imp_spmv(const KM<double> m, const T* _
 
 // One colour of a block Gauss-Seidel sweep: x_i = D_i^-1 (r_i - sum O x_n).
 // r = rbase + (*rk) * stride when rk is given (the current Krylov vector).
+// In the forward sweep (fwd = this colour) only neighbours of lower colours
+// are read: the higher colours have no value yet (zero start).
 template <class T>
 __global__ void __launch_bounds__(256) k_imp_gs(const KM<double> m, const T* __restrict__ jf,
                                                 const T* __restrict__ dinv, const int* __restrict__ cells,
                                                 const int n, const T* __restrict__ rbase, const int* __restrict__ rk,
                                                 const long long stride, typename B4<T>::type* __restrict__ x,
                                                 const int* __restrict__ stop, const int* __restrict__ case_of,
-                                                const int* __restrict__ case_done) {
+                                                const int* __restrict__ case_done,
+                                                const unsigned char* __restrict__ col, const int fwd) {
     if (stop && *stop) return;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
@@ -430,6 +458,7 @@ __global__ void __launch_bounds__(256) k_imp_gs(const KM<double> m, const T* __r
         const int fs = pick(sl, k);
         const int o = pick(nb, k);
         if (fs == 0 || o < 0) continue;
+        if (fwd >= 0 && (int)__ldg(&col[o]) >= fwd) continue;
         const int f = (fs > 0 ? fs : -fs) - 1;
         T xo[4];
         ldt(&x[o], xo);
@@ -440,87 +469,124 @@ __global__ void __launch_bounds__(256) k_imp_gs(const KM<double> m, const T* __r
     stt(&x[i], xi);
 }
 
-template <class T>
-__global__ void k_imp_zero(const int n4, T* __restrict__ x, const int* __restrict__ stop) {
-    if (stop && *stop) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n4) x[i] = T(0);
+// Dot products against the Krylov basis v_0..v_{nv-1} (v_j = V + j*n) in
+// one pass, with the Gram-Schmidt update fused in:
+//   MODE 0: out_j = v_j . w
+//   MODE 1: w -= sum_j hin_j v_j, then out_j = v_j . w   (CGS pass 1 + dots of pass 2)
+//   MODE 2: w -= sum_j hin_j v_j, then out_0 = w . w     (CGS pass 2 + the norm)
+// Each block writes its partial sums; the last block to finish adds them in
+// a fixed pattern (DOT_G threads per output, each over a fixed stride of
+// blocks, then a fixed shuffle tree), so the result is deterministic, and
+// re-arms the counter.
+// 16-byte chunks of a vector in T, their dot product and w -= h v
+template <class T> struct Vec16;
+template <> struct Vec16<float> { using type = float4; static constexpr int W = 4; };
+template <> struct Vec16<double> { using type = double2; static constexpr int W = 2; };
+__device__ __forceinline__ float vdot(const float4 a, const float4 b) {
+    return ((a.x * b.x + a.y * b.y) + a.z * b.z) + a.w * b.w;
+}
+__device__ __forceinline__ double vdot(const double2 a, const double2 b) { return a.x * b.x + a.y * b.y; }
+__device__ __forceinline__ void vsub(float4& w, const float h, const float4 v) {
+    w.x -= h * v.x; w.y -= h * v.y; w.z -= h * v.z; w.w -= h * v.w;
+}
+__device__ __forceinline__ void vsub(double2& w, const double h, const double2 v) {
+    w.x -= h * v.x; w.y -= h * v.y;
 }
 
-// Dot products of w with v_0..v_{nv-1} (v_j = V + j*n) in one launch: each
-// block writes its partial sums, and the last block to finish adds the
-// partials in block order (a fixed order, so the result is deterministic)
-// and re-arms the counter.
-template <class T>
-__global__ void __launch_bounds__(DOT_THREADS) k_imp_dots(const int n, int nv, const int* __restrict__ nvk,
-                                                          const T* __restrict__ V, const T* __restrict__ w,
-                                                          double* __restrict__ part, unsigned* __restrict__ counter,
-                                                          double* __restrict__ out, const int* __restrict__ stop) {
+constexpr int DOT_G = 8;  // threads of the last block per output
+static_assert(DOT_THREADS / DOT_G >= GM_M + 1, "one group per output");
+
+template <class T, int MODE>
+__global__ void __launch_bounds__(DOT_THREADS, 2) k_imp_dots(const int n, int nv, const int* __restrict__ nvk,
+                                                          const T* __restrict__ V, T* __restrict__ w,
+                                                          const double* __restrict__ hin, double* __restrict__ part,
+                                                          unsigned* __restrict__ counter, double* __restrict__ out,
+                                                          const int* __restrict__ stop) {
     __shared__ double sh[DOT_THREADS / 32][GM_M + 1];
+    __shared__ T hs[GM_M + 1];
     __shared__ bool last;
     if (stop && *stop) return;
     if (nvk) nv = *nvk + 1;  // v_0 .. v_k of the current Arnoldi step
-    // one pass over w and the nv vectors, nv accumulators per thread
-    // per-thread partial sums in T (a few elements each), then double
+    const int nout = MODE == 2 ? 1 : nv;
+    if (MODE > 0) {
+        if ((int)threadIdx.x < nv) hs[threadIdx.x] = (T)hin[threadIdx.x];
+        __syncthreads();
+    }
+    // per-thread partial sums in T over 16-byte chunks of the vectors (a few
+    // chunks each; n is 4 * cells, so whole chunks), then double
+    using VT = typename Vec16<T>::type;
+    const int nc = n / Vec16<T>::W;
+    const VT* __restrict__ Vv = reinterpret_cast<const VT*>(V);
+    VT* __restrict__ wv = reinterpret_cast<VT*>(w);
     T acc[GM_M + 1];
 #pragma unroll
     for (int j = 0; j <= GM_M; ++j) acc[j] = 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const T wi = w[i];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x) {
+        VT wi = wv[i];
+        if (MODE == 0) {
 #pragma unroll
-        for (int j = 0; j <= GM_M; ++j)
-            if (j < nv) acc[j] += V[(size_t)j * n + i] * wi;
+            for (int j = 0; j <= GM_M; ++j)
+                if (j < nv) acc[j] += vdot(Vv[(size_t)j * nc + i], wi);
+        } else {
+#pragma unroll
+            for (int j = 0; j <= GM_M; ++j)
+                if (j < nv) vsub(wi, hs[j], Vv[(size_t)j * nc + i]);
+            wv[i] = wi;
+            if (MODE == 1) {
+                // the basis chunks again, from L2 where they were just read (no
+                // new HBM traffic, and no registers held across the update)
+#pragma unroll
+                for (int j = 0; j <= GM_M; ++j)
+                    if (j < nv) acc[j] += vdot(__ldcg(&Vv[(size_t)j * nc + i]), wi);
+            } else {
+                acc[0] += vdot(wi, wi);
+            }
+        }
     }
     const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
 #pragma unroll
     for (int j = 0; j <= GM_M; ++j) {
-        if (j >= nv) break;
+        if (j >= nout) break;
         double v = (double)acc[j];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
         if (lane == 0) sh[wp][j] = v;
     }
     __syncthreads();
-    if ((int)threadIdx.x < nv) {
+    if ((int)threadIdx.x < nout) {
         double t = 0;
         for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += sh[k][threadIdx.x];
-        part[(size_t)blockIdx.x * nv + threadIdx.x] = t;
+        part[(size_t)blockIdx.x * nout + threadIdx.x] = t;
         __threadfence();  // the partials are visible before the block is counted
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        last = atomicAdd(counter, 1u) == gridDim.x - 1;
-    }
+    if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
     __syncthreads();
     if (!last) return;
     __threadfence();
-    // the last block: each of nv threads adds the block partials in block order
-    if ((int)threadIdx.x < nv) {
-        double t = 0;
-        for (int b = 0; b < (int)gridDim.x; ++b) t += ((volatile double*)part)[(size_t)b * nv + threadIdx.x];
-        out[threadIdx.x] = t;
+    // the last block: DOT_G threads per output, each over blocks g, g+DOT_G,
+    // ... (L2 reads, several in flight), then a fixed shuffle tree
+    const int j = threadIdx.x / DOT_G, g = threadIdx.x % DOT_G;
+    double t = 0;
+    if (j < nout) {
+        const int nb = (int)gridDim.x;
+        int b = g;
+        double t1 = 0, t2 = 0, t3 = 0;
+        for (; b + 3 * DOT_G < nb; b += 4 * DOT_G) {
+            t += __ldcg(&part[(size_t)b * nout + j]);
+            t1 += __ldcg(&part[(size_t)(b + DOT_G) * nout + j]);
+            t2 += __ldcg(&part[(size_t)(b + 2 * DOT_G) * nout + j]);
+            t3 += __ldcg(&part[(size_t)(b + 3 * DOT_G) * nout + j]);
+        }
+        for (; b < nb; b += DOT_G) t += __ldcg(&part[(size_t)b * nout + j]);
+        t = (t + t1) + (t2 + t3);
     }
+#pragma unroll
+    for (int o = DOT_G / 2; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o, DOT_G);
+    if (j < nout && g == 0) out[j] = t;
     if (threadIdx.x == 0) *counter = 0;
 }
 
-// w -= sum_j h[j] v_j
-template <class T>
-__global__ void __launch_bounds__(256) k_imp_orth(const int n, int nv, const int* __restrict__ nvk,
-                                                  const T* __restrict__ V, const double* __restrict__ h,
-                                                  T* __restrict__ w, const int* __restrict__ stop) {
-    __shared__ T hs[GM_M + 1];
-    if (stop && *stop) return;
-    if (nvk) nv = *nvk + 1;
-    if ((int)threadIdx.x < nv) hs[threadIdx.x] = (T)h[threadIdx.x];
-    __syncthreads();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    T s = w[i];
-    for (int j = 0; j < nv; ++j) s -= hs[j] * V[(size_t)j * n + i];
-    w[i] = s;
-}
-
-// v = w * scale[0] (scale read from the device)
 // v = w * scale[0]; with vk given, v = vbase + (*vk) * n (the next Krylov vector)
 template <class T>
 __global__ void __launch_bounds__(256) k_imp_scale(const int n, const T* __restrict__ w, const double* __restrict__ scale,
@@ -544,7 +610,7 @@ __global__ void __launch_bounds__(32) k_imp_arnoldi(GmresCtl* c, const double* _
     __shared__ double col[GM_M + 1], cs[GM_M], sn[GM_M], gj[1];
     const int lane = threadIdx.x;
     if (c->stop) {
-        if (lane == 0) cudaGraphSetConditional(c->hin, 0);
+        if (lane == 0 && c->graph) cudaGraphSetConditional(c->hin, 0);
         return;
     }
     const int j = c->k;
@@ -580,7 +646,7 @@ __global__ void __launch_bounds__(32) k_imp_arnoldi(GmresCtl* c, const double* _
         c->iters += 1;
         const int st = (c->res <= c->tol || j + 1 == GM_M || hn == 0 || c->iters >= c->max_iters) ? 1 : 0;
         c->stop = st;
-        cudaGraphSetConditional(c->hin, st ? 0 : 1);
+        if (c->graph) cudaGraphSetConditional(c->hin, st ? 0 : 1);
     }
     __syncwarp();
     for (int t = lane; t <= j + 1; t += 32) c->H[t + (GM_M + 1) * j] = col[t];
@@ -671,18 +737,20 @@ __global__ void k_imp_cycle_init(GmresCtl* c, const double* __restrict__ rr, dou
     c->stop = (beta <= c->tol) ? 1 : 0;
     c->halt = c->stop;
     scale[0] = beta > 0 ? 1.0 / beta : 0.0;
-    if (first) cudaGraphSetConditional(c->hout, c->stop ? 0 : 1);
+    if (first && c->graph) cudaGraphSetConditional(c->hout, c->stop ? 0 : 1);
 }
 
 // Start of a restart cycle (inside the restart loop's body): enter the
 // Arnoldi loop unless the cycle is already converged
-__global__ void k_imp_enter(GmresCtl* c) { cudaGraphSetConditional(c->hin, c->stop ? 0 : 1); }
+__global__ void k_imp_enter(GmresCtl* c) {
+    if (c->graph) cudaGraphSetConditional(c->hin, c->stop ? 0 : 1);
+}
 
 // End of a restart cycle: another one if not converged and under the limit
 __global__ void k_imp_outer_check(GmresCtl* c) {
     const int cont = (c->res > c->tol) && (c->iters < c->max_iters) && (c->k > 0);
     c->halt = cont ? 0 : 1;
-    cudaGraphSetConditional(c->hout, cont ? 1 : 0);
+    if (c->graph) cudaGraphSetConditional(c->hout, cont ? 1 : 0);
 }
 
 }  // namespace dev
@@ -696,6 +764,7 @@ inline int nb_(long long n, int b) { return (int)((n + b - 1) / b); }
 
 struct ImplicitEngine {
     bool f32 = false;
+    bool graph = true;  // GMRES as one graph with device-side loops, else a host loop
     int N = 0, F = 0, n4 = 0;
     int n_colors = 0;
     std::vector<int> color_ptr;
@@ -724,9 +793,11 @@ struct ImplicitEngine {
     size_t ts() const { return f32 ? 4 : 8; }
 };
 
-ImplicitEngine* implicit_create(const StepArgs& a, bool f32, const std::vector<int>& colors, cudaStream_t s) {
+ImplicitEngine* implicit_create(const StepArgs& a, bool f32, bool graph, const std::vector<int>& colors,
+                                cudaStream_t s) {
     auto* e = new ImplicitEngine();
     e->f32 = f32;
+    e->graph = graph;
     e->N = a.n_cells;
     e->F = a.n_faces;
     e->n4 = 4 * a.n_cells;
@@ -752,7 +823,11 @@ ImplicitEngine* implicit_create(const StepArgs& a, bool f32, const std::vector<i
     chk(cudaMalloc(&e->z, (size_t)e->n4 * T));
     chk(cudaMalloc(&e->t, (size_t)e->n4 * T));
     chk(cudaMalloc((void**)&e->x, (size_t)e->n4 * 8));
-    e->nbd = std::min(1024, nb_(e->n4, dev::DOT_THREADS * 4));
+    int dev_id = 0, sms = 0;
+    cudaGetDevice(&dev_id);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_id);
+    // two resident blocks per SM at most: the last block then sums few partials
+    e->nbd = std::max(1, std::min(2 * std::max(sms, 1), nb_(e->n4, dev::DOT_THREADS * 4)));
     chk(cudaMalloc((void**)&e->part, (size_t)e->nbd * (dev::GM_M + 1) * 8));
     chk(cudaMalloc((void**)&e->small, (2 * (dev::GM_M + 1) + 2) * 8));
     chk(cudaMalloc((void**)&e->counter, sizeof(unsigned)));
@@ -768,6 +843,8 @@ ImplicitEngine* implicit_create(const StepArgs& a, bool f32, const std::vector<i
         chk(cudaStreamSynchronize(s));
     }
     chk(cudaMemsetAsync(e->jf, 0, (size_t)e->F * 32 * T, s));
+    e->h_ctl->graph = graph ? 1 : 0;
+    chk(cudaMemcpyAsync(&e->ctl->graph, &e->h_ctl->graph, sizeof(int), cudaMemcpyHostToDevice, s));
     chk(cudaStreamSynchronize(s));
     return e;
 }
@@ -854,22 +931,27 @@ struct Ops {
         dev::k_imp_spmv<T><<<nb_(e->N, 256), 256, 0, s>>>(m, (const T*)e->jf, (const T*)e->dblk, (const V4*)x, (V4*)y,
                                                           st, a.case_of, a.case_done);
     }
-    // one symmetric multicolour block Gauss-Seidel sweep from x = 0; the
-    // input is r, or the current Krylov vector V + k*n when rk is given
+    // one symmetric multicolour block Gauss-Seidel sweep from x = 0 (the
+    // ILU(0) factors in the colour ordering); the input is r, or the current
+    // Krylov vector V + k*n when rk is given.  The forward sweep forms every
+    // cell (reading lower colours only); the backward sweep skips the top
+    // colour, whose value it would form again unchanged.
     void precond(const T* r, const int* rk, T* x, const int* st) const {
-        dev::k_imp_zero<T><<<nb_(e->n4, 256), 256, 0, s>>>(e->n4, x, st);
-        for (int pass = 0; pass < 2; ++pass)
-            for (int k = 0; k < e->n_colors; ++k) {
-                const int c = pass == 0 ? k : e->n_colors - 1 - k;
-                const int c0 = e->color_ptr[c], cn = e->color_ptr[c + 1] - c0;
-                if (cn == 0) continue;
-                dev::k_imp_gs<T><<<nb_(cn, 256), 256, 0, s>>>(m, (const T*)e->jf, (const T*)e->dinv,
-                                                              e->color_cells + c0, cn, r, rk, (long long)e->n4,
-                                                              (V4*)x, st, a.case_of, a.case_done);
-            }
+        const int C = e->n_colors;
+        for (int k = 0; k < 2 * C - 1; ++k) {
+            const int c = k < C ? k : 2 * C - 2 - k;
+            const int c0 = e->color_ptr[c], cn = e->color_ptr[c + 1] - c0;
+            if (cn == 0) continue;
+            dev::k_imp_gs<T><<<nb_(cn, 256), 256, 0, s>>>(m, (const T*)e->jf, (const T*)e->dinv, e->color_cells + c0,
+                                                          cn, r, rk, (long long)e->n4, (V4*)x, st, a.case_of,
+                                                          a.case_done, e->color_of, k < C ? c : -1);
+        }
     }
-    void dots(int nv, const int* nvk, const T* V, const T* w, double* out, const int* st) const {
-        dev::k_imp_dots<T><<<e->nbd, dev::DOT_THREADS, 0, s>>>(e->n4, nv, nvk, V, w, e->part, e->counter, out, st);
+    // MODE 0: out = V^T w; 1: w -= V hin, out = V^T w; 2: w -= V hin, out = w.w
+    template <int MODE>
+    void dots(int nv, const int* nvk, const T* V, T* w, const double* hin, double* out, const int* st) const {
+        dev::k_imp_dots<T, MODE><<<e->nbd, dev::DOT_THREADS, 0, s>>>(e->n4, nv, nvk, V, w, hin, e->part, e->counter,
+                                                                   out, st);
     }
 };
 
@@ -922,7 +1004,7 @@ cudaGraphExec_t build_gmres_graph(ImplicitEngine* e, const Ops<T>& o0, const dou
     T* v0 = o.vec(0);
     cudaMemsetAsync(e->x, 0, (size_t)n * 8, s);
     k_imp_cast<T><<<nb_(n, 256), 256, 0, s>>>(n, b, v0, nullptr);
-    o.dots(1, nullptr, v0, v0, ww, nullptr);
+    o.template dots<0>(1, nullptr, v0, v0, nullptr, ww, nullptr);
     k_imp_cycle_init<<<1, 1, 0, s>>>(e->ctl, ww, scale, 1, 1e-2, max_iters);
     k_imp_scale<T><<<nb_(n, 256), 256, 0, s>>>(n, v0, scale, v0, nullptr, stop);
     cudaGraph_t body_out = add_while(s, &hout);
@@ -943,7 +1025,7 @@ cudaGraphExec_t build_gmres_graph(ImplicitEngine* e, const Ops<T>& o0, const dou
         k_imp_cast<T><<<nb_(n, 256), 256, 0, s2>>>(n, e->x, (T*)e->t, halt);
         q.spmv((const T*)e->t, (T*)e->w, halt);
         k_imp_resid<T><<<nb_(n, 256), 256, 0, s2>>>(n, b, (const T*)e->w, q.vec(0), halt);
-        q.dots(1, nullptr, q.vec(0), q.vec(0), ww, halt);
+        q.template dots<0>(1, nullptr, q.vec(0), q.vec(0), nullptr, ww, halt);
         k_imp_cycle_init<<<1, 1, 0, s2>>>(e->ctl, ww, scale, 0, 1e-2, max_iters);
         k_imp_scale<T><<<nb_(n, 256), 256, 0, s2>>>(n, q.vec(0), scale, q.vec(0), nullptr, halt);
         chk(cudaStreamEndCapture(s2, &body_out));
@@ -952,11 +1034,11 @@ cudaGraphExec_t build_gmres_graph(ImplicitEngine* e, const Ops<T>& o0, const dou
         Ops<T> r(e, o0.a, s3);
         r.precond(r.vec(0), kptr, (T*)e->z, stop);
         r.spmv((const T*)e->z, (T*)e->w, stop);
-        r.dots(0, kptr, r.vec(0), (const T*)e->w, h1, stop);
-        k_imp_orth<T><<<nb_(n, 256), 256, 0, s3>>>(n, 0, kptr, r.vec(0), h1, (T*)e->w, stop);
-        r.dots(0, kptr, r.vec(0), (const T*)e->w, h2, stop);
-        k_imp_orth<T><<<nb_(n, 256), 256, 0, s3>>>(n, 0, kptr, r.vec(0), h2, (T*)e->w, stop);
-        r.dots(1, nullptr, (const T*)e->w, (const T*)e->w, ww, stop);
+        // CGS2 in three passes over the basis: h1 = V^T w; w -= V h1 and
+        // h2 = V^T w; w -= V h2 and ||w||^2
+        r.template dots<0>(0, kptr, r.vec(0), (T*)e->w, nullptr, h1, stop);
+        r.template dots<1>(0, kptr, r.vec(0), (T*)e->w, h1, h2, stop);
+        r.template dots<2>(0, kptr, r.vec(0), (T*)e->w, h2, ww, stop);
         k_imp_arnoldi<<<1, 32, 0, s3>>>(e->ctl, h1, h2, ww, scale);
         k_imp_scale<T><<<nb_(n, 256), 256, 0, s3>>>(n, (const T*)e->w, scale, r.vec(0), kptr, stop);
         chk(cudaStreamEndCapture(s3, &body_in));
@@ -973,8 +1055,69 @@ cudaGraphExec_t build_gmres_graph(ImplicitEngine* e, const Ops<T>& o0, const dou
     return ex;
 }
 
+// The same solve as build_gmres_graph with the two loops on the host: the
+// control block is read back after every Arnoldi step, so each kernel is a
+// plain launch (for profilers; slower by one host round trip per step).
+template <class T>
+int gmres_host_loop(ImplicitEngine* e, const StepArgs& a, const double* b, cudaStream_t s, int max_iters) {
+    using namespace dev;
+    const int n = e->n4;
+    double* h1 = e->small;
+    double* h2 = e->small + (GM_M + 1);
+    double* ww = e->small + 2 * (GM_M + 1);
+    double* scale = ww + 1;
+    int* kptr = &e->ctl->k;
+    int* stop = &e->ctl->stop;
+    int* halt = &e->ctl->halt;
+    Ops<T> o(e, a, s);
+    auto read_ctl = [&]() {
+        // stop, k, iters, halt: the loop conditions
+        if (cudaMemcpyAsync(e->h_ctl, e->ctl, 4 * sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            throw Error(7, "implicit solver: GMRES failed");
+    };
+    T* v0 = o.vec(0);
+    cudaMemsetAsync(e->x, 0, (size_t)n * 8, s);
+    k_imp_cast<T><<<nb_(n, 256), 256, 0, s>>>(n, b, v0, nullptr);
+    o.template dots<0>(1, nullptr, v0, v0, nullptr, ww, nullptr);
+    k_imp_cycle_init<<<1, 1, 0, s>>>(e->ctl, ww, scale, 1, 1e-2, max_iters);
+    k_imp_scale<T><<<nb_(n, 256), 256, 0, s>>>(n, v0, scale, v0, nullptr, stop);
+    read_ctl();
+    if (!e->h_ctl->stop) {
+        for (;;) {
+            for (;;) {  // Arnoldi steps of the cycle
+                read_ctl();
+                if (e->h_ctl->stop) break;
+                o.precond(o.vec(0), kptr, (T*)e->z, stop);
+                o.spmv((const T*)e->z, (T*)e->w, stop);
+                o.template dots<0>(0, kptr, o.vec(0), (T*)e->w, nullptr, h1, stop);
+                o.template dots<1>(0, kptr, o.vec(0), (T*)e->w, h1, h2, stop);
+                o.template dots<2>(0, kptr, o.vec(0), (T*)e->w, h2, ww, stop);
+                k_imp_arnoldi<<<1, 32, 0, s>>>(e->ctl, h1, h2, ww, scale);
+                k_imp_scale<T><<<nb_(n, 256), 256, 0, s>>>(n, (const T*)e->w, scale, o.vec(0), kptr, stop);
+            }
+            k_imp_solve_y<<<1, 32, 0, s>>>(e->ctl);
+            k_imp_lincomb<T><<<nb_(n, 256), 256, 0, s>>>(n, o.vec(0), e->ctl, (T*)e->t);
+            o.precond((const T*)e->t, nullptr, (T*)e->z, nullptr);
+            k_imp_addx<T><<<nb_(n, 256), 256, 0, s>>>(n, (const T*)e->z, e->x);
+            k_imp_outer_check<<<1, 1, 0, s>>>(e->ctl);
+            k_imp_cast<T><<<nb_(n, 256), 256, 0, s>>>(n, e->x, (T*)e->t, halt);
+            o.spmv((const T*)e->t, (T*)e->w, halt);
+            k_imp_resid<T><<<nb_(n, 256), 256, 0, s>>>(n, b, (const T*)e->w, o.vec(0), halt);
+            o.template dots<0>(1, nullptr, o.vec(0), o.vec(0), nullptr, ww, halt);
+            k_imp_cycle_init<<<1, 1, 0, s>>>(e->ctl, ww, scale, 0, 1e-2, max_iters);
+            k_imp_scale<T><<<nb_(n, 256), 256, 0, s>>>(n, o.vec(0), scale, o.vec(0), nullptr, halt);
+            read_ctl();
+            if (e->h_ctl->halt) break;
+        }
+    }
+    read_ctl();
+    return e->h_ctl->iters;
+}
+
 template <class T>
 int gmres(ImplicitEngine* e, const StepArgs& a, const double* b, cudaStream_t s, int max_iters) {
+    if (!e->graph) return gmres_host_loop<T>(e, a, b, s, max_iters);
     Ops<T> o(e, a, s);
     if (e->cyc_b != b || !e->cyc[0]) {
         if (e->cyc[0]) cudaGraphExecDestroy(e->cyc[0]);

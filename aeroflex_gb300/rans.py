@@ -32,7 +32,7 @@ ABI_SYMBOLS = [
     "afx_batch_case_history", "afx_batch_forces", "afx_batch_set_farfield", "afx_batch_autotune",
     "afx_batch_last_device_seconds", "afx_residual_vjp", "afx_boundary_states", "afx_adjoint_solve",
     "afx_adjoint_state", "afx_linear_iterations", "afx_prolongate", "afx_patch_nodes", "afx_deform_patch",
-    "afx_adjoint_patch", "afx_wall_distance", "afx_mesh_set_nodes",
+    "afx_adjoint_patch", "afx_wall_distance", "afx_mesh_set_nodes", "afx_batch_linear_iterations",
 ]
 N_KERNEL_KINDS = 7
 
@@ -112,6 +112,7 @@ def lib():
         "afx_adjoint_solve": (i, [vp, cp, cp, d, i, vp, P(i), P(d)]),
         "afx_adjoint_state": (i, [vp, vp, ll]),
         "afx_linear_iterations": (i, [vp, P(i)]),
+        "afx_batch_linear_iterations": (i, [vp, vp, i]),
         "afx_prolongate": (i, [vp, vp]),
         "afx_patch_nodes": (i, [vp, cp, vp, vp, vp, i, P(i)]),
         "afx_deform_patch": (i, [vp, cp, vp, i, d]),
@@ -499,3 +500,9 @@ class Batch:
         s = ctypes.c_double()
         _check(lib().afx_batch_last_device_seconds(self.h, ctypes.byref(s)))
         return s.value
+
+    def linear_iterations(self):
+        """Krylov iterations of each case in the last implicit iteration."""
+        out = np.zeros(self.n, np.int32)
+        _check(lib().afx_batch_linear_iterations(self.h, _ptr(out), self.n))
+        return out

@@ -171,11 +171,32 @@ def run_lean(args):
     marr = meshgen.channel(args.nx, args.ny, jitter=0.2, seed=1, shuffle_seed=2)
     q0 = meshgen.density_bump_state(marr, mach=MACH)
     m = rans.mesh.from_arrays(marr)
+    if args.implicit and args.implicit_batch > 0:
+        # implicit iterations of a batch of subsonic polar-sweep cases from freestream
+        cases = [c for c in meshgen.polar_sweep_cases(256, seed=4) if c["mach"] <= 0.5 and c["aoa_deg"] <= 8.0]
+        cases = cases[:args.implicit_batch]
+        meshes = [rans.mesh.from_arrays(c["mesh"]) for c in cases]
+        for precision in args.precision.split(","):
+            sts = []
+            for c in cases:
+                st = rans.Settings().set("solver", "implicit").set("precision", precision).set("start_cfl", 40.0)
+                st.set("slope_cfl", 50.0).set("max_cfl", 100.0).set("krylov_graph", 0 if args.krylov_host_loop else 1)
+                st.set_bc("farfield", "farfield", 1.0, c["mach"], c["aoa_deg"] * 0.01745, 1.0).set_bc("wall", "slip-wall")
+                sts.append(st)
+            b = rans.Batch(meshes, sts)
+            b.init()
+            b.iterate(args.steps, raise_nonfinite=False)
+            print(json.dumps({"implicit_batch": precision, "cases": len(cases), "cells": b.n_cells_total(),
+                              "iterations": args.steps, "krylov_last_iteration": int(b.linear_iterations()[0]),
+                              "device_s": b.last_device_seconds()}))
+            del b
+        return
     if args.implicit:
         # two implicit iterations on the 128 x 128 airfoil O-mesh from freestream, CFL 40
         am = rans.mesh.from_arrays(meshgen.airfoil_omesh(128, 128, split=False))
         for precision in args.precision.split(","):
             st = rans.Settings().set("solver", "implicit").set("precision", precision).set("start_cfl", 40.0)
+            st.set("krylov_graph", 0 if args.krylov_host_loop else 1)
             st.set_bc("farfield", "farfield", 1.0, 0.5, 1.25 * 0.01745, 1.0).set_bc("wall", "slip-wall")
             g = rans.Solver(am, st)
             g.init()
@@ -589,6 +610,10 @@ def main():
     ap.add_argument("--adjoint", action="store_true", help="--lean: FP64 residual vJP calls instead of iterations")
     ap.add_argument("--implicit", action="store_true",
                     help="--lean: implicit iterations on the 128x128 airfoil O-mesh (--steps of them)")
+    ap.add_argument("--implicit-batch", type=int, default=0,
+                    help="--lean --implicit: a batch of this many subsonic polar-sweep cases instead")
+    ap.add_argument("--krylov-host-loop", action="store_true",
+                    help="--lean --implicit: GMRES loops on the host, every kernel a plain launch (for ncu)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank = int(os.environ.get("RANK", "0"))

@@ -288,6 +288,9 @@ int afx_batch_set_farfield(afx_batch b, int c, const char* patch, double mach, d
 /* afx_autotune over the whole batch (state and qW put back). */
 int afx_batch_autotune(afx_batch b, int iters, char* variant, int cap, int* block, double* ms_per_iter);
 int afx_batch_last_device_seconds(afx_batch b, double* sec);
+/* Krylov iterations of each case in the last implicit iteration (0 for the
+ * explicit solver); iters holds n_cases entries. */
+int afx_batch_linear_iterations(afx_batch b, int* iters, int n_cases);
 
 #ifdef __cplusplus
 }

@@ -49,3 +49,18 @@ def test_implicit_iterate_and_stop_semantics(afx):
     r1 = g.iterate(3)
     r2 = g.iterate(3)
     assert np.isfinite(r1) and np.isfinite(r2) and r2 < r1
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32-mixed"])
+def test_krylov_host_loop_equals_the_solve_graph(afx, precision):
+    # krylov_graph = 0 drives the same kernels from a host loop: same Krylov
+    # iterations, bit-identical states
+    m = meshgen.airfoil_omesh(32, 24, split=False)
+    out = []
+    for graph in (1, 0):
+        g = gpu_solver(afx, m, BCS, precision, solver="implicit", start_cfl=40.0, krylov_graph=graph)
+        g.init()
+        g.iterate(3)
+        out.append((g.get_q(), g.linear_iterations()))
+    assert out[0][1] == out[1][1] and out[0][1] > 0
+    assert np.array_equal(out[0][0], out[1][0])
