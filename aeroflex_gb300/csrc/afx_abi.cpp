@@ -37,7 +37,7 @@ void enqueue_wall_dist(int nc, const double* cx, const double* cy, int nw, const
                        double* out, cudaStream_t s);
 struct ImplicitEngine;
 ImplicitEngine* implicit_create(const StepArgs& a, bool f32, bool graph, const std::vector<int>& colors,
-                                cudaStream_t s);
+                                const int* cslot, const int* cnbr, cudaStream_t s);
 void implicit_destroy(ImplicitEngine* e);
 void implicit_fill(ImplicitEngine* e, const StepArgs& a, int p, cudaStream_t s);
 int implicit_solve_update(ImplicitEngine* e, const StepArgs& a, int p, const double* b, double relax,
@@ -1164,7 +1164,8 @@ static std::unique_ptr<afx_solver_s> make_solver(const HostMesh& m, const Device
                 color[i] = c;
             }
             s->imp_b = s->dalloc(N * 32);
-            s->imp = implicit_create(s->A64(), !s->fp64, st.krylov_graph, color, s->stream);
+            s->imp = implicit_create(s->A64(), !s->fp64, st.krylov_graph, color, L.cslot.data(), L.cnbr.data(),
+                                     s->stream);
         }
         s->d_stage.alloc(N * 32);
         AFX_CUDA(cudaHostAlloc((void**)&s->h_stage, N * 32, cudaHostAllocDefault));

@@ -195,22 +195,93 @@ __global__ void __launch_bounds__(128) k_imp_jac(const KM<double> m, const int n
     }
 }
 
-// Diagonal block A/dt I + sum (own: J, other: -K) and its inverse (Gauss-
-// Jordan with partial pivoting, in double).
+// Row layout of the linear system.  Rows are grouped by colour (the cells
+// of a colour in device order), so a colour of the Gauss-Seidel sweep is a
+// contiguous range of rows and every per-row access is coalesced.  A row's
+// four off-diagonal blocks (ELL slots: the cell's face slots) carry the sign
+// of the cell's side.
+struct Ell {
+    const int* perm;      // [N] device cell of row p
+    const int4* col;      // [N] row of the neighbour in each slot, -1: none
+    const int4* face;     // [N] signed face of each slot (cslot convention), 0: none
+    const int4* tr;       // [N] ELL index 4 q + s' of the transposed block of each slot
+    const int* case_row;  // [N] batch: case of row p, else null
+};
+
+// Off-diagonal blocks are interleaved across rows: 16-byte chunk c of slot
+// s of row p (c = the block's row for FP32, half-row for FP64) is chunk
+// (s * CPB + c) * N + p, so a warp's loads of one chunk are contiguous.
+template <class T> struct Ell16 { static constexpr int W = 16 / sizeof(T), CPB = 16 / W; };
 template <class T>
-__global__ void __launch_bounds__(128) k_imp_diag(const KM<double> m, const double* __restrict__ dt,
-                                                  const T* __restrict__ jf, T* __restrict__ dblk,
-                                                  T* __restrict__ dinv, int* __restrict__ singular,
-                                                  Ctrl* __restrict__ ctrl, const int* __restrict__ case_of,
-                                                  int* __restrict__ case_done, CaseCtrl* __restrict__ cctrl) {
+__device__ __forceinline__ size_t ell_at(const int N, const int p, const int s, const int k) {
+    constexpr int W = Ell16<T>::W, CPB = Ell16<T>::CPB;
+    return ((size_t)(s * CPB + k / W) * N + p) * W + (k % W);
+}
+// y += sgn * O x for the block of slot s of row p
+template <class T>
+__device__ __forceinline__ void ell_mv_add(const T* __restrict__ off, const int N, const int p, const int s,
+                                           const T* x, T* y, const T sgn);
+template <>
+__device__ __forceinline__ void ell_mv_add<float>(const float* __restrict__ off, const int N, const int p,
+                                                  const int s, const float* x, float* y, const float sgn) {
+    const float4* b = reinterpret_cast<const float4*>(off);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const float4 row = __ldg(&b[(size_t)(s * 4 + r) * N + p]);
+        float t = 0;
+        t += row.x * x[0];
+        t += row.y * x[1];
+        t += row.z * x[2];
+        t += row.w * x[3];
+        y[r] += sgn * t;
+    }
+}
+template <>
+__device__ __forceinline__ void ell_mv_add<double>(const double* __restrict__ off, const int N, const int p,
+                                                   const int s, const double* x, double* y, const double sgn) {
+    const double2* b = reinterpret_cast<const double2*>(off);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const double2 u = __ldg(&b[(size_t)(s * 8 + 2 * r) * N + p]);
+        const double2 v = __ldg(&b[(size_t)(s * 8 + 2 * r + 1) * N + p]);
+        double t = 0;
+        t += u.x * x[0];
+        t += u.y * x[1];
+        t += v.x * x[2];
+        t += v.y * x[3];
+        y[r] += sgn * t;
+    }
+}
+
+// Diagonal block A/dt I + sum (own: J, other: -K) of row p and its inverse
+// (Gauss-Jordan with partial pivoting, in double), and the row's
+// off-diagonal blocks (own: K, other: -J) from the face Jacobians.
+template <class T>
+__global__ void __launch_bounds__(128) k_imp_assemble(const KM<double> m, const Ell e, const double* __restrict__ dt,
+                                                      const T* __restrict__ jf, T* __restrict__ dblk,
+                                                      T* __restrict__ dinv, T* __restrict__ off,
+                                                      int* __restrict__ singular, Ctrl* __restrict__ ctrl,
+                                                      int* __restrict__ case_done, CaseCtrl* __restrict__ cctrl) {
     if (ctrl->done) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m.n_cells) return;
-    if (held(case_of, case_done, i)) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= m.n_cells) return;
+    const int i = __ldg(&e.perm[p]);
+    const int4 fsl = __ldg(&e.face[p]);
+    const int4 col = __ldg(&e.col[p]);
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+        const int fs = pick(fsl, s);
+        if (fs == 0 || pick(col, s) < 0) continue;
+        const int f = (fs > 0 ? fs : -fs) - 1;
+        const T* B = jf + 32 * (size_t)f + (fs > 0 ? 16 : 0);
+#pragma unroll
+        for (int k = 0; k < 16; ++k) off[ell_at<T>(m.n_cells, p, s, k)] = fs > 0 ? B[k] : -B[k];
+    }
+    if (held(e.case_row, case_done, p)) {
 #pragma unroll
         for (int k = 0; k < 16; ++k) {
-            dblk[16 * (size_t)i + k] = T((k % 5 == 0) ? 1 : 0);
-            dinv[16 * (size_t)i + k] = T((k % 5 == 0) ? 1 : 0);
+            dblk[16 * (size_t)p + k] = T((k % 5 == 0) ? 1 : 0);
+            dinv[16 * (size_t)p + k] = T((k % 5 == 0) ? 1 : 0);
         }
         return;
     }
@@ -218,10 +289,9 @@ __global__ void __launch_bounds__(128) k_imp_diag(const KM<double> m, const doub
     const double ad = __ldg(&m.area[i]) / __ldg(&dt[i]);
 #pragma unroll
     for (int k = 0; k < 16; ++k) D[k] = (k % 5 == 0) ? ad : 0.0;
-    const int4 sl = __ldg(&m.cslot[i]);
 #pragma unroll
     for (int s = 0; s < 4; ++s) {
-        const int fs = pick(sl, s);
+        const int fs = pick(fsl, s);
         if (fs == 0) continue;
         const int f = (fs > 0 ? fs : -fs) - 1;
         const T* B = jf + 32 * (size_t)f + (fs > 0 ? 0 : 16);
@@ -229,38 +299,38 @@ __global__ void __launch_bounds__(128) k_imp_diag(const KM<double> m, const doub
 #pragma unroll
         for (int k = 0; k < 16; ++k) D[k] += sg * (double)B[k];
     }
-    T* Do = dblk + 16 * (size_t)i;
+    T* Do = dblk + 16 * (size_t)p;
 #pragma unroll
     for (int k = 0; k < 16; ++k) Do[k] = (T)D[k];
     double I[16];
 #pragma unroll
     for (int k = 0; k < 16; ++k) I[k] = (k % 5 == 0) ? 1.0 : 0.0;
     for (int c = 0; c < 4; ++c) {
-        int p = c;
+        int pv = c;
         double best = fabs(D[4 * c + c]);
         for (int r = c + 1; r < 4; ++r)
             if (fabs(D[4 * r + c]) > best) {
                 best = fabs(D[4 * r + c]);
-                p = r;
+                pv = r;
             }
         if (!(best > 0)) {
             if (case_done) {
-                stop_case(case_of, case_done, cctrl, ctrl, i);
+                stop_case(e.case_row, case_done, cctrl, ctrl, p);
 #pragma unroll
-                for (int k = 0; k < 16; ++k) dinv[16 * (size_t)i + k] = T((k % 5 == 0) ? 1 : 0);
+                for (int k = 0; k < 16; ++k) dinv[16 * (size_t)p + k] = T((k % 5 == 0) ? 1 : 0);
             } else {
                 *singular = 1;
             }
             return;
         }
-        if (p != c)
+        if (pv != c)
             for (int k = 0; k < 4; ++k) {
                 double t = D[4 * c + k];
-                D[4 * c + k] = D[4 * p + k];
-                D[4 * p + k] = t;
+                D[4 * c + k] = D[4 * pv + k];
+                D[4 * pv + k] = t;
                 t = I[4 * c + k];
-                I[4 * c + k] = I[4 * p + k];
-                I[4 * p + k] = t;
+                I[4 * c + k] = I[4 * pv + k];
+                I[4 * pv + k] = t;
             }
         const double inv = 1.0 / D[4 * c + c];
         for (int k = 0; k < 4; ++k) {
@@ -276,7 +346,7 @@ __global__ void __launch_bounds__(128) k_imp_diag(const KM<double> m, const doub
             }
         }
     }
-    T* Io = dinv + 16 * (size_t)i;
+    T* Io = dinv + 16 * (size_t)p;
 #pragma unroll
     for (int k = 0; k < 16; ++k) Io[k] = (T)I[k];
 }
@@ -331,41 +401,41 @@ __device__ __forceinline__ void inv4(const double* A, double* I, int* singular) 
 }
 
 template <class T>
-__global__ void __launch_bounds__(128) k_imp_ilu(const KM<double> m, const T* __restrict__ jf,
-                                                 const T* __restrict__ dblk, const int* __restrict__ cells,
-                                                 const int n, const int color, const unsigned char* __restrict__ col,
-                                                 T* __restrict__ dinv, int* __restrict__ singular,
-                                                 const int* __restrict__ case_of, int* __restrict__ case_done,
+__global__ void __launch_bounds__(128) k_imp_ilu(const Ell e, const int N, const T* __restrict__ dblk,
+                                                 const T* __restrict__ off, const int c0, const int n,
+                                                 T* __restrict__ dinv,
+                                                 int* __restrict__ singular, int* __restrict__ case_done,
                                                  CaseCtrl* __restrict__ cctrl, Ctrl* __restrict__ ctrl) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
-    const int i = __ldg(&cells[t]);
-    if (held(case_of, case_done, i)) return;
+    const int p = c0 + t;
+    if (held(e.case_row, case_done, p)) return;
     double D[16];
 #pragma unroll
-    for (int k = 0; k < 16; ++k) D[k] = (double)dblk[16 * (size_t)i + k];
-    const int4 sl = __ldg(&m.cslot[i]);
-    const int4 nb = __ldg(&m.cnbr[i]);
+    for (int k = 0; k < 16; ++k) D[k] = (double)dblk[16 * (size_t)p + k];
+    const int4 col = __ldg(&e.col[p]);
+    const int4 tr = __ldg(&e.tr[p]);
 #pragma unroll 1
     for (int s = 0; s < 4; ++s) {
-        const int fs = pick(sl, s);
-        const int o = pick(nb, s);
-        if (fs == 0 || o < 0 || (int)__ldg(&col[o]) >= color) continue;
-        const int f = (fs > 0 ? fs : -fs) - 1;
-        const T* J = jf + 32 * (size_t)f;
-        const T* Oio = J + (fs > 0 ? 16 : 0);  // row i, column o
-        const T* Ooi = J + (fs > 0 ? 0 : 16);  // row o, column i
-        const double sio = fs > 0 ? 1.0 : -1.0, soi = -sio;
-        const T* Dinv_o = dinv + 16 * (size_t)o;
-        double Y[16];  // D~_o^-1 O_oi
+        const int q = pick(col, s);
+        if (q < 0 || q >= c0) continue;  // rows of lower colours precede c0
+        const int t2 = pick(tr, s);  // 4 q + s': the block of row q, column p
+        double Oio[16], Ooi[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            Oio[k] = (double)off[ell_at<T>(N, p, s, k)];
+            Ooi[k] = (double)off[ell_at<T>(N, t2 >> 2, t2 & 3, k)];
+        }
+        const T* Dinv_o = dinv + 16 * (size_t)q;
+        double Y[16];  // D~_q^-1 O_qp
 #pragma unroll
         for (int r = 0; r < 4; ++r)
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
                 double acc = 0;
 #pragma unroll
-                for (int k = 0; k < 4; ++k) acc += (double)Dinv_o[4 * r + k] * (double)Ooi[4 * k + c];
-                Y[4 * r + c] = soi * acc;
+                for (int k = 0; k < 4; ++k) acc += (double)Dinv_o[4 * r + k] * Ooi[4 * k + c];
+                Y[4 * r + c] = acc;
             }
 #pragma unroll
         for (int r = 0; r < 4; ++r)
@@ -373,8 +443,8 @@ __global__ void __launch_bounds__(128) k_imp_ilu(const KM<double> m, const T* __
             for (int c = 0; c < 4; ++c) {
                 double acc = 0;
 #pragma unroll
-                for (int k = 0; k < 4; ++k) acc += (double)Oio[4 * r + k] * Y[4 * k + c];
-                D[4 * r + c] -= sio * acc;
+                for (int k = 0; k < 4; ++k) acc += Oio[4 * r + k] * Y[4 * k + c];
+                D[4 * r + c] -= acc;
             }
     }
     double I[16];
@@ -382,91 +452,83 @@ __global__ void __launch_bounds__(128) k_imp_ilu(const KM<double> m, const T* __
     inv4(D, I, &sing);
     if (sing) {
         if (case_done) {
-            stop_case(case_of, case_done, cctrl, ctrl, i);
+            stop_case(e.case_row, case_done, cctrl, ctrl, p);
         } else {
             *singular = 1;
         }
         return;
     }
 #pragma unroll
-    for (int k = 0; k < 16; ++k) dinv[16 * (size_t)i + k] = (T)I[k];
+    for (int k = 0; k < 16; ++k) dinv[16 * (size_t)p + k] = (T)I[k];
 }
 
 // --------------------------------------------------------- linear algebra
-// y = M x (gather over each cell's faces, edge order)
+// y = M x over the rows (diagonal block, then the slots in face order)
 template <class T>
-__global__ void __launch_bounds__(256) k_imp_spmv(const KM<double> m, const T* __restrict__ jf,
-                                                  const T* __restrict__ dblk, const typename B4<T>::type* __restrict__ x,
+__global__ void __launch_bounds__(256) k_imp_spmv(const int n_rows, const Ell e, const T* __restrict__ dblk,
+                                                  const T* __restrict__ off,
+                                                  const typename B4<T>::type* __restrict__ x,
                                                   typename B4<T>::type* __restrict__ y, const int* __restrict__ stop,
-                                                  const int* __restrict__ case_of, const int* __restrict__ case_done) {
+                                                  const int* __restrict__ case_done) {
     if (stop && *stop) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m.n_cells) return;
-    if (held(case_of, case_done, i)) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n_rows) return;
+    if (held(e.case_row, case_done, p)) {
         const T z[4] = {0, 0, 0, 0};
-        stt(&y[i], z);
+        stt(&y[p], z);
         return;
     }
     T xi[4], yi[4] = {0, 0, 0, 0};
-    ldt(&x[i], xi);
-    bmv_add<T>(dblk + 16 * (size_t)i, xi, yi, T(1));
-    const int4 sl = __ldg(&m.cslot[i]);
-    const int4 nb = __ldg(&m.cnbr[i]);
+    ldt(&x[p], xi);
+    bmv_add<T>(dblk + 16 * (size_t)p, xi, yi, T(1));
+    const int4 col = __ldg(&e.col[p]);
 #pragma unroll
     for (int s = 0; s < 4; ++s) {
-        const int fs = pick(sl, s);
-        const int o = pick(nb, s);
-        if (fs == 0 || o < 0) continue;
-        const int f = (fs > 0 ? fs : -fs) - 1;
+        const int q = pick(col, s);
+        if (q < 0) continue;
         T xo[4];
-        ldt(&x[o], xo);
-        // row c0: K x_c1; row c1: -J x_c0
-        bmv_add<T>(jf + 32 * (size_t)f + (fs > 0 ? 16 : 0), xo, yi, fs > 0 ? T(1) : T(-1));
+        ldt(&x[q], xo);
+        ell_mv_add<T>(off, n_rows, p, s, xo, yi, T(1));
     }
-    stt(&y[i], yi);
+    stt(&y[p], yi);
 }
 
-// One colour of a block Gauss-Seidel sweep: x_i = D_i^-1 (r_i - sum O x_n).
-// r = rbase + (*rk) * stride when rk is given (the current Krylov vector).
-// In the forward sweep (fwd = this colour) only neighbours of lower colours
-// are read: the higher colours have no value yet (zero start).
+// One colour (rows c0 .. c0+n-1) of a block Gauss-Seidel sweep:
+// x_p = D_p^-1 (r_p - sum O x_q).  r = rbase + (*rk) * stride when rk is
+// given (the current Krylov vector).  In the forward sweep only rows of
+// lower colours (q < c0) are read: the higher colours have no value yet
+// (zero start).
 template <class T>
-__global__ void __launch_bounds__(256) k_imp_gs(const KM<double> m, const T* __restrict__ jf,
-                                                const T* __restrict__ dinv, const int* __restrict__ cells,
-                                                const int n, const T* __restrict__ rbase, const int* __restrict__ rk,
-                                                const long long stride, typename B4<T>::type* __restrict__ x,
-                                                const int* __restrict__ stop, const int* __restrict__ case_of,
-                                                const int* __restrict__ case_done,
-                                                const unsigned char* __restrict__ col, const int fwd) {
+__global__ void __launch_bounds__(256) k_imp_gs(const Ell e, const int N, const T* __restrict__ dinv,
+                                                const T* __restrict__ off, const int c0, const int n, const T* __restrict__ rbase,
+                                                const int* __restrict__ rk, const long long stride,
+                                                typename B4<T>::type* __restrict__ x, const int* __restrict__ stop,
+                                                const int* __restrict__ case_done, const bool fwd) {
     if (stop && *stop) return;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     const typename B4<T>::type* r =
         reinterpret_cast<const typename B4<T>::type*>(rbase + (rk ? (long long)*rk * stride : 0));
-    const int i = __ldg(&cells[t]);
-    if (held(case_of, case_done, i)) {
+    const int p = c0 + t;
+    if (held(e.case_row, case_done, p)) {
         const T z[4] = {0, 0, 0, 0};
-        stt(&x[i], z);
+        stt(&x[p], z);
         return;
     }
     T s[4];
-    ldt(&r[i], s);
-    const int4 sl = __ldg(&m.cslot[i]);
-    const int4 nb = __ldg(&m.cnbr[i]);
+    ldt(&r[p], s);
+    const int4 col = __ldg(&e.col[p]);
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        const int fs = pick(sl, k);
-        const int o = pick(nb, k);
-        if (fs == 0 || o < 0) continue;
-        if (fwd >= 0 && (int)__ldg(&col[o]) >= fwd) continue;
-        const int f = (fs > 0 ? fs : -fs) - 1;
+        const int q = pick(col, k);
+        if (q < 0 || (fwd && q >= c0)) continue;
         T xo[4];
-        ldt(&x[o], xo);
-        bmv_add<T>(jf + 32 * (size_t)f + (fs > 0 ? 16 : 0), xo, s, fs > 0 ? T(-1) : T(1));
+        ldt(&x[q], xo);
+        ell_mv_add<T>(off, N, p, k, xo, s, T(-1));
     }
     T xi[4] = {0, 0, 0, 0};
-    bmv_add<T>(dinv + 16 * (size_t)i, s, xi, T(1));
-    stt(&x[i], xi);
+    bmv_add<T>(dinv + 16 * (size_t)p, s, xi, T(1));
+    stt(&x[p], xi);
 }
 
 // Dot products against the Krylov basis v_0..v_{nv-1} (v_j = V + j*n) in
@@ -492,12 +554,14 @@ __device__ __forceinline__ void vsub(float4& w, const float h, const float4 v) {
 __device__ __forceinline__ void vsub(double2& w, const double h, const double2 v) {
     w.x -= h * v.x; w.y -= h * v.y;
 }
+__device__ __forceinline__ void vscale(float4& a, const float s) { a.x *= s; a.y *= s; a.z *= s; a.w *= s; }
+__device__ __forceinline__ void vscale(double2& a, const double s) { a.x *= s; a.y *= s; }
 
 constexpr int DOT_G = 8;  // threads of the last block per output
 static_assert(DOT_THREADS / DOT_G >= GM_M + 1, "one group per output");
 
 template <class T, int MODE>
-__global__ void __launch_bounds__(DOT_THREADS, 2) k_imp_dots(const int n, int nv, const int* __restrict__ nvk,
+__global__ void __launch_bounds__(DOT_THREADS, MODE == 1 ? 1 : 2) k_imp_dots(const int n, int nv, const int* __restrict__ nvk,
                                                           const T* __restrict__ V, T* __restrict__ w,
                                                           const double* __restrict__ hin, double* __restrict__ part,
                                                           unsigned* __restrict__ counter, double* __restrict__ out,
@@ -528,16 +592,21 @@ __global__ void __launch_bounds__(DOT_THREADS, 2) k_imp_dots(const int n, int nv
             for (int j = 0; j <= GM_M; ++j)
                 if (j < nv) acc[j] += vdot(Vv[(size_t)j * nc + i], wi);
         } else {
+            // MODE 1 keeps the basis chunks in registers for the second
+            // product (one block per SM; the loads of a chunk are all in
+            // flight at once)
+            VT vv[GM_M + 1];
 #pragma unroll
             for (int j = 0; j <= GM_M; ++j)
-                if (j < nv) vsub(wi, hs[j], Vv[(size_t)j * nc + i]);
+                if (j < nv) {
+                    vv[j] = Vv[(size_t)j * nc + i];
+                    vsub(wi, hs[j], vv[j]);
+                }
             wv[i] = wi;
             if (MODE == 1) {
-                // the basis chunks again, from L2 where they were just read (no
-                // new HBM traffic, and no registers held across the update)
 #pragma unroll
                 for (int j = 0; j <= GM_M; ++j)
-                    if (j < nv) acc[j] += vdot(__ldcg(&Vv[(size_t)j * nc + i]), wi);
+                    if (j < nv) acc[j] += vdot(vv[j], wi);
             } else {
                 acc[0] += vdot(wi, wi);
             }
@@ -588,15 +657,20 @@ __global__ void __launch_bounds__(DOT_THREADS, 2) k_imp_dots(const int n, int nv
 }
 
 // v = w * scale[0]; with vk given, v = vbase + (*vk) * n (the next Krylov vector)
+// (16-byte chunks; w and v may be the same vector)
 template <class T>
-__global__ void __launch_bounds__(256) k_imp_scale(const int n, const T* __restrict__ w, const double* __restrict__ scale,
-                                                   T* __restrict__ v, const int* __restrict__ vk,
-                                                   const int* __restrict__ stop) {
+__global__ void __launch_bounds__(256) k_imp_scale(const int n, const T* w, const double* __restrict__ scale, T* v,
+                                                   const int* __restrict__ vk, const int* __restrict__ stop) {
     if (stop && *stop) return;
+    using VT = typename Vec16<T>::type;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (vk) v += (long long)*vk * n;
     const T sc = (T)scale[0];
-    if (i < n) v[i] = w[i] * sc;
+    if (i < n / Vec16<T>::W) {
+        VT a = reinterpret_cast<const VT*>(w)[i];
+        vscale(a, sc);
+        reinterpret_cast<VT*>(v)[i] = a;
+    }
 }
 
 // Arnoldi step j = c->k, classical Gram-Schmidt twice: h1 (first pass) and
@@ -695,12 +769,21 @@ __global__ void __launch_bounds__(256) k_imp_addx(const int n, const T* __restri
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) x[i] += (double)z[i];
 }
+// r = b - y, b in device cell order, r and y in row order (4N long)
 template <class T>
-__global__ void __launch_bounds__(256) k_imp_resid(const int n, const double* __restrict__ b, const T* __restrict__ y,
+__global__ void __launch_bounds__(256) k_imp_resid(const int n, const double* __restrict__ b,
+                                                   const int* __restrict__ perm, const T* __restrict__ y,
                                                    T* __restrict__ r, const int* __restrict__ stop) {
     if (stop && *stop) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) r[i] = (T)(b[i] - (double)y[i]);
+    if (i < n) r[i] = (T)(b[4 * (size_t)__ldg(&perm[i >> 2]) + (i & 3)] - (double)y[i]);
+}
+// t = b in row order (b in device cell order)
+template <class T>
+__global__ void __launch_bounds__(256) k_imp_gather_b(const int n, const double* __restrict__ b,
+                                                      const int* __restrict__ perm, T* __restrict__ t) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) t[i] = (T)b[4 * (size_t)__ldg(&perm[i >> 2]) + (i & 3)];
 }
 template <class T>
 __global__ void __launch_bounds__(256) k_imp_cast(const int n, const double* __restrict__ x, T* __restrict__ t,
@@ -712,12 +795,22 @@ __global__ void __launch_bounds__(256) k_imp_cast(const int n, const double* __r
 
 // q += relax * dq over the real cells; dq also becomes qW (the reference's
 // qW holds the last linear solution, read by get_uniform_residual)
-__global__ void __launch_bounds__(256) k_imp_update(const int n, const double* __restrict__ dq, const double relax,
+// (dq in row order, q and qW in device cell order)
+__global__ void __launch_bounds__(256) k_imp_update(const int n, const double* __restrict__ dq,
+                                                    const int* __restrict__ perm, const double relax,
                                                     double* __restrict__ q, double* __restrict__ qW) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    q[i] += dq[i] * relax;
-    qW[i] = dq[i];
+    const size_t j = 4 * (size_t)__ldg(&perm[i >> 2]) + (i & 3);
+    q[j] += dq[i] * relax;
+    qW[j] = dq[i];
+}
+
+// case of each row (batch)
+__global__ void k_imp_case_rows(const int n, const int* __restrict__ perm, const int* __restrict__ case_of,
+                                int* __restrict__ case_row) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < n) case_row[p] = case_of[perm[p]];
 }
 
 // GMRES initialisation of a cycle: g = (beta, 0, ...), stop = beta <= tol
@@ -768,11 +861,16 @@ struct ImplicitEngine {
     int N = 0, F = 0, n4 = 0;
     int n_colors = 0;
     std::vector<int> color_ptr;
-    void* jf = nullptr;
-    void* dblk = nullptr;
-    void* dinv = nullptr;
-    int* color_cells = nullptr;
-    unsigned char* color_of = nullptr;  // colour of each cell
+    void* jf = nullptr;    // face Jacobians J, K (16 T each)
+    void* dblk = nullptr;  // diagonal block of each row
+    void* dinv = nullptr;  // its ILU(0) inverse
+    void* off = nullptr;   // off-diagonal blocks, 4 slots per row
+    int* perm = nullptr;   // device cell of each row (rows grouped by colour)
+    int4* ell_col = nullptr;
+    int4* ell_face = nullptr;
+    int4* ell_tr = nullptr;
+    int* case_row = nullptr;          // batch: case of each row
+    const int* case_row_src = nullptr;  // the case_of it was formed from
     int* singular = nullptr;
     void* V = nullptr;     // (GM_M+1) x 4N
     void* w = nullptr;     // 4N
@@ -785,38 +883,66 @@ struct ImplicitEngine {
     cudaGraphExec_t cyc[2] = {nullptr, nullptr};  // cyc[0]: the GMRES solve graph
     cudaStream_t s2 = nullptr, s3 = nullptr;      // capture streams of the loop bodies
     const void* cyc_b = nullptr;                  // right-hand side the graphs were captured with
-    int nbd = 0;
+    int nbd = 0, nbd1 = 0;  // blocks of the dot passes (two / one per SM)
     dev::GmresCtl* ctl = nullptr;
     dev::GmresCtl* h_ctl = nullptr;
     int last_iters = 0;
 
     size_t ts() const { return f32 ? 4 : 8; }
+    dev::Ell ell() const { return dev::Ell{perm, ell_col, ell_face, ell_tr, case_row}; }
 };
 
+// cslot, cnbr: the host copies of the cell slots (4 per cell, device order)
 ImplicitEngine* implicit_create(const StepArgs& a, bool f32, bool graph, const std::vector<int>& colors,
-                                cudaStream_t s) {
+                                const int* cslot, const int* cnbr, cudaStream_t s) {
     auto* e = new ImplicitEngine();
     e->f32 = f32;
     e->graph = graph;
     e->N = a.n_cells;
     e->F = a.n_faces;
     e->n4 = 4 * a.n_cells;
+    const int N = e->N;
     int nc = 0;
     for (int c : colors) nc = std::max(nc, c + 1);
     e->n_colors = nc;
     e->color_ptr.assign(nc + 1, 0);
     for (int c : colors) e->color_ptr[c + 1]++;
     for (int c = 0; c < nc; ++c) e->color_ptr[c + 1] += e->color_ptr[c];
-    std::vector<int> cells(colors.size()), fill(e->color_ptr.begin(), e->color_ptr.end() - 1);
-    for (int i = 0; i < (int)colors.size(); ++i) cells[fill[colors[i]]++] = i;
+    // rows: the cells of colour 0, then colour 1, ..., each in device order
+    std::vector<int> perm(N), rowof(N), fill(e->color_ptr.begin(), e->color_ptr.end() - 1);
+    for (int i = 0; i < N; ++i) perm[fill[colors[i]]++] = i;
+    for (int p = 0; p < N; ++p) rowof[perm[p]] = p;
+    std::vector<int> ecol(4 * (size_t)N, -1), eface(4 * (size_t)N, 0), etr(4 * (size_t)N, -1);
+    for (int p = 0; p < N; ++p) {
+        const int i = perm[p];
+        for (int k = 0; k < 4; ++k) {
+            const int fs = cslot[4 * (size_t)i + k], o = cnbr[4 * (size_t)i + k];
+            eface[4 * (size_t)p + k] = fs;
+            if (fs != 0 && o >= 0) ecol[4 * (size_t)p + k] = rowof[o];
+        }
+    }
+    for (int p = 0; p < N; ++p)
+        for (int k = 0; k < 4; ++k) {
+            const int q = ecol[4 * (size_t)p + k];
+            if (q < 0) continue;
+            const int f = std::abs(eface[4 * (size_t)p + k]);
+            for (int k2 = 0; k2 < 4; ++k2)
+                if (std::abs(eface[4 * (size_t)q + k2]) == f) etr[4 * (size_t)p + k] = 4 * q + k2;
+            if (etr[4 * (size_t)p + k] < 0) throw Error(7, "implicit solver: face slots are not symmetric");
+        }
     const size_t T = e->ts();
     auto chk = [](cudaError_t r) {
         if (r != cudaSuccess) throw Error(7, std::string("implicit solver: ") + cudaGetErrorString(r));
     };
+    const size_t N1 = std::max(N, 1);
     chk(cudaMalloc(&e->jf, (size_t)e->F * 32 * T));
-    chk(cudaMalloc(&e->dblk, (size_t)e->N * 16 * T));
-    chk(cudaMalloc(&e->dinv, (size_t)e->N * 16 * T));
-    chk(cudaMalloc((void**)&e->color_cells, std::max<size_t>(cells.size(), 1) * sizeof(int)));
+    chk(cudaMalloc(&e->dblk, N1 * 16 * T));
+    chk(cudaMalloc(&e->dinv, N1 * 16 * T));
+    chk(cudaMalloc(&e->off, N1 * 64 * T));
+    chk(cudaMalloc((void**)&e->perm, N1 * sizeof(int)));
+    chk(cudaMalloc((void**)&e->ell_col, N1 * sizeof(int4)));
+    chk(cudaMalloc((void**)&e->ell_face, N1 * sizeof(int4)));
+    chk(cudaMalloc((void**)&e->ell_tr, N1 * sizeof(int4)));
     chk(cudaMalloc((void**)&e->singular, sizeof(int)));
     chk(cudaMalloc(&e->V, (size_t)(dev::GM_M + 1) * e->n4 * T));
     chk(cudaMalloc(&e->w, (size_t)e->n4 * T));
@@ -828,21 +954,19 @@ ImplicitEngine* implicit_create(const StepArgs& a, bool f32, bool graph, const s
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_id);
     // two resident blocks per SM at most: the last block then sums few partials
     e->nbd = std::max(1, std::min(2 * std::max(sms, 1), nb_(e->n4, dev::DOT_THREADS * 4)));
+    e->nbd1 = std::max(1, std::min(std::max(sms, 1), e->nbd));
     chk(cudaMalloc((void**)&e->part, (size_t)e->nbd * (dev::GM_M + 1) * 8));
     chk(cudaMalloc((void**)&e->small, (2 * (dev::GM_M + 1) + 2) * 8));
     chk(cudaMalloc((void**)&e->counter, sizeof(unsigned)));
     chk(cudaMemsetAsync(e->counter, 0, sizeof(unsigned), s));
     chk(cudaMalloc((void**)&e->ctl, sizeof(dev::GmresCtl)));
     chk(cudaHostAlloc((void**)&e->h_ctl, sizeof(dev::GmresCtl), cudaHostAllocDefault));
-    chk(cudaMemcpyAsync(e->color_cells, cells.data(), cells.size() * sizeof(int), cudaMemcpyHostToDevice, s));
-    {
-        if (nc > 255) throw Error(7, "implicit solver: too many colours");
-        std::vector<unsigned char> col(colors.begin(), colors.end());
-        chk(cudaMalloc((void**)&e->color_of, std::max<size_t>(col.size(), 1)));
-        chk(cudaMemcpyAsync(e->color_of, col.data(), col.size(), cudaMemcpyHostToDevice, s));
-        chk(cudaStreamSynchronize(s));
-    }
+    chk(cudaMemcpyAsync(e->perm, perm.data(), (size_t)N * sizeof(int), cudaMemcpyHostToDevice, s));
+    chk(cudaMemcpyAsync(e->ell_col, ecol.data(), (size_t)N * sizeof(int4), cudaMemcpyHostToDevice, s));
+    chk(cudaMemcpyAsync(e->ell_face, eface.data(), (size_t)N * sizeof(int4), cudaMemcpyHostToDevice, s));
+    chk(cudaMemcpyAsync(e->ell_tr, etr.data(), (size_t)N * sizeof(int4), cudaMemcpyHostToDevice, s));
     chk(cudaMemsetAsync(e->jf, 0, (size_t)e->F * 32 * T, s));
+    chk(cudaMemsetAsync(e->off, 0, N1 * 64 * T, s));
     e->h_ctl->graph = graph ? 1 : 0;
     chk(cudaMemcpyAsync(&e->ctl->graph, &e->h_ctl->graph, sizeof(int), cudaMemcpyHostToDevice, s));
     chk(cudaStreamSynchronize(s));
@@ -855,9 +979,9 @@ void implicit_destroy(ImplicitEngine* e) {
         if (e->cyc[k]) cudaGraphExecDestroy(e->cyc[k]);
     if (e->s2) cudaStreamDestroy(e->s2);
     if (e->s3) cudaStreamDestroy(e->s3);
-    if (e->color_of) cudaFree(e->color_of);
-    for (void* p : {e->jf, e->dblk, e->dinv, (void*)e->color_cells, (void*)e->singular, e->V, e->w, e->z, e->t,
-                    (void*)e->x, (void*)e->part, (void*)e->small, (void*)e->ctl, (void*)e->counter})
+    for (void* p : {e->jf, e->dblk, e->dinv, e->off, (void*)e->perm, (void*)e->ell_col, (void*)e->ell_face,
+                    (void*)e->ell_tr, (void*)e->case_row, (void*)e->singular, e->V, e->w, e->z, e->t, (void*)e->x,
+                    (void*)e->part, (void*)e->small, (void*)e->ctl, (void*)e->counter})
         if (p) cudaFree(p);
     if (e->h_ctl) cudaFreeHost(e->h_ctl);
     delete e;
@@ -865,54 +989,46 @@ void implicit_destroy(ImplicitEngine* e) {
 
 // fillRhoLHS (solver.h:1016-1090): dt from the state of parity p at the CFL
 // in a.cfl, face Jacobians, diagonal blocks and their inverses.
+namespace {
+template <class T>
+void fill_t(ImplicitEngine* e, const StepArgs& a, const dev::KM<double>& m, const dev::d4* q, cudaStream_t s) {
+    using namespace dev;
+    const int nf = nb_(a.n_faces, 128), nc = nb_(a.n_cells, 128);
+    if (a.visc == 1)
+        k_imp_jac<T, 1><<<nf, 128, 0, s>>>(m, a.n_faces, q, (const d4*)a.gx, (const d4*)a.gy, (T*)e->jf, a.ctrl);
+    else
+        k_imp_jac<T, 0><<<nf, 128, 0, s>>>(m, a.n_faces, q, (const d4*)a.gx, (const d4*)a.gy, (T*)e->jf, a.ctrl);
+    const Ell el = e->ell();
+    k_imp_assemble<T><<<nc, 128, 0, s>>>(m, el, (const double*)a.dt, (const T*)e->jf, (T*)e->dblk, (T*)e->dinv,
+                                         (T*)e->off, e->singular, a.ctrl, a.case_done, a.cctrl);
+    for (int c = 1; c < e->n_colors; ++c) {
+        const int c0 = e->color_ptr[c], cn = e->color_ptr[c + 1] - c0;
+        if (cn > 0)
+            k_imp_ilu<T><<<nb_(cn, 128), 128, 0, s>>>(el, e->N, (const T*)e->dblk, (const T*)e->off, c0, cn,
+                                                      (T*)e->dinv, e->singular, a.case_done, a.cctrl, a.ctrl);
+    }
+}
+}  // namespace
+
 void implicit_fill(ImplicitEngine* e, const StepArgs& a0, int p, cudaStream_t s) {
     using namespace dev;
     StepArgs a = a0;
     a.variant = 0;  // the prep that also forms dt
     a.second = 0;   // gradients only when viscous (solver.h:1023-1026)
     a.need_grad = a.visc == 1 ? 1 : 0;
+    if (a.case_of && e->case_row_src != a.case_of) {
+        // a batch: the case of each row, formed once
+        if (!e->case_row && cudaMalloc((void**)&e->case_row, (size_t)std::max(e->N, 1) * sizeof(int)) != cudaSuccess)
+            throw Error(7, "implicit solver: out of device memory");
+        k_imp_case_rows<<<nb_(e->N, 256), 256, 0, s>>>(e->N, e->perm, a.case_of, e->case_row);
+        e->case_row_src = a.case_of;
+    }
     const KM<double> m = make_km<double>(a);
     launch_prep<double, double>(a, m, (const d4*)a.qm[p], s);
     cudaMemsetAsync(e->singular, 0, sizeof(int), s);
     const d4* q = (const d4*)a.qm[p];
-    const int nf = nb_(a.n_faces, 128), nc = nb_(a.n_cells, 128);
-    if (e->f32) {
-        if (a.visc == 1)
-            k_imp_jac<float, 1><<<nf, 128, 0, s>>>(m, a.n_faces, q, (const d4*)a.gx, (const d4*)a.gy, (float*)e->jf,
-                                                   a.ctrl);
-        else
-            k_imp_jac<float, 0><<<nf, 128, 0, s>>>(m, a.n_faces, q, (const d4*)a.gx, (const d4*)a.gy, (float*)e->jf,
-                                                   a.ctrl);
-        k_imp_diag<float><<<nc, 128, 0, s>>>(m, (const double*)a.dt, (const float*)e->jf, (float*)e->dblk,
-                                             (float*)e->dinv, e->singular, a.ctrl, a.case_of, a.case_done,
-                                             a.cctrl);
-        for (int c = 1; c < e->n_colors; ++c) {
-            const int c0 = e->color_ptr[c], cn = e->color_ptr[c + 1] - c0;
-            if (cn > 0)
-                k_imp_ilu<float><<<nb_(cn, 128), 128, 0, s>>>(m, (const float*)e->jf, (const float*)e->dblk,
-                                                              e->color_cells + c0, cn, c, e->color_of,
-                                                              (float*)e->dinv, e->singular, a.case_of,
-                                                              a.case_done, a.cctrl, a.ctrl);
-        }
-    } else {
-        if (a.visc == 1)
-            k_imp_jac<double, 1><<<nf, 128, 0, s>>>(m, a.n_faces, q, (const d4*)a.gx, (const d4*)a.gy,
-                                                    (double*)e->jf, a.ctrl);
-        else
-            k_imp_jac<double, 0><<<nf, 128, 0, s>>>(m, a.n_faces, q, (const d4*)a.gx, (const d4*)a.gy,
-                                                    (double*)e->jf, a.ctrl);
-        k_imp_diag<double><<<nc, 128, 0, s>>>(m, (const double*)a.dt, (const double*)e->jf, (double*)e->dblk,
-                                              (double*)e->dinv, e->singular, a.ctrl, a.case_of,
-                                              a.case_done, a.cctrl);
-        for (int c = 1; c < e->n_colors; ++c) {
-            const int c0 = e->color_ptr[c], cn = e->color_ptr[c + 1] - c0;
-            if (cn > 0)
-                k_imp_ilu<double><<<nb_(cn, 128), 128, 0, s>>>(m, (const double*)e->jf, (const double*)e->dblk,
-                                                               e->color_cells + c0, cn, c, e->color_of,
-                                                               (double*)e->dinv, e->singular, a.case_of,
-                                                               a.case_done, a.cctrl, a.ctrl);
-        }
-    }
+    if (e->f32) fill_t<float>(e, a, m, q, s);
+    else fill_t<double>(e, a, m, q, s);
 }
 
 namespace {
@@ -928,8 +1044,12 @@ struct Ops {
     T* vec(int j) const { return (T*)e->V + (size_t)j * e->n4; }
     int* stop() const { return &e->ctl->stop; }
     void spmv(const T* x, T* y, const int* st) const {
-        dev::k_imp_spmv<T><<<nb_(e->N, 256), 256, 0, s>>>(m, (const T*)e->jf, (const T*)e->dblk, (const V4*)x, (V4*)y,
-                                                          st, a.case_of, a.case_done);
+        dev::k_imp_spmv<T><<<nb_(e->N, 256), 256, 0, s>>>(e->N, e->ell(), (const T*)e->dblk, (const T*)e->off,
+                                                          (const V4*)x, (V4*)y, st, a.case_done);
+    }
+    // t = b in row order
+    void gather_b(const double* b, T* t) const {
+        dev::k_imp_gather_b<T><<<nb_(e->n4, 256), 256, 0, s>>>(e->n4, b, e->perm, t);
     }
     // one symmetric multicolour block Gauss-Seidel sweep from x = 0 (the
     // ILU(0) factors in the colour ordering); the input is r, or the current
@@ -942,16 +1062,22 @@ struct Ops {
             const int c = k < C ? k : 2 * C - 2 - k;
             const int c0 = e->color_ptr[c], cn = e->color_ptr[c + 1] - c0;
             if (cn == 0) continue;
-            dev::k_imp_gs<T><<<nb_(cn, 256), 256, 0, s>>>(m, (const T*)e->jf, (const T*)e->dinv, e->color_cells + c0,
-                                                          cn, r, rk, (long long)e->n4, (V4*)x, st, a.case_of,
-                                                          a.case_done, e->color_of, k < C ? c : -1);
+            dev::k_imp_gs<T><<<nb_(cn, 256), 256, 0, s>>>(e->ell(), e->N, (const T*)e->dinv, (const T*)e->off, c0,
+                                                          cn, r, rk, (long long)e->n4, (V4*)x, st, a.case_done,
+                                                          k < C);
         }
     }
     // MODE 0: out = V^T w; 1: w -= V hin, out = V^T w; 2: w -= V hin, out = w.w
     template <int MODE>
     void dots(int nv, const int* nvk, const T* V, T* w, const double* hin, double* out, const int* st) const {
-        dev::k_imp_dots<T, MODE><<<e->nbd, dev::DOT_THREADS, 0, s>>>(e->n4, nv, nvk, V, w, hin, e->part, e->counter,
-                                                                   out, st);
+        // MODE 1 holds one block per SM
+        const int g = MODE == 1 ? e->nbd1 : e->nbd;
+        dev::k_imp_dots<T, MODE><<<g, dev::DOT_THREADS, 0, s>>>(e->n4, nv, nvk, V, w, hin, e->part, e->counter, out,
+                                                              st);
+    }
+    // v = w * scale (k given: v = V_{*k})
+    void scale(const T* w, const double* sc, T* v, const int* k, const int* st) const {
+        dev::k_imp_scale<T><<<nb_(e->n4 / (16 / (int)sizeof(T)), 256), 256, 0, s>>>(e->n4, w, sc, v, k, st);
     }
 };
 
@@ -1003,10 +1129,10 @@ cudaGraphExec_t build_gmres_graph(ImplicitEngine* e, const Ops<T>& o0, const dou
     Ops<T> o(e, o0.a, s);
     T* v0 = o.vec(0);
     cudaMemsetAsync(e->x, 0, (size_t)n * 8, s);
-    k_imp_cast<T><<<nb_(n, 256), 256, 0, s>>>(n, b, v0, nullptr);
+    o.gather_b(b, v0);
     o.template dots<0>(1, nullptr, v0, v0, nullptr, ww, nullptr);
     k_imp_cycle_init<<<1, 1, 0, s>>>(e->ctl, ww, scale, 1, 1e-2, max_iters);
-    k_imp_scale<T><<<nb_(n, 256), 256, 0, s>>>(n, v0, scale, v0, nullptr, stop);
+    o.scale(v0, scale, v0, nullptr, stop);
     cudaGraph_t body_out = add_while(s, &hout);
     cudaMemcpyAsync(e->h_ctl, e->ctl, sizeof(GmresCtl), cudaMemcpyDeviceToHost, s);
     cudaGraph_t G;
@@ -1024,10 +1150,10 @@ cudaGraphExec_t build_gmres_graph(ImplicitEngine* e, const Ops<T>& o0, const dou
         k_imp_outer_check<<<1, 1, 0, s2>>>(e->ctl);
         k_imp_cast<T><<<nb_(n, 256), 256, 0, s2>>>(n, e->x, (T*)e->t, halt);
         q.spmv((const T*)e->t, (T*)e->w, halt);
-        k_imp_resid<T><<<nb_(n, 256), 256, 0, s2>>>(n, b, (const T*)e->w, q.vec(0), halt);
+        k_imp_resid<T><<<nb_(n, 256), 256, 0, s2>>>(n, b, e->perm, (const T*)e->w, q.vec(0), halt);
         q.template dots<0>(1, nullptr, q.vec(0), q.vec(0), nullptr, ww, halt);
         k_imp_cycle_init<<<1, 1, 0, s2>>>(e->ctl, ww, scale, 0, 1e-2, max_iters);
-        k_imp_scale<T><<<nb_(n, 256), 256, 0, s2>>>(n, q.vec(0), scale, q.vec(0), nullptr, halt);
+        q.scale(q.vec(0), scale, q.vec(0), nullptr, halt);
         chk(cudaStreamEndCapture(s2, &body_out));
         // Arnoldi step k: z = P^-1 v_k, w = M z, CGS2 against v_0..v_k, rotations, v_{k+1}
         chk(cudaStreamBeginCaptureToGraph(s3, body_in, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
@@ -1040,7 +1166,7 @@ cudaGraphExec_t build_gmres_graph(ImplicitEngine* e, const Ops<T>& o0, const dou
         r.template dots<1>(0, kptr, r.vec(0), (T*)e->w, h1, h2, stop);
         r.template dots<2>(0, kptr, r.vec(0), (T*)e->w, h2, ww, stop);
         k_imp_arnoldi<<<1, 32, 0, s3>>>(e->ctl, h1, h2, ww, scale);
-        k_imp_scale<T><<<nb_(n, 256), 256, 0, s3>>>(n, (const T*)e->w, scale, r.vec(0), kptr, stop);
+        r.scale((const T*)e->w, scale, r.vec(0), kptr, stop);
         chk(cudaStreamEndCapture(s3, &body_in));
     }
     cudaGraphExec_t ex;
@@ -1078,10 +1204,10 @@ int gmres_host_loop(ImplicitEngine* e, const StepArgs& a, const double* b, cudaS
     };
     T* v0 = o.vec(0);
     cudaMemsetAsync(e->x, 0, (size_t)n * 8, s);
-    k_imp_cast<T><<<nb_(n, 256), 256, 0, s>>>(n, b, v0, nullptr);
+    o.gather_b(b, v0);
     o.template dots<0>(1, nullptr, v0, v0, nullptr, ww, nullptr);
     k_imp_cycle_init<<<1, 1, 0, s>>>(e->ctl, ww, scale, 1, 1e-2, max_iters);
-    k_imp_scale<T><<<nb_(n, 256), 256, 0, s>>>(n, v0, scale, v0, nullptr, stop);
+    o.scale(v0, scale, v0, nullptr, stop);
     read_ctl();
     if (!e->h_ctl->stop) {
         for (;;) {
@@ -1094,7 +1220,7 @@ int gmres_host_loop(ImplicitEngine* e, const StepArgs& a, const double* b, cudaS
                 o.template dots<1>(0, kptr, o.vec(0), (T*)e->w, h1, h2, stop);
                 o.template dots<2>(0, kptr, o.vec(0), (T*)e->w, h2, ww, stop);
                 k_imp_arnoldi<<<1, 32, 0, s>>>(e->ctl, h1, h2, ww, scale);
-                k_imp_scale<T><<<nb_(n, 256), 256, 0, s>>>(n, (const T*)e->w, scale, o.vec(0), kptr, stop);
+                o.scale((const T*)e->w, scale, o.vec(0), kptr, stop);
             }
             k_imp_solve_y<<<1, 32, 0, s>>>(e->ctl);
             k_imp_lincomb<T><<<nb_(n, 256), 256, 0, s>>>(n, o.vec(0), e->ctl, (T*)e->t);
@@ -1103,10 +1229,10 @@ int gmres_host_loop(ImplicitEngine* e, const StepArgs& a, const double* b, cudaS
             k_imp_outer_check<<<1, 1, 0, s>>>(e->ctl);
             k_imp_cast<T><<<nb_(n, 256), 256, 0, s>>>(n, e->x, (T*)e->t, halt);
             o.spmv((const T*)e->t, (T*)e->w, halt);
-            k_imp_resid<T><<<nb_(n, 256), 256, 0, s>>>(n, b, (const T*)e->w, o.vec(0), halt);
+            k_imp_resid<T><<<nb_(n, 256), 256, 0, s>>>(n, b, e->perm, (const T*)e->w, o.vec(0), halt);
             o.template dots<0>(1, nullptr, o.vec(0), o.vec(0), nullptr, ww, halt);
             k_imp_cycle_init<<<1, 1, 0, s>>>(e->ctl, ww, scale, 0, 1e-2, max_iters);
-            k_imp_scale<T><<<nb_(n, 256), 256, 0, s>>>(n, o.vec(0), scale, o.vec(0), nullptr, halt);
+            o.scale(o.vec(0), scale, o.vec(0), nullptr, halt);
             read_ctl();
             if (e->h_ctl->halt) break;
         }
@@ -1146,7 +1272,8 @@ int implicit_solve_update(ImplicitEngine* e, const StepArgs& a, int p, const dou
     cudaStreamSynchronize(s);
     if (sing) return -1;
     const int it = e->f32 ? gmres<float>(e, a, b, s, 500) : gmres<double>(e, a, b, s, 500);
-    dev::k_imp_update<<<nb_(e->n4, 256), 256, 0, s>>>(e->n4, e->x, relax, (double*)a.qm[p], (double*)a.Rq);
+    dev::k_imp_update<<<nb_(e->n4, 256), 256, 0, s>>>(e->n4, e->x, e->perm, relax, (double*)a.qm[p],
+                                                      (double*)a.Rq);
     e->last_iters = it;
     return it;
 }

@@ -896,7 +896,24 @@ __global__ void __launch_bounds__(256) k_uniform(const KM<T> m, const V4<S>* __r
 // every case): one block per case sums the per-cell squares of its cells in
 // a fixed order.  A case that stops is marked in case_done (its cells then
 // hold their state); the whole run stops when every case has.
-static __global__ void __launch_bounds__(256) k_case_control(const double* __restrict__ cell_sq,
+// Sum of cell_sq over [b0, b1) by one block: four accumulators per thread
+// (several loads in flight), then the fixed-order block sum.
+__device__ __forceinline__ double case_sum(const double* __restrict__ cell_sq, const int b0, const int b1,
+                                           double* sh) {
+    const int st = blockDim.x;
+    double v0 = 0, v1 = 0, v2 = 0, v3 = 0;
+    int k = b0 + threadIdx.x;
+    for (; k + 3 * st < b1; k += 4 * st) {
+        v0 += cell_sq[k];
+        v1 += cell_sq[k + st];
+        v2 += cell_sq[k + 2 * st];
+        v3 += cell_sq[k + 3 * st];
+    }
+    for (; k < b1; k += st) v0 += cell_sq[k];
+    return block_sum((v0 + v1) + (v2 + v3), sh);
+}
+
+static __global__ void __launch_bounds__(1024) k_case_control(const double* __restrict__ cell_sq,
                                                              const int* __restrict__ case_off, CaseCtrl* cctrl,
                                                              int* case_done, double* chist, Ctrl* ctrl, int n_cases,
                                                              int uniform) {
@@ -906,9 +923,7 @@ static __global__ void __launch_bounds__(256) k_case_control(const double* __res
     CaseCtrl& cc = cctrl[c];
     if (!uniform && cc.done) return;
     const int b0 = case_off[c], b1 = case_off[c + 1];
-    double v = 0;
-    for (int k = b0 + threadIdx.x; k < b1; k += blockDim.x) v += cell_sq[k];
-    const double t = block_sum(v, sh);
+    const double t = case_sum(cell_sq, b0, b1, sh);
     if (threadIdx.x != 0) return;
     const double norm = sqrt(t);
     if (uniform) {
@@ -942,7 +957,7 @@ static __global__ void __launch_bounds__(256) k_case_control(const double* __res
 // Implicit batches, right after a right-hand side: a case whose face sums
 // are not finite stops (status 4) and its right-hand-side rows are zeroed
 // before the linear solve, so it cannot spread into the other cases.
-static __global__ void __launch_bounds__(256) k_case_nonfinite(const double* __restrict__ cell_sq,
+static __global__ void __launch_bounds__(1024) k_case_nonfinite(const double* __restrict__ cell_sq,
                                                                const int* __restrict__ case_off, CaseCtrl* cctrl,
                                                                int* case_done, Ctrl* ctrl, d4* __restrict__ b) {
     __shared__ double sh[32];
@@ -950,9 +965,7 @@ static __global__ void __launch_bounds__(256) k_case_nonfinite(const double* __r
     const int c = blockIdx.x;
     if (cctrl[c].done) return;
     const int b0 = case_off[c], b1 = case_off[c + 1];
-    double v = 0;
-    for (int k = b0 + threadIdx.x; k < b1; k += blockDim.x) v += cell_sq[k];
-    const double t = block_sum(v, sh);
+    const double t = case_sum(cell_sq, b0, b1, sh);
     if (threadIdx.x == 0) {
         bad = !(t == t) || t > 1.7976931348623157e308;
         if (bad) {

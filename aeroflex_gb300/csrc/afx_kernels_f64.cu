@@ -11,11 +11,11 @@ void enqueue_iteration_f64(const StepArgs& a, int p, cudaStream_t s) { dev::iter
 void enqueue_residual_f64(const StepArgs& a, int p, cudaStream_t s) { dev::residual<double, double>(a, p, s); }
 void enqueue_rhs_f64(const StepArgs& a, int p, cudaStream_t s) { dev::rhs<double, double>(a, p, s); }
 void enqueue_case_nonfinite(const StepArgs& a, void* b, cudaStream_t s) {
-    dev::k_case_nonfinite<<<a.n_cases, 256, 0, s>>>(a.cell_sq, a.case_off, a.cctrl, a.case_done, a.ctrl,
+    dev::k_case_nonfinite<<<a.n_cases, 1024, 0, s>>>(a.cell_sq, a.case_off, a.cctrl, a.case_done, a.ctrl,
                                                     (dev::d4*)b);
 }
 void enqueue_case_control(const StepArgs& a, cudaStream_t s) {
-    dev::k_case_control<<<a.n_cases, 256, 0, s>>>(a.cell_sq, a.case_off, a.cctrl, a.case_done, a.chist, a.ctrl,
+    dev::k_case_control<<<a.n_cases, 1024, 0, s>>>(a.cell_sq, a.case_off, a.cctrl, a.case_done, a.chist, a.ctrl,
                                                   a.n_cases, 0);
     dev::k_batch_finalize<<<1, 1, 0, s>>>(a.ctrl, a.n_cases);
 }

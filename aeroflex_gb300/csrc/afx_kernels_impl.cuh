@@ -176,7 +176,7 @@ void iteration(const StepArgs& a, int p, cudaStream_t s) {
         launch_stage<T, S>(a, m, qk, q, o, st == 0, s);
     }
     if (a.n_cases > 0) {
-        k_case_control<<<a.n_cases, 256, 0, s>>>(a.cell_sq, a.case_off, a.cctrl, a.case_done, a.chist, a.ctrl,
+        k_case_control<<<a.n_cases, 1024, 0, s>>>(a.cell_sq, a.case_off, a.cctrl, a.case_done, a.chist, a.ctrl,
                                                  a.n_cases, 0);
         k_batch_finalize<<<1, 1, 0, s>>>(a.ctrl, a.n_cases);
     } else {
@@ -232,7 +232,7 @@ void uniform(const StepArgs& a, int p, const double* qf, cudaStream_t s) {
                                                    qf[2], qf[3], (d4*)a.Rq, a.partials, a.qfar_case, a.case_of,
                                                    a.cell_sq);
     if (a.n_cases > 0)
-        k_case_control<<<a.n_cases, 256, 0, s>>>(a.cell_sq, a.case_off, a.cctrl, a.case_done, a.chist, a.ctrl,
+        k_case_control<<<a.n_cases, 1024, 0, s>>>(a.cell_sq, a.case_off, a.cctrl, a.case_done, a.chist, a.ctrl,
                                                  a.n_cases, 1);
     else
         k_control<<<1, 1024, 0, s>>>(a.partials, nb, a.ctrl, a.hist, nullptr, 1);
