@@ -42,6 +42,11 @@ void implicit_destroy(ImplicitEngine* e);
 void implicit_fill(ImplicitEngine* e, const StepArgs& a, int p, cudaStream_t s);
 int implicit_solve_update(ImplicitEngine* e, const StepArgs& a, int p, const double* b, double relax,
                           cudaStream_t s);
+void implicit_transpose(ImplicitEngine* e, cudaStream_t s);
+void implicit_norm2(ImplicitEngine* e, const StepArgs& a, const double* v, double* out, cudaStream_t s);
+void implicit_adjoint_rho(ImplicitEngine* e, const double* u, const double* g, double* rho, cudaStream_t s);
+int implicit_adjoint_step(ImplicitEngine* e, const StepArgs& a, const double* rho, double relax, double* lam,
+                          cudaStream_t s);
 }  // namespace afx
 
 using namespace afx;
@@ -2027,66 +2032,100 @@ int afx_adjoint_solve(afx_solver s, const char* patch, const char* objective, do
         ForceArgs f = force_args(s, patch, vf);
         AFX_CUDA(cudaMemsetAsync(J.g.p, 0, N * 32, s->stream));
         enqueue_objective_grad(f, cx, cy, J.g.p, s->stream);
-        // gradients, limiter and local time step of the converged state; an
-        // implicit solver's CFL is not an explicit one: the pseudo-time steps
-        // then use CFL 1
-        StepArgs ap = a;
-        if (s->imp) ap.cfl = 1.0;
-        enqueue_adjoint_prep(ap, p, true, s->stream);
-        // pseudo-time iteration lam <- lam + relax*dt*(J^T lam + dJ/dq) with
-        // the solver's three stages (alpha = 1/4, 1/2, 1), from lam = 0
-        AFX_CUDA(cudaMemsetAsync(J.lam[0].p, 0, N * 32, s->stream));
-        static const double alpha[3] = {0.25, 0.5, 1.0};
-        const int nparts = (int)((N + 255) / 256);
-        std::vector<double> parts(nparts);
         int q = 0, it = 0;
         double r0 = -1, r = 0;
-        const int chunk = 10;
-        auto one = [&](int qq, bool norm) {
-            const void* l0 = J.lam[qq].p;
-            for (int st = 0; st < 3; ++st) {
-                const void* lk = st == 0 ? l0 : J.ls[st - 1].p;
-                enqueue_vjp(a, p, J.args(lk, J.u.p), s->stream);
-                void* out = st < 2 ? J.ls[st].p : J.lam[qq ^ 1].p;
-                enqueue_adjoint_update((int)N, l0, J.u.p, J.g.p, a.dt, alpha[st], a.relax, out,
-                                       (st == 2 && norm) ? (double*)J.partials.p : nullptr, s->stream);
-            }
-        };
-        // a graph of `chunk` iterations (even, so it starts and ends on lam[0])
-        cudaGraph_t gr;
-        cudaGraphExec_t ge;
-        AFX_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
-        for (int k = 0; k < chunk; ++k) one(k & 1, k == chunk - 1);
-        AFX_CUDA(cudaStreamEndCapture(s->stream, &gr));
-        AFX_CUDA(cudaGraphInstantiate(&ge, gr, 0));
-        cudaGraphDestroy(gr);
-        AFX_CUDA(cudaEventRecord(s->ev0, s->stream));
-        try {
-            while (it < max_it) {
-                AFX_CUDA(cudaGraphLaunch(ge, s->stream));
-                it += chunk;
-                AFX_CUDA(cudaMemcpyAsync(parts.data(), J.partials.p, nparts * 8, cudaMemcpyDeviceToHost, s->stream));
+        if (s->imp) {
+            // an implicit solver: defect correction with its own matrix at the
+            // converged state, transposed -- rho = dJ/dq + (dR/dq)^T lam (the
+            // exact vJP), M^T d = rho (GMRES, the transposed ILU(0)), then
+            // lam += relaxation * A d: the primal's implicit iteration for the
+            // adjoint equation (dR/dq)^T lam = -dJ/dq
+            StepArgs m = a;
+            m.cfl = s->st.max_cfl;
+            implicit_fill(s->imp, m, p, s->stream);
+            implicit_transpose(s->imp, s->stream);
+            enqueue_adjoint_prep(a, p, false, s->stream);  // gradients and limiter of the state for the vJP
+            AFX_CUDA(cudaMemsetAsync(J.lam[0].p, 0, N * 32, s->stream));
+            double* nrm = (double*)J.partials.p;
+            auto norm = [&](const void* v) {
+                implicit_norm2(s->imp, a, (const double*)v, nrm, s->stream);
+                double h = 0;
+                AFX_CUDA(cudaMemcpyAsync(&h, nrm, 8, cudaMemcpyDeviceToHost, s->stream));
                 AFX_CUDA(cudaStreamSynchronize(s->stream));
-                double t = 0;
-                for (double x : parts) t += x;
-                r = std::sqrt(t);
+                return std::sqrt(h);
+            };
+            AFX_CUDA(cudaEventRecord(s->ev0, s->stream));
+            const double g0 = norm(J.g.p);
+            r0 = g0 > 0 ? g0 : 1.0;
+            for (;;) {
+                enqueue_vjp(a, p, J.args(J.lam[0].p, J.u.p), s->stream);
+                implicit_adjoint_rho(s->imp, (const double*)J.u.p, (const double*)J.g.p, (double*)s->imp_b,
+                                     s->stream);
+                r = norm(s->imp_b);
                 if (!(r == r) || r > 1.7976931348623157e308) throw Error(AFX_ERR_NONFINITE, "adjoint diverged");
-                if (r0 < 0) {
-                    // the first chunk's residual stands in for ||dJ/dq|| (lam = 0)
-                    std::vector<double> gh(4 * N);
-                    AFX_CUDA(cudaMemcpy(gh.data(), J.g.p, N * 32, cudaMemcpyDeviceToHost));
-                    double g2 = 0;
-                    for (double x : gh) g2 += x * x;
-                    r0 = std::sqrt(g2) > 0 ? std::sqrt(g2) : 1.0;
-                }
-                if (r / r0 < tol || s->stop.load()) break;
+                if (r / r0 < tol || it >= max_it || s->stop.load()) break;
+                if (implicit_adjoint_step(s->imp, a, (const double*)s->imp_b, s->st.relaxation, (double*)J.lam[0].p,
+                                          s->stream) < 0)
+                    throw Error(AFX_ERR_NONFINITE, "adjoint: singular diagonal block");
+                ++it;
             }
-        } catch (...) {
+        } else {
+            // gradients, limiter and local time step of the converged state
+            enqueue_adjoint_prep(a, p, true, s->stream);
+            // pseudo-time iteration lam <- lam + relax*dt*(J^T lam + dJ/dq) with
+            // the solver's three stages (alpha = 1/4, 1/2, 1), from lam = 0
+            AFX_CUDA(cudaMemsetAsync(J.lam[0].p, 0, N * 32, s->stream));
+            static const double alpha[3] = {0.25, 0.5, 1.0};
+            const int nparts = (int)((N + 255) / 256);
+            std::vector<double> parts(nparts);
+            const int chunk = 10;
+            auto one = [&](int qq, bool norm) {
+                const void* l0 = J.lam[qq].p;
+                for (int st = 0; st < 3; ++st) {
+                    const void* lk = st == 0 ? l0 : J.ls[st - 1].p;
+                    enqueue_vjp(a, p, J.args(lk, J.u.p), s->stream);
+                    void* out = st < 2 ? J.ls[st].p : J.lam[qq ^ 1].p;
+                    enqueue_adjoint_update((int)N, l0, J.u.p, J.g.p, a.dt, alpha[st], a.relax, out,
+                                           (st == 2 && norm) ? (double*)J.partials.p : nullptr, s->stream);
+                }
+            };
+            // a graph of `chunk` iterations (even, so it starts and ends on lam[0])
+            cudaGraph_t gr;
+            cudaGraphExec_t ge;
+            AFX_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+            for (int k = 0; k < chunk; ++k) one(k & 1, k == chunk - 1);
+            AFX_CUDA(cudaStreamEndCapture(s->stream, &gr));
+            AFX_CUDA(cudaGraphInstantiate(&ge, gr, 0));
+            cudaGraphDestroy(gr);
+            AFX_CUDA(cudaEventRecord(s->ev0, s->stream));
+            try {
+                while (it < max_it) {
+                    AFX_CUDA(cudaGraphLaunch(ge, s->stream));
+                    it += chunk;
+                    AFX_CUDA(cudaMemcpyAsync(parts.data(), J.partials.p, nparts * 8, cudaMemcpyDeviceToHost,
+                                             s->stream));
+                    AFX_CUDA(cudaStreamSynchronize(s->stream));
+                    double t = 0;
+                    for (double x : parts) t += x;
+                    r = std::sqrt(t);
+                    if (!(r == r) || r > 1.7976931348623157e308) throw Error(AFX_ERR_NONFINITE, "adjoint diverged");
+                    if (r0 < 0) {
+                        // the first chunk's residual stands in for ||dJ/dq|| (lam = 0)
+                        std::vector<double> gh(4 * N);
+                        AFX_CUDA(cudaMemcpy(gh.data(), J.g.p, N * 32, cudaMemcpyDeviceToHost));
+                        double g2 = 0;
+                        for (double x : gh) g2 += x * x;
+                        r0 = std::sqrt(g2) > 0 ? std::sqrt(g2) : 1.0;
+                    }
+                    if (r / r0 < tol || s->stop.load()) break;
+                }
+            } catch (...) {
+                cudaGraphExecDestroy(ge);
+                throw;
+            }
             cudaGraphExecDestroy(ge);
-            throw;
         }
         AFX_CUDA(cudaEventRecord(s->ev1, s->stream));
-        cudaGraphExecDestroy(ge);
         AFX_CUDA(cudaEventSynchronize(s->ev1));
         float ms = 0;
         AFX_CUDA(cudaEventElapsedTime(&ms, s->ev0, s->ev1));

@@ -846,6 +846,62 @@ __global__ void k_imp_outer_check(GmresCtl* c) {
     if (c->graph) cudaGraphSetConditional(c->hout, cont ? 1 : 0);
 }
 
+// ------------------------------------------------------------ adjoint
+// M -> M^T in place: row p, slot s takes (O_qp)^T from the copy `src` of the
+// off-diagonal blocks; the diagonal block and its ILU(0) inverse are
+// transposed in their row.  The transposed inverses are exactly the ILU(0)
+// factors of M^T in the same colour order (D~' = D~^T by induction over
+// the colours), so the Gauss-Seidel sweep then applies P^T.
+template <class T>
+__global__ void __launch_bounds__(128) k_imp_transpose(const int N, const Ell e, const T* __restrict__ src,
+                                                       T* __restrict__ off, T* __restrict__ dblk,
+                                                       T* __restrict__ dinv) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= N) return;
+    const int4 col = __ldg(&e.col[p]);
+    const int4 tr = __ldg(&e.tr[p]);
+#pragma unroll 1
+    for (int s = 0; s < 4; ++s) {
+        if (pick(col, s) < 0) continue;
+        const int t2 = pick(tr, s);
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) off[ell_at<T>(N, p, s, 4 * r + c)] = src[ell_at<T>(N, t2 >> 2, t2 & 3, 4 * c + r)];
+    }
+    T* D = dblk + 16 * (size_t)p;
+    T* I = dinv + 16 * (size_t)p;
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = r + 1; c < 4; ++c) {
+            T t = D[4 * r + c];
+            D[4 * r + c] = D[4 * c + r];
+            D[4 * c + r] = t;
+            t = I[4 * r + c];
+            I[4 * r + c] = I[4 * c + r];
+            I[4 * c + r] = t;
+        }
+}
+
+// rho = u + g over the real cells (AoS FP64)
+__global__ void __launch_bounds__(256) k_imp_adj_rho(const int n, const double* __restrict__ u,
+                                                     const double* __restrict__ g, double* __restrict__ rho) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) rho[i] = u[i] + g[i];
+}
+
+// lam += relax * A .* d (d in row order, lam in device cell order)
+__global__ void __launch_bounds__(256) k_imp_adj_update(const int n, const double* __restrict__ d,
+                                                        const int* __restrict__ perm,
+                                                        const double* __restrict__ area, const double relax,
+                                                        double* __restrict__ lam) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int c = __ldg(&perm[i >> 2]);
+    lam[4 * (size_t)c + (i & 3)] += relax * area[c] * d[i];
+}
+
 }  // namespace dev
 
 // ----------------------------------------------------------------- host
@@ -1274,6 +1330,44 @@ int implicit_solve_update(ImplicitEngine* e, const StepArgs& a, int p, const dou
     const int it = e->f32 ? gmres<float>(e, a, b, s, 500) : gmres<double>(e, a, b, s, 500);
     dev::k_imp_update<<<nb_(e->n4, 256), 256, 0, s>>>(e->n4, e->x, e->perm, relax, (double*)a.qm[p],
                                                       (double*)a.Rq);
+    e->last_iters = it;
+    return it;
+}
+
+// The filled system transposed in place (M -> M^T, the ILU(0) factors ->
+// those of M^T) for the adjoint's linear solves.  The next implicit_fill
+// forms M again.  FP64 engines.
+void implicit_transpose(ImplicitEngine* e, cudaStream_t s) {
+    using namespace dev;
+    if (e->f32) throw Error(7, "implicit solver: the adjoint needs an FP64 engine");
+    // the Krylov basis (124 T per row) holds the copy of the blocks (64 T per row)
+    cudaMemcpyAsync(e->V, e->off, (size_t)e->N * 64 * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    k_imp_transpose<double><<<nb_(e->N, 128), 128, 0, s>>>(e->N, e->ell(), (const double*)e->V, (double*)e->off,
+                                                           (double*)e->dblk, (double*)e->dinv);
+}
+
+// ||v||^2 of an AoS FP64 vector over the real cells into out (device)
+void implicit_norm2(ImplicitEngine* e, const StepArgs& a, const double* v, double* out, cudaStream_t s) {
+    Ops<double> o(e, a, s);
+    o.template dots<0>(1, nullptr, v, const_cast<double*>(v), nullptr, out, nullptr);
+}
+
+// rho = g + (dR/dq)^T lam, u being the vJP (AoS FP64, device order)
+void implicit_adjoint_rho(ImplicitEngine* e, const double* u, const double* g, double* rho, cudaStream_t s) {
+    dev::k_imp_adj_rho<<<nb_(e->n4, 256), 256, 0, s>>>(e->n4, u, g, rho);
+}
+
+// One defect-correction step of the adjoint with the transposed system:
+// M^T d = rho by GMRES, then lam += relax * A .* d.  Returns the Krylov
+// iterations, -1 if a diagonal block was singular.
+int implicit_adjoint_step(ImplicitEngine* e, const StepArgs& a, const double* rho, double relax, double* lam,
+                          cudaStream_t s) {
+    int sing = 0;
+    cudaMemcpyAsync(&sing, e->singular, sizeof(int), cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    if (sing) return -1;
+    const int it = gmres<double>(e, a, rho, s, 500);
+    dev::k_imp_adj_update<<<nb_(e->n4, 256), 256, 0, s>>>(e->n4, e->x, e->perm, (const double*)a.area, relax, lam);
     e->last_iters = it;
     return it;
 }

@@ -86,8 +86,10 @@ int afx_config_from_ini_string(const char* text, afx_config* out);
  * rhs_iterations, max_iterations, second_order (0/1); this library's
  * block_size (0 auto | 32 | 64 | 128 | 256), fp64_correction_interval
  * (FP32-mixed: refresh an FP64 defect correction every n iterations, 0 off)
- * and fp64_finish (FP32-mixed: afx_run_to_convergence continues with FP64
- * iterations once the FP32 residual stops falling, 0/1). */
+ * fp64_finish (FP32-mixed: afx_run_to_convergence continues with FP64
+ * iterations once the FP32 residual stops falling, 0/1) and krylov_graph
+ * (implicit solver: 1 = each GMRES solve is one CUDA graph with device-side
+ * loops, 0 = the same kernels driven from a host loop, for profilers). */
 int afx_config_set_double(afx_config c, const char* key, double v);
 int afx_config_get_double(afx_config c, const char* key, double* v);
 /* String fields: solver ("explicit"/"implicit"), gradient ("green-gauss"/
@@ -216,10 +218,13 @@ int afx_residual_vjp(afx_solver s, const double* q, const double* v, double* u, 
 int afx_boundary_states(afx_solver s, double* bq, long long n);
 /* Sensitivities of a force coefficient J ("cl" or "cd" over `patch`,
  * post.h:301-387) at the solver's (converged) state: solves
- * (dR/dq)^T lam = -(dJ/dq)^T by pseudo-time iteration with the solver's own
- * local time step (CFL 1 for an implicit solver) and three stages, until ||(dR/dq)^T lam + dJ/dq|| falls
- * below tol * ||dJ/dq|| (tol <= 0: 1e-10) or max_it iterations
- * (<= 0: 100000).  dJ[0] = dJ/d(angle) per radian of the farfield angle,
+ * (dR/dq)^T lam = -(dJ/dq)^T until ||(dR/dq)^T lam + dJ/dq|| falls below
+ * tol * ||dJ/dq|| (tol <= 0: 1e-10) or max_it iterations (<= 0: 100000).
+ * An explicit solver iterates in pseudo-time with its own local time step
+ * and three stages.  An implicit solver runs its own implicit iteration
+ * transposed: the matrix at max_cfl and the converged state, transposed
+ * with its ILU(0) factors, GMRES for M^T d = dJ/dq + (dR/dq)^T lam, then
+ * lam += relaxation * A d (iterations = these steps).  dJ[0] = dJ/d(angle) per radian of the farfield angle,
  * dJ[1] = dJ/d(Mach), both for every farfield-type boundary together.
  * iters, res: iterations run and the final relative adjoint residual. */
 int afx_adjoint_solve(afx_solver s, const char* patch, const char* objective, double tol, int max_it, double* dJ,

@@ -151,6 +151,40 @@ def test_adjoint_alpha_mach_sensitivities_match_fd(afx):
             assert abs(ad - fd) <= 1e-6 * abs(fd) + 1e-9, (obj, k, ad, fd)
 
 
+@pytest.mark.parametrize("viscosity,wall", [("inviscid", "slip-wall"), ("laminar", "wall")])
+def test_implicit_adjoint_alpha_mach_sensitivities_match_fd(afx, viscosity, wall):
+    # an implicit solver's adjoint: its implicit iteration transposed (the
+    # ILU(0)-preconditioned GMRES on M^T), with the exact vJP in the defect
+    from aeroflex_gb300.rans import get_wall_profile
+    from aeroflex_gb300 import meshgen
+    m = meshgen.airfoil_omesh(32, 24, split=False, m=0.02, p=0.4, t=0.12)
+    bcs = {"farfield": dict(type="farfield", T=1.0, mach=0.5, angle=2.0 * DEG, p=1.0), "wall": dict(type=wall)}
+    M0, a0 = 0.5, 2.0 * DEG
+
+    def conv(M, a):
+        b = dict(bcs)
+        b["farfield"] = dict(b["farfield"], mach=M, angle=a)
+        g = gpu_solver(afx, m, b, viscosity=viscosity, solver="implicit", start_cfl=40.0, slope_cfl=50.0,
+                       max_cfl=100.0)
+        g.init()
+        g.run_solver(1e-12, 3000)
+        return g
+
+    g = conv(M0, a0)
+    out = {}
+    for obj in ("cl", "cd"):
+        d, iters, res = g.adjoint_solve("wall", obj, tol=1e-12, max_it=5000)
+        assert res < 1e-11 and iters < 5000, (obj, iters, res)
+        out[obj] = d
+    for k, (dM, da) in ((0, (0.0, 1e-5)), (1, (1e-5, 0.0))):
+        gp, gm = conv(M0 + dM, a0 + da), conv(M0 - dM, a0 - da)
+        h = dM + da
+        for obj in ("cl", "cd"):
+            fd = (get_wall_profile(gp, "wall")[obj] - get_wall_profile(gm, "wall")[obj]) / (2 * h)
+            ad = out[obj][k]
+            assert abs(ad - fd) <= 1e-6 * abs(fd) + 1e-9, (obj, k, ad, fd)
+
+
 def _implicit(afx, m, bcs, a=None, **kw):
     g = gpu_solver(afx, m, bcs, solver="implicit", start_cfl=40.0, slope_cfl=50.0, max_cfl=100.0, **kw)
     g.init()
