@@ -10,22 +10,26 @@
 // rhs_iterations chord steps with the same matrix.
 //
 // GB300 form:
-//   * block storage: one 4x4 diagonal block per cell and the two 4x4 flux
-//     Jacobians J = dF/dq_c0 L, K = dF/dq_c1 L per face (off-diagonal blocks
-//     K for row c0 and -J for row c1), never a general sparse matrix;
-//   * face Jacobians by the reference's one-sided differences
-//     (physics.h:533-578: step max(1e-6, 1e-6 |q|)), one thread per face;
-//   * preconditioner: block ILU(0) in a multicolour ordering (cells
-//     coloured so no two neighbours share a colour; the factor's diagonal
-//     blocks formed colour by colour), applied as a forward then a backward
-//     sweep over the colours -- a fixed linear operator, so right
+//   * face Jacobians J = dF/dq_c0 L, K = dF/dq_c1 L by the reference's
+//     one-sided differences (physics.h:533-578: step max(1e-6, 1e-6 |q|)),
+//     one thread per face;
+//   * block rows, not a general sparse matrix: rows grouped by colour (no
+//     two face neighbours share a colour), one 4x4 diagonal block per row and
+//     four off-diagonal ELL blocks (K for the face's cell 0, -J for its cell
+//     1), interleaved across rows so every warp load is contiguous;
+//   * preconditioner: block ILU(0) in that colour ordering (the factor's
+//     diagonal blocks formed colour by colour), applied as a forward then a
+//     backward sweep over the colours -- a fixed linear operator, so right
 //     preconditioned GMRES applies unchanged;
 //   * Krylov vectors and matrix blocks in T = double (FP64 path) or float
 //     (FP32-mixed path: the right-hand side, the update and the norms stay
 //     FP64, so the iteration converges to the FP64 solution);
-//   * every reduction is a fixed-order two-level sum (deterministic);
-//     Arnoldi steps after convergence are skipped on the device, so a
-//     restart cycle is launched without host round trips.
+//   * CGS2 in three fused passes over the basis, 16-byte loads; every
+//     reduction is a fixed-order two-level sum (deterministic);
+//   * each solve is one CUDA graph whose restart and Arnoldi loops are
+//     device-side WHILE nodes (or, with krylov_graph = 0, the same kernels
+//     from a host loop);
+//   * the adjoint transposes the filled system in place and reuses all of it.
 #include <algorithm>
 #include <string>
 #include <vector>
