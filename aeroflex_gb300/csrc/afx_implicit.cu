@@ -31,6 +31,7 @@
 //     from a host loop);
 //   * the adjoint transposes the filled system in place and reuses all of it.
 #include <algorithm>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -952,10 +953,14 @@ struct ImplicitEngine {
     dev::Ell ell() const { return dev::Ell{perm, ell_col, ell_face, ell_tr, case_row}; }
 };
 
+void implicit_destroy(ImplicitEngine* e);
+
 // cslot, cnbr: the host copies of the cell slots (4 per cell, device order)
 ImplicitEngine* implicit_create(const StepArgs& a, bool f32, bool graph, const std::vector<int>& colors,
                                 const int* cslot, const int* cnbr, cudaStream_t s) {
-    auto* e = new ImplicitEngine();
+    // freed again if any step below throws
+    std::unique_ptr<ImplicitEngine, void (*)(ImplicitEngine*)> guard(new ImplicitEngine(), implicit_destroy);
+    ImplicitEngine* e = guard.get();
     e->f32 = f32;
     e->graph = graph;
     e->N = a.n_cells;
@@ -1030,7 +1035,7 @@ ImplicitEngine* implicit_create(const StepArgs& a, bool f32, bool graph, const s
     e->h_ctl->graph = graph ? 1 : 0;
     chk(cudaMemcpyAsync(&e->ctl->graph, &e->h_ctl->graph, sizeof(int), cudaMemcpyHostToDevice, s));
     chk(cudaStreamSynchronize(s));
-    return e;
+    return guard.release();
 }
 
 void implicit_destroy(ImplicitEngine* e) {

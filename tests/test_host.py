@@ -141,6 +141,18 @@ def test_config_ini(afx):
     assert c3.get("viscosity") == "inviscid"  # unknown strings leave the setting unchanged (core.h:218-227)
 
 
+def test_library_settings_roundtrip(afx):
+    # this library's own numeric settings: defaults, set, read back
+    c = afx.Settings()
+    assert c.get("krylov_graph") == 1.0 and c.get("fp64_finish") == 0.0 and c.get("block_size") == 0.0
+    c.set("krylov_graph", 0).set("fp64_finish", 1).set("block_size", 128).set("fp64_correction_interval", 20)
+    assert c.get("krylov_graph") == 0.0 and c.get("fp64_finish") == 1.0
+    assert c.get("block_size") == 128.0 and c.get("fp64_correction_interval") == 20.0
+    with pytest.raises(afx.AfxError) as e:
+        c.set("block_size", 100)
+    assert e.value.code == 2
+
+
 @pytest.mark.parametrize("mutate,msg", [
     (lambda t: t.replace("<name = wall, type = slip-wall>\n", ""), "Invalid number of boundary conditions"),
     (lambda t: t.replace("[rans-alphas]", "[rans-alphaz]"), "Section [rans-alphas] not found"),
