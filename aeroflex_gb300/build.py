@@ -41,6 +41,7 @@ def _units():
         (cxx + ["-c"], "afx_mesh.cpp"),
         (cxx + ["-c"], "afx_config.cpp"),
         (cxx + ["-c"], "afx_abi.cpp"),
+        (cxx + ["-c"], "afx_vtu.cpp"),
         (nv + ["-fmad=false", "-c"], "afx_kernels_f64.cu"),
         (nv + ["-fmad=false", "-c"], "afx_noalloc.cu"),
         (nv + ["-fmad=false", "-c"], "afx_adjoint.cu"),

@@ -2406,6 +2406,29 @@ int afx_wall_distance(afx_solver s, double* out, long long n) {
     });
 }
 
+// rans::save (post.h:58-180) of a host state on a mesh
+int afx_write_vtu(afx_mesh m, const double* q, const double* wall_dist, long long n, double gamma, double R,
+                  const char* path) {
+    return guarded([&] {
+        if (!m || !q || !path) throw Error(AFX_ERR_ARG, "null argument");
+        if (n != 4 * (long long)m->m.nRealCells) throw Error(AFX_ERR_ARG, "state size must be 4*n_real_cells");
+        write_vtu(m->m, q, wall_dist, gamma, R, path);
+    });
+}
+
+// save(filename, solver) of the solver's state, with the wall distance that
+// multigrid.h:71 forms before a run (mesh::compute_wall_dist, on the GPU)
+int afx_save_vtu(afx_solver s, const char* path) {
+    return guarded([&] {
+        if (!s || !path) throw Error(AFX_ERR_ARG, "null argument");
+        const size_t N = s->a.n_cells;
+        std::vector<double> q(4 * N), wd(s->geo_area.size());
+        if (int rc = afx_get_state(s, q.data(), (long long)q.size())) throw Error(rc, afx_last_error());
+        if (int rc = afx_wall_distance(s, wd.data(), (long long)wd.size())) throw Error(rc, afx_last_error());
+        write_vtu(s->hm, q.data(), wd.data(), s->st.gamma, s->st.R, path);
+    });
+}
+
 int afx_linear_iterations(afx_solver s, int* n) {
     return guarded([&] {
         if (!s || !n) throw Error(AFX_ERR_ARG, "null argument");

@@ -100,6 +100,11 @@ struct HostMesh {
 
 HostMesh load_gmsh(const std::string& path);
 
+// rans::save (post.h:58-180): the ASCII VTU file of state q (4 per real cell,
+// reference order) on m; wall_dist per real cell, or null for zeros.
+void write_vtu(const HostMesh& m, const double* q, const double* wall_dist, double gamma, double R,
+               const std::string& path);
+
 // Device numbering of cells and faces, with per-cell face slots sorted by the
 // reference's edge id (so a per-cell sum over its faces adds in the same
 // order as the reference's serial edge loop).

@@ -33,6 +33,7 @@ ABI_SYMBOLS = [
     "afx_batch_last_device_seconds", "afx_residual_vjp", "afx_boundary_states", "afx_adjoint_solve",
     "afx_adjoint_state", "afx_linear_iterations", "afx_prolongate", "afx_patch_nodes", "afx_deform_patch",
     "afx_adjoint_patch", "afx_wall_distance", "afx_mesh_set_nodes", "afx_batch_linear_iterations",
+    "afx_write_vtu", "afx_save_vtu",
 ]
 N_KERNEL_KINDS = 7
 
@@ -119,6 +120,8 @@ def lib():
         "afx_adjoint_patch": (i, [vp, cp, cp, d, d, vp, i]),
         "afx_wall_distance": (i, [vp, vp, ll]),
         "afx_mesh_set_nodes": (i, [vp, vp, vp, ll]),
+        "afx_write_vtu": (i, [vp, vp, vp, ll, d, d, cp]),
+        "afx_save_vtu": (i, [vp, cp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -181,6 +184,14 @@ class mesh:
         x = np.ascontiguousarray(x, np.float64)
         y = np.ascontiguousarray(y, np.float64)
         _check(lib().afx_mesh_set_nodes(self.h, _ptr(x), _ptr(y), x.size))
+
+    def write_vtu(self, path, q, wall_dist=None, gamma=1.4, R=0.71428571428):
+        """`save` (post.h:58-180) of host state q (4 per real cell, reference
+        order) on this mesh; wall_dist per real cell (None: zeros)."""
+        q = np.ascontiguousarray(q, np.float64).ravel()
+        wd = None if wall_dist is None else np.ascontiguousarray(wall_dist, np.float64)
+        _check(lib().afx_write_vtu(self.h, _ptr(q), None if wd is None else _ptr(wd), q.size, float(gamma), float(R),
+                                   str(path).encode()))
 
     def boundary_names(self):
         buf = ctypes.create_string_buffer(256)
@@ -320,6 +331,11 @@ class Solver:
         _check(lib().afx_autotune(self.h, int(iters), buf, 16, ctypes.byref(blk), ctypes.byref(ms)))
         return dict(variant=buf.value.decode(), block=blk.value, ms_per_iter=ms.value)
 
+    def save_vtu(self, path):
+        """`save(filename, solver)` (post.h:58-180): the solver's state, its
+        wall distance and gas."""
+        _check(lib().afx_save_vtu(self.h, str(path).encode()))
+
     def wall_distance(self):
         """mesh::compute_wall_dist (mesh.h:794-830) on the GPU: all cells."""
         out = np.empty(self.n_real + self.n_boundary, np.float64)
@@ -399,6 +415,11 @@ class Solver:
         _check(lib().afx_profile_iterations(self.h, int(n), _ptr(ms), _ptr(cnt), N_KERNEL_KINDS))
         return {lib().afx_kernel_name(k).decode(): (float(ms[k]), int(cnt[k])) for k in range(N_KERNEL_KINDS)
                 if cnt[k] > 0}
+
+
+def save(filename, s):
+    """`rans::save` (post.h:58-180): the VTU file of solver s."""
+    s.save_vtu(filename)
 
 
 def get_wall_profile(s, patch="wall", cap=1 << 20):

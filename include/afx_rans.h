@@ -199,6 +199,20 @@ int afx_wall_distance(afx_solver s, double* out, long long n);
  * solver.  No counterpart in the reference (Eigen's iterations() is only
  * printed under RANS_DEBUG). */
 int afx_linear_iterations(afx_solver s, int* n);
+/* ---- Output.  Replaces rans::save (post.h:58-180): the ASCII VTU file,
+ * byte for byte as the reference writes it (node coordinates, real cells as
+ * VTK triangles 5 / quads 9, and per cell the wall distance, Mach, density,
+ * pressure, temperature and velocity of solution, core.h:119-164). */
+/* A host state q (4*n_real doubles, reference order) on mesh m; wall_dist:
+ * n_real doubles or NULL (zeros: a mesh whose compute_wall_dist has not run);
+ * gamma, R: the gas. */
+int afx_write_vtu(afx_mesh m, const double* q, const double* wall_dist, long long n, double gamma, double R,
+                  const char* path);
+/* The solver's state on its (possibly deformed) mesh, with the wall distance
+ * of its wall / slip-wall patches (mesh.h:794-830, as multigrid.h:71 forms
+ * it before a run) and its gas. */
+int afx_save_vtu(afx_solver s, const char* path);
+
 
 /* ---- Adjoint of the FP64 residual.  No counterpart in the reference (it
  * has no adjoint).  R(q) is the residual afx_residual returns (first-stage

@@ -12,7 +12,9 @@
 //    converged solution is the same;
 //  * mesh paths come from the caller (rans.h:84-85 hard-code
 //    "../../../../examples/rans/<name>_coarse.msh" and "_mid.msh"); pass
-//    both to solve_airfoil for the reference's two-level sequence.
+//    both to solve_airfoil for the reference's two-level sequence;
+//  * the VTU file of every angle (rans.h:103) is written when solve_airfoil
+//    is given a file prefix (the reference always writes it).
 #pragma once
 
 #include <atomic>
@@ -154,6 +156,9 @@ inline wallProfile get_wall_profile(solver& s, const std::string& patch_name) {
     return w;
 }
 
+// save (post.h:58-180): the ASCII VTU file of the solver's state
+inline void save(const std::string& filename, solver& s) { afx_check(afx_save_vtu(s.handle(), filename.c_str())); }
+
 // rans::Rans (rans.h:25-123): alpha sweep with warm restarts.
 class Rans {
   public:
@@ -181,8 +186,11 @@ class Rans {
     // level starting from the coarser one's solution (multigrid::run,
     // multigrid.h:295-363), and every level keeps its own state from one
     // angle to the next (run(false)).  The polar is read on the last level.
+    // vtu_prefix non-empty: the VTU file of the last level after every angle,
+    // named prefix + "_" + std::to_string(alpha) + ".vtu" (rans.h:103)
     void solve_airfoil(const std::vector<std::string>& level_paths, airfoil_db& db,
-                       const std::string& farfield = "farfield", const std::string& wall = "wall") {
+                       const std::string& farfield = "farfield", const std::string& wall = "wall",
+                       const std::string& vtu_prefix = "") {
         if (level_paths.empty()) throw std::runtime_error("[RANS] no mesh");
         iters = 0;
         if (alphas.empty()) compute_alphas();
@@ -207,11 +215,12 @@ class Rans {
             db.cl.push_back(wp.cl);
             db.cd.push_back(wp.cd);
             db.cmy.push_back(wp.cm);
+            if (!vtu_prefix.empty()) save(vtu_prefix + "_" + std::to_string(a) + ".vtu", *levels_.back());
         }
     }
     void solve_airfoil(const std::string& mesh_path, airfoil_db& db, const std::string& farfield = "farfield",
-                       const std::string& wall = "wall") {
-        solve_airfoil(std::vector<std::string>{mesh_path}, db, farfield, wall);
+                       const std::string& wall = "wall", const std::string& vtu_prefix = "") {
+        solve_airfoil(std::vector<std::string>{mesh_path}, db, farfield, wall, vtu_prefix);
     }
 
   private:

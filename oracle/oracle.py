@@ -69,6 +69,7 @@ def lib():
         L.orc_time_residuals.argtypes = [vp, ip]
         d = ctypes.c_double
         L.orc_face_flux.argtypes = [d, ip, ip, d, d, vp, vp, vp, vp, vp]
+        L.orc_save_vtu.argtypes = [vp, vp, vp, d, d, cp]
         _lib = L
     return _lib
 
@@ -134,6 +135,14 @@ class Mesh:
 
     def boundary_names(self):
         return [lib().orc_mesh_boundary_name(self.h, b).decode() for b in range(self.n_boundary)]
+
+    def save_vtu(self, path, q, wall_dist=None, gamma=1.4, R=0.71428571428):
+        """save (post.h:58-180) of state q (4 per real cell) on this mesh."""
+        q = np.ascontiguousarray(q, np.float64)
+        wd = None if wall_dist is None else np.ascontiguousarray(wall_dist, np.float64)
+        if lib().orc_save_vtu(self.h, _ptr(q), None if wd is None else _ptr(wd), float(gamma), float(R),
+                              str(path).encode()):
+            raise OSError("oracle: cannot write " + str(path))
 
     def __del__(self):
         if getattr(self, "h", None) and _lib is not None:

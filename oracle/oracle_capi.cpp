@@ -4,6 +4,7 @@
 // non-zero return and a message in orc_last_error().
 #include <chrono>
 #include <omp.h>
+#include <cstdio>
 #include <cstring>
 #include <string>
 
@@ -133,6 +134,20 @@ long long orc_mesh_get_int(void* mp, const char* what, long long* out) {
         return (long long)m->boundaryEdges.size();
     }
     return -1;
+}
+
+// save (post.h:58-180) of state q on mesh mp to path; wd per real cell or
+// null (the mesh's wall_dist); returns 0, or -1 if the file cannot be written.
+int orc_save_vtu(void* mp, const double* q, const double* wd, double gamma, double R, const char* path) {
+    Gas g;
+    g.gamma = gamma;
+    g.R = R;
+    const std::string t = save_text(*(Mesh*)mp, q, wd, g);
+    std::FILE* f = std::fopen(path, "wb");
+    if (!f) return -1;
+    const size_t w = std::fwrite(t.data(), 1, t.size(), f);
+    std::fclose(f);
+    return w == t.size() ? 0 : -1;
 }
 
 // Boundary patch name of boundary edge b.

@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
+#include <iomanip>
 #include <sstream>
 
 namespace oracle {
@@ -914,5 +915,82 @@ void prolongate(ExplicitSolver& coarse, ExplicitSolver& fine) {
     }
     fine.q = out;
     fine.refill_bcs();
+}
+
+// ------------------------------------------------------------ post.h:58-180
+// save(): the same text the reference assembles.  Node coordinates through
+// std::to_string (double2string is not used there), cell data through a
+// fixed-notation stream with 16 digits (double2string, post.h:33-37), the
+// derived fields of solution (core.h:119-164).
+namespace {
+std::string fixed16(double x) {
+    std::ostringstream o;
+    o << std::fixed << std::setprecision(16) << x;
+    return o.str();
+}
+}  // namespace
+
+std::string save_text(const Mesh& m, const double* q, const double* wd, const Gas& g) {
+    const uint nc = m.nRealCells;
+    auto rho = [&](uint i) { return q[4 * i]; };
+    auto ru = [&](uint i) { return q[4 * i + 1]; };
+    auto rv = [&](uint i) { return q[4 * i + 2]; };
+    auto re = [&](uint i) { return q[4 * i + 3]; };
+    auto pres = [&](uint i) { return (g.gamma - 1) * (re(i) - 0.5 / rho(i) * (ru(i) * ru(i) + rv(i) * rv(i))); };
+    auto sound = [&](uint i) { return std::sqrt(g.gamma * pres(i) / rho(i)); };
+    std::string t;
+    t += "<VTKFile type=\"UnstructuredGrid\" version=\"0.1\" byte_order=\"BigEndian\">\n";
+    t += "  <UnstructuredGrid>\n";
+    t += "    <Piece NumberOfPoints=\"" + std::to_string(m.nodesX.size()) + "\" NumberOfCells=\"" +
+         std::to_string(nc) + "\">\n";
+    t += "      <Points>\n";
+    t += "        <DataArray type=\"Float32\" NumberOfComponents=\"3\" Format=\"ascii\">\n";
+    for (size_t k = 0; k < m.nodesX.size(); ++k)
+        t += "          " + std::to_string(m.nodesX[k]) + " " + std::to_string(m.nodesY[k]) + " 0.0\n";
+    t += "        </DataArray>\n";
+    t += "      </Points>\n";
+    t += "      <Cells>\n";
+    t += "        <DataArray type=\"Int32\" Name=\"connectivity\" Format=\"ascii\">\n";
+    t += "          ";
+    for (uint i = 0; i < nc; ++i) {
+        const uint k = m.cellsIsTriangle[i] ? 3 : 4;
+        for (uint j = 0; j < k; ++j) t += std::to_string(m.cellsNodes[i][j]) + "  ";
+        t += "\n          ";
+    }
+    t += "        </DataArray>\n";
+    t += "        <DataArray type=\"Int32\" Name=\"offsets\" Format=\"ascii\">\n";
+    t += "          ";
+    uint off = 0;
+    for (uint i = 0; i < nc; ++i) {
+        off += m.cellsIsTriangle[i] ? 3 : 4;
+        t += std::to_string(off) + "  ";
+    }
+    t += "\n";
+    t += "        </DataArray>\n";
+    t += "        <DataArray type=\"Int32\" Name=\"types\" Format=\"ascii\">\n";
+    t += "          ";
+    for (uint i = 0; i < nc; ++i) t += m.cellsIsTriangle[i] ? "5  " : "9  ";
+    t += "\n";
+    t += "        </DataArray>\n";
+    t += "      </Cells>\n";
+    t += "      <CellData Scalars=\"scalars\">\n";
+    auto field = [&](const char* name, auto f) {
+        t += std::string("        <DataArray type=\"Float32\" Name=\"") + name + "\" Format=\"ascii\">\n";
+        for (uint i = 0; i < nc; ++i) t += "          " + fixed16(f(i)) + "\n";
+        t += "        </DataArray>\n";
+    };
+    field("Wall Distance", [&](uint i) { return wd ? wd[i] : m.wall_dist[i]; });
+    field("Mach", [&](uint i) { return std::sqrt(ru(i) * ru(i) + rv(i) * rv(i)) / (rho(i) * sound(i)); });
+    field("Density", rho);
+    field("Pressure", pres);
+    field("Temperature", [&](uint i) { return pres(i) / (g.R * rho(i)); });
+    t += "        <DataArray type=\"Float32\" Name=\"Velocity\" NumberOfComponents=\"3\" Format=\"ascii\">\n";
+    for (uint i = 0; i < nc; ++i) t += "          " + fixed16(ru(i) / rho(i)) + " " + fixed16(rv(i) / rho(i)) + " 0.0\n";
+    t += "        </DataArray>\n";
+    t += "      </CellData>\n";
+    t += "    </Piece>\n";
+    t += "  </UnstructuredGrid>\n";
+    t += "</VTKFile>";
+    return t;
 }
 }  // namespace oracle

@@ -181,4 +181,8 @@ void internal_flux(const Gas& g, double nx, double ny, int viscous_type, const d
 void boundary_state(const Gas& g, int type, double nx, double ny, const double qL[4],
                     const double qbc[4], double qR[4]);
 
+// save (post.h:58-180): the VTU text of state q (4 per real cell) on m, with
+// wall distances wd (per real cell; null: the mesh's own wall_dist) and gas g.
+std::string save_text(const Mesh& m, const double* q, const double* wd, const Gas& g);
+
 }  // namespace oracle
