@@ -109,3 +109,19 @@ def test_save_vtu_of_a_solver_matches_oracle(afx, orc, tmp_path):
     om, s = _oracle_state(orc, m, bcs, iters=10)
     om.save_vtu(tmp_path / "o.vtu", s.q(), s.wall_distance()[: om.n_real])
     assert (tmp_path / "g.vtu").read_bytes() == (tmp_path / "o.vtu").read_bytes()
+
+
+def test_vtu_extreme_values_match_oracle(afx, orc, tmp_path):
+    # long fixed-notation numbers (1e300 has 301 integer digits), tiny ones,
+    # negative zero: the library's formatting equals the stream formatting
+    m, bcs = omesh_case(16, 8, split=True)
+    gm, om = afx.mesh.from_arrays(m), orc.Mesh.from_arrays(m)
+    n = gm.nRealCells
+    q = np.tile([1.4, 0.7, 0.05, 2.8], n)
+    q[0::4][:3] = [1e300, 1e-300, 3.0]
+    q[1::4][:3] = [-0.0, 1e150, -1e-200]
+    wd = np.full(n, 0.0)
+    wd[:4] = [-0.0, 1e300, 5e-324, 0.1]
+    gm.write_vtu(tmp_path / "a.vtu", q, wd)
+    om.save_vtu(tmp_path / "b.vtu", q, wd)
+    assert (tmp_path / "a.vtu").read_bytes() == (tmp_path / "b.vtu").read_bytes()
