@@ -48,6 +48,7 @@ def _units():
         (nv + ["-c"], "afx_implicit.cu"),
         (nv + ["-fmad=false", "-c"], "afx_prolong.cu"),
         (nv + ["-use_fast_math", "-c"], "afx_kernels_f32.cu"),
+        (nv + ["-c"], "afx_peak.cu"),
     ], nvcc
 
 

@@ -25,6 +25,7 @@ void enqueue_permute_in(int n, const int* cell_old, const void* src, void* dst, 
 void enqueue_permute_out(int n, const int* cell_old, const void* src, void* dst, cudaStream_t s);
 void enqueue_to_f32(int n, const void* src, void* dst, cudaStream_t s);
 void enqueue_correction(int n, const void* R64, const void* R32, void* corr, cudaStream_t s);
+double fp64_fma_peak(int reps);
 long long noalloc_max_cells();
 long long noalloc_max_faces();
 cudaError_t noalloc_residual_f64(const StepArgs& a, const int* cell_old, const double* q_ref, double* R_ref,
@@ -1251,6 +1252,27 @@ int afx_residual(afx_solver s, double* R, long long n) {
     });
 }
 
+// fillRhoRHS (solver.h:1079-1152) of the current state, for an implicit
+// solver: the face sums of the second-order residual, not divided by the
+// area, ghost rows zero.  rhs gets the real-cell rows (AoS FP64, reference
+// cell order).
+int afx_implicit_rhs(afx_solver s, double* rhs, long long n) {
+    return guarded([&] {
+        if (!s || !rhs) throw Error(AFX_ERR_ARG, "null argument");
+        if (!s->imp) throw Error(AFX_ERR_CONFIG, "afx_implicit_rhs needs an implicit solver");
+        const size_t N = s->a.n_cells;
+        if (n != (long long)(4 * N)) throw Error(AFX_ERR_ARG, "size must be 4*n_real_cells");
+        s->ensure_shadow();
+        s->materialize_qW();
+        s->set_ctrl(0, 0, 0);
+        s->imp_rhs(s->parity);
+        enqueue_permute_out((int)N, (const int*)s->d_cell_old.p, s->imp_b, s->d_stage.p, s->stream);
+        AFX_CUDA(cudaMemcpyAsync(rhs, s->d_stage.p, N * 32, cudaMemcpyDefault, s->stream));
+        AFX_CUDA(cudaStreamSynchronize(s->stream));
+        AFX_CUDA(cudaGetLastError());
+    });
+}
+
 // The implicit path of afx_iterate / afx_run_to_convergence: the loop of
 // multigrid<implicitSolver>::run_solver (multigrid.h:240-293) with its CFL
 // ramp min(start + (i+1) slope, max); run_mode 0 runs n iterations without
@@ -1626,6 +1648,15 @@ int afx_autotune(afx_solver s, int iters, char* variant, int cap, int* block, do
     return guarded([&] { autotune_impl(s, iters, variant, cap, block, ms_per_iter); });
 }
 
+int afx_measure_fp64_peak(int reps, double* tflops) {
+    return guarded([&] {
+        if (!tflops) throw Error(AFX_ERR_ARG, "null argument");
+        const double t = fp64_fma_peak(reps > 0 ? reps : 5);
+        if (t < 0) throw Error(AFX_ERR_CUDA, "FP64 peak kernel failed");
+        *tflops = t;
+    });
+}
+
 const char* afx_kernel_name(int k) {
     static const char* names[K_COUNT] = {"k_prep", "k_limiter", "k_face_flux", "k_cell_sum", "k_resid_gather",
                                          "k_control", "k_resid_tile"};
@@ -1635,7 +1666,8 @@ const char* afx_kernel_name(int k) {
 // For callers that cannot let the library allocate device memory (see
 // afx_noalloc.cu): the residual of a caller-owned device state, written to a
 // caller-owned device array, with all scratch in the library's fixed device
-// array.  No cudaMalloc/cudaFree or other allocating call is made here.
+// array.  No cudaMalloc/cudaFree or other allocating call is made here.  The
+// work runs on the solver's own stream, which is synchronised before return.
 int afx_residual_noalloc(afx_solver s, const double* q_dev, double* R_dev, long long n) {
     return guarded([&] {
         if (!s || !q_dev || !R_dev) throw Error(AFX_ERR_ARG, "null argument");
@@ -1655,6 +1687,9 @@ int afx_residual_noalloc(afx_solver s, const double* q_dev, double* R_dev, long 
                 throw Error(AFX_ERR_ARG, "afx_residual_noalloc takes device pointers");
             }
         }
+        // the lazily formed last-stage qW of a previous iterate() reads the
+        // gradient/limiter buffers that the residual below overwrites
+        s->materialize_qW();
         s->set_ctrl(0, 0, 0);
         AFX_CUDA(noalloc_residual_f64(s->a, (const int*)s->d_cell_old.p, q_dev, R_dev, s->stream));
         AFX_CUDA(cudaStreamSynchronize(s->stream));

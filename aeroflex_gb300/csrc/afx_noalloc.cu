@@ -1,12 +1,13 @@
 // Residual evaluation that allocates no device memory.
 //
 // Some callers cannot let a library call cudaMalloc: a structural or coupling
-// code that owns all device memory through its own pool (a library-side
-// cudaMalloc/cudaFree would synchronise the whole device and break its stream
-// overlap), or a caller that is recording CUDA stream capture, where
-// allocating calls are not permitted.  For them the face-flux form of the FP64
-// residual keeps its scratch — the state in device cell order and the face
-// fluxes F*L — in the fixed device array below instead of allocating it.
+// code that owns all device memory through its own pool, sized at start-up (a
+// library-side cudaMalloc/cudaFree would synchronise the whole device and break
+// its stream overlap, and could fail once the pool holds the memory).  For
+// them the face-flux form of the FP64 residual keeps its scratch — the state
+// in device cell order and the face fluxes F*L — in the fixed device array
+// below instead of allocating it.  The work runs on the solver's own stream;
+// the entry point synchronises that stream before it returns.
 //
 // Limits: at most AFX_NOALLOC_MAX_CELLS real cells and AFX_NOALLOC_MAX_FACES
 // faces (24 MiB of device memory in total).  Every GPU that loads the library
@@ -15,8 +16,7 @@
 // nothing needs clearing.  Calls that overlap on the GPU (two streams, two
 // threads, two solvers) race on the array and must be serialised by the
 // caller.  On each device, the first call looks up the array's device address
-// (cudaGetSymbolAddress) with that device current; make that first call
-// before any stream capture.
+// (cudaGetSymbolAddress) with that device current.
 #include <mutex>
 
 #include "afx_kernels_impl.cuh"

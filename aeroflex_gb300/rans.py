@@ -14,7 +14,7 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libafx_rans.so")
 
-AFX_ERRORS = {1: "IO", 2: "CONFIG", 3: "MESH", 4: "NONFINITE", 5: "DIVERGED", 6: "TIMEOUT", 7: "CUDA", 8: "ARG",
+AFX_ERRORS = {1: "IO", 2: "CONFIG", 3: "MESH", 4: "NONFINITE", 5: "DIVERGED", 7: "CUDA", 8: "ARG",
               9: "STOPPED"}
 
 # Symbols declared in include/afx_rans.h.
@@ -27,7 +27,7 @@ ABI_SYMBOLS = [
     "afx_solver_free", "afx_init_freestream", "afx_set_state", "afx_get_state", "afx_residual", "afx_iterate",
     "afx_run_to_convergence", "afx_residual_history", "afx_forces", "afx_set_farfield", "afx_request_stop",
     "afx_last_device_seconds", "afx_profile_iterations", "afx_kernel_name", "afx_autotune",
-    "afx_residual_noalloc", "afx_batch_create", "afx_batch_free", "afx_batch_counts", "afx_batch_init_freestream",
+    "afx_residual_noalloc", "afx_implicit_rhs", "afx_measure_fp64_peak", "afx_batch_create", "afx_batch_free", "afx_batch_counts", "afx_batch_init_freestream",
     "afx_batch_set_state", "afx_batch_get_state", "afx_batch_iterate", "afx_batch_run_to_convergence",
     "afx_batch_case_history", "afx_batch_forces", "afx_batch_set_farfield", "afx_batch_autotune",
     "afx_batch_last_device_seconds", "afx_residual_vjp", "afx_boundary_states", "afx_adjoint_solve",
@@ -95,6 +95,8 @@ def lib():
         "afx_kernel_name": (cp, [i]),
         "afx_autotune": (i, [vp, i, ctypes.c_char_p, i, P(i), P(d)]),
         "afx_residual_noalloc": (i, [vp, vp, vp, ll]),
+        "afx_implicit_rhs": (i, [vp, vp, ll]),
+        "afx_measure_fp64_peak": (i, [ctypes.c_int, vp]),
         "afx_batch_create": (i, [i, vp, vp, P(vp)]),
         "afx_batch_free": (None, [vp]),
         "afx_batch_counts": (i, [vp, P(i), P(ll)]),
@@ -294,6 +296,13 @@ class Solver:
         _check(lib().afx_residual(self.h, _ptr(R), R.size))
         return R
 
+    def implicit_rhs(self):
+        """fillRhoRHS (solver.h:1079-1152) of the current state (implicit
+        solvers): face sums not divided by the area."""
+        R = np.empty(4 * self.n_real, np.float64)
+        _check(lib().afx_implicit_rhs(self.h, _ptr(R), R.size))
+        return R
+
     def iterate(self, n):
         r = ctypes.c_double()
         _check(lib().afx_iterate(self.h, int(n), ctypes.byref(r)))
@@ -420,6 +429,13 @@ class Solver:
 def save(filename, s):
     """`rans::save` (post.h:58-180): the VTU file of solver s."""
     s.save_vtu(filename)
+
+
+def measure_fp64_peak(reps=5):
+    """FP64 FMA-chain peak of the current GPU in TFLOP/s (afx_measure_fp64_peak)."""
+    t = ctypes.c_double()
+    _check(lib().afx_measure_fp64_peak(int(reps), ctypes.byref(t)))
+    return t.value
 
 
 def get_wall_profile(s, patch="wall", cap=1 << 20):

@@ -29,7 +29,7 @@ typedef enum {
     AFX_ERR_MESH = 3,      /* malformed mesh (mesh.h throws std::invalid_argument) */
     AFX_ERR_NONFINITE = 4, /* residual norm became NaN/Inf */
     AFX_ERR_DIVERGED = 5,  /* residual grew past the divergence guard */
-    AFX_ERR_TIMEOUT = 6,   /* a bounded device wait ran out */
+    /* 6 is not used: no entry point waits on the device without a bound */
     AFX_ERR_CUDA = 7,      /* CUDA runtime error or no usable GPU */
     AFX_ERR_ARG = 8,       /* null handle / bad size / unknown name */
     AFX_ERR_STOPPED = 9    /* afx_request_stop() ended a run early (results are valid) */
@@ -124,6 +124,10 @@ int afx_get_state(afx_solver s, double* q, long long n);
  * Green-Gauss gradient, limiter, face loop, /area (solver.h:745-799).
  * R gets AoS FP64 [4*n_real]. */
 int afx_residual(afx_solver s, double* R, long long n);
+/* Implicit solvers: fillRhoRHS (solver.h:1079-1152) of the current state —
+ * the second-order face sums not divided by the area (RhoVector), real-cell
+ * rows, AoS FP64 [4*n_real], reference cell order. */
+int afx_implicit_rhs(afx_solver s, double* rhs, long long n);
 /* n explicit iterations (explicitSolver::solve, solver.h:802-828); res_norm
  * gets ‖qW‖₂ of the last stage of the last iteration. */
 int afx_iterate(afx_solver s, int n_iters, double* res_norm);
@@ -152,6 +156,11 @@ int afx_last_device_seconds(afx_solver s, double* sec);
  * iterations exactly as afx_iterate would. */
 int afx_profile_iterations(afx_solver s, int n_iters, double* ms, int* launches, int n_kinds);
 const char* afx_kernel_name(int k);
+/* FP64 arithmetic peak of the current GPU, measured (no counterpart in the
+ * reference): independent fused multiply-add chains on every SM, best of
+ * `reps` launches timed with CUDA events, 2 flops per FMA, in TFLOP/s.  The
+ * denominator of the FP64 path's roofline, which the FP64 pipe bounds. */
+int afx_measure_fp64_peak(int reps, double* tflops);
 /* Launch autotuner (no counterpart in the reference): times `iters`
  * iterations of each residual-kernel variant ("gather": per-cell flux
  * re-formation; "face": one flux per face + ordered cell sum) at 64, 128 and
@@ -161,19 +170,26 @@ const char* afx_kernel_name(int k);
 int afx_autotune(afx_solver s, int iters, char* variant, int cap, int* block, double* ms_per_iter);
 
 /* Residual without device allocation.  No counterpart in the reference.
- * For callers that cannot let a library allocate device memory — a coupling
- * code that owns all device memory through its own pool (a library-side
- * cudaMalloc would synchronise the device and break its stream overlap), or
- * code recording a CUDA stream capture, where allocating calls are not
- * allowed.  Same result as afx_residual (bit for bit) for the state q_dev,
- * but q_dev and R_dev are the caller's DEVICE arrays of 4*n_real doubles in
- * reference cell order, and the scratch lives in a fixed 24 MiB device array
- * inside the library: at most 262,144 cells and 524,288 faces (larger meshes
- * return AFX_ERR_ARG).  FP64 solvers only.  The solver's own state is not
- * changed; its gradient/limiter buffers are overwritten as afx_residual does.
- * Calls share the fixed array, so calls that overlap on the GPU race: the
- * caller serialises them.  The first call on each device looks up the
- * array's address; make it before any stream capture. */
+ * For callers that cannot let a library allocate device memory: a structural
+ * or coupling code that owns all device memory through its own pool sized at
+ * start-up (a library-side cudaMalloc/cudaFree would synchronise the whole
+ * device and break that code's stream overlap, and could fail once the pool
+ * holds the memory).  Same result as afx_residual (bit for bit) for the state
+ * q_dev, but q_dev and R_dev are the caller's DEVICE arrays of 4*n_real
+ * doubles in reference cell order, and the scratch lives in a fixed 24 MiB
+ * device array inside the library: at most 262,144 cells and 524,288 faces
+ * (larger meshes return AFX_ERR_ARG).  FP64 solvers only.
+ * Ordering: the call reads q_dev on the solver's own stream, which is not
+ * ordered after the caller's streams, so q_dev must be complete on the
+ * device when the call is made (the caller synchronises the stream that
+ * wrote it).  The call synchronises the solver's stream before it returns,
+ * so R_dev is complete on return.
+ * The solver's state is not changed; its gradient/limiter buffers are
+ * overwritten as afx_residual does (a pending last-stage qW is formed first).
+ * Calls share the fixed array, so calls that overlap on the GPU (two host
+ * threads, two solvers) race: the caller serialises them.  On each device,
+ * the first call looks up the array's device address with that device
+ * current. */
 int afx_residual_noalloc(afx_solver s, const double* q_dev, double* R_dev, long long n);
 
 /* Grid sequencing: multigrid::run's transfer between levels (multigrid.h:

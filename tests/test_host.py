@@ -9,9 +9,10 @@ import numpy as np
 import pytest
 
 from aeroflex_gb300 import meshgen
+from oracle import refsrc
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF_MESHES = "/root/reference/examples/rans"
+REF_MESHES = refsrc.path("examples", "rans")
 METRICS = ["cx", "cy", "area", "ex", "ey", "nx", "ny", "L"]
 
 
@@ -168,7 +169,7 @@ def test_config_errors(afx, mutate, msg):
 
 @pytest.mark.skipif(not os.path.isdir(REF_MESHES), reason="reference examples not mounted")
 def test_reference_configs(afx):
-    c = afx.Settings.from_ini("/root/reference/examples/conf.ini")
+    c = afx.Settings.from_ini(refsrc.path("examples", "conf.ini"))
     assert c.get("max_cfl") == 100.0 and c.get("tolerance") == 1e-4
     # examples/rans/config.ini has no [rans-alphas]: import fails as in the reference (core.h:269)
     with pytest.raises(afx.AfxError) as e:

@@ -9,8 +9,9 @@ import numpy as np
 import pytest
 
 from tests.cases import channel_case, omesh_case
+from oracle import refsrc
 
-REF_MESHES = "/root/reference/examples/rans"
+REF_MESHES = refsrc.path("examples", "rans")
 
 
 def _oracle_state(orc, m, bcs, iters=12):
