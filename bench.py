@@ -164,6 +164,38 @@ def measured_traffic(kernel, precision, n, f):
         return None
 
 
+def evaluation_bytes(n, g, f, precision):
+    """Compulsory HBM bytes of one cell-residual evaluation of the whole
+    mesh (gradient + limiter + flux, one RK stage), each array counted once:
+    (N+G)(4 w_s + 3 w_geo) + N (16 w_g + 8 w_phi + 4 w_r) + F (8 + 5 w_geo)
+    -- q of every cell and ghost; area and centroid; gx, gy written and read;
+    the limiter written and read; R written; per face two cell ids and
+    (n_x, n_y, L, x_f, y_f).  FP64: every w = 8; FP32-mixed: w = 4 except
+    the FP64 residual (w_r = 8)."""
+    w = 8 if precision == "fp64" else 4
+    return (n + g) * (4 * w + 3 * w) + n * (16 * w + 8 * w + 4 * 8) + f * (8 + 5 * w)
+
+
+# FP64 operations (add, sub, mul, div, sqrt each 1) of the explicit scheme,
+# hand-counted from the reference's expressions (physics.h:160-264,
+# solver.h:308-356, 428-469, 517-593, 745-828), per interior face and per
+# cell of ONE iteration (three RK stages) as the GPU path forms it: the
+# gradient (formed from the stage-0 state, the same in every stage) and the
+# time step once per iteration; limiter, reconstruction and flux per stage.
+FLUX_OPS = 207        # internal_flux, inviscid: 18 divisions, 6 square roots
+RECON_OPS = 44        # q +- phi (grad q . d), both sides
+FLUX_SCATTER_OPS = 12  # F*L and the two accumulations
+LIMITER_OPS = 230     # Venkatakrishnan, both sides of the face
+GRADIENT_OPS = 73     # Green-Gauss face term (weights, vars(), 4 x 13)
+DT_OPS = 38           # spectral radius of both sides, accumulation
+CELL_OPS = 70         # gradient / area, dt, 3 x (residual / area + update)
+
+
+def fp64_ops_per_iteration(n, f):
+    per_face = 3 * (FLUX_OPS + RECON_OPS + FLUX_SCATTER_OPS + LIMITER_OPS) + GRADIENT_OPS + DT_OPS
+    return f * per_face + n * CELL_OPS
+
+
 def run_lean(args):
     """Warm-up + K iterations and nothing else (the command profiled by ncu)."""
     from aeroflex_gb300 import meshgen, rans
@@ -236,8 +268,10 @@ def run_gpu(args):
     q0 = meshgen.density_bump_state(marr, mach=MACH)
     m = rans.mesh.from_arrays(marr)
     N, F = m.nRealCells, m.n_edges
+    G = m.n_boundary
     setup_s = time.time() - t0
     hbm_peak, peak_kind = _peaks()
+    fp64_peak = rans.measure_fp64_peak(5)
     result = {}
     for precision in ("fp32-mixed", "fp64"):
         g = _setup_gpu(precision, m, q0)
@@ -264,9 +298,8 @@ def run_gpu(args):
         launches_per_iter = sum(v[1] for v in prof.values()) / n_prof
         entry = dict(value=evals, ms_per_step=sec / K * 1e3, steps=K, tuned=tuned,
                      kernels={k: dict(ms_total=v[0], launches=v[1], share=v[0] / tot) for k, v in prof.items()},
-                     # the FP64 path is bound by the FP64 pipe (87% active under ncu,
-                     # profiles/k_face_flux_fp64_channel1024x512.md): its HBM
-                     # fraction is reported for reference only
+                     # the FP64 path is bound by the FP64 pipe (87% active under
+                     # ncu): its HBM fraction is reported for reference only
                      roofline=dict(kernel=kname, bound="hbm" if precision == "fp32-mixed" else "fp64-pipe",
                                    achieved=achieved, peak=hbm_peak, unit="GB/s",
                                    frac=achieved / hbm_peak, peak_source=peak_kind,
@@ -275,21 +308,39 @@ def run_gpu(args):
                      gpu_launches=int(round(launches_per_iter * K)))
         if precision == "fp32-mixed":
             entry["clocks"] = ck
-            # end-to-end through the C ABI: host state -> device, iterate, norm back
-            qh = torch.from_numpy(q0.copy()).pin_memory().numpy() if torch.cuda.is_available() else q0.copy()
-            Ke = max(3, min(args.steps, 20))
+        # end-to-end through the C ABI, every step: the host state (pinned)
+        # to the device, one iteration, the updated state and the residual
+        # norm back to pinned host memory
+        qh = torch.from_numpy(q0.copy()).pin_memory().numpy() if torch.cuda.is_available() else q0.copy()
+        qo = torch.empty(q0.size, dtype=torch.float64).pin_memory().numpy() if torch.cuda.is_available() \
+            else np.empty_like(q0)
+        Ke = max(3, min(args.steps if precision == "fp32-mixed" else K, 20))
+        g.set_q(qh)
+        g.iterate(1)
+        g.get_q(qo)
+        t1 = time.perf_counter()
+        for _ in range(Ke):
             g.set_q(qh)
             g.iterate(1)
-            t1 = time.perf_counter()
-            for _ in range(Ke):
-                g.set_q(qh)
-                g.iterate(1)
-            e2e_s = (time.perf_counter() - t1) / Ke
-            entry["e2e"] = dict(value=N * 3 / e2e_s, unit="cell-residual evals/s", h2d_bytes_per_step=N * 32,
-                                d2h_bytes_per_step=8, ms_per_step=e2e_s * 1e3, steps=Ke)
+            g.get_q(qo)
+        e2e_s = (time.perf_counter() - t1) / Ke
+        entry["e2e"] = dict(value=N * 3 / e2e_s, unit="cell-residual evals/s", h2d_bytes_per_step=N * 32,
+                            d2h_bytes_per_step=N * 32 + 8, ms_per_step=e2e_s * 1e3, steps=Ke)
+        # the whole evaluation against the compulsory bytes of one evaluation
+        eb = evaluation_bytes(N, G, F, precision)
+        entry["roofline_evaluation"] = dict(bytes_per_evaluation=eb, achieved=eb * 3 / (sec / K) / 1e9,
+                                            peak=hbm_peak, unit="GB/s",
+                                            frac=eb * 3 / (sec / K) / 1e9 / hbm_peak, peak_source=peak_kind)
+        if precision == "fp64":
+            ops = fp64_ops_per_iteration(N, F)
+            entry["fp64_ops"] = dict(ops_per_iteration=ops, achieved_tflops=ops / (sec / K) / 1e12,
+                                     peak_tflops=fp64_peak, frac=ops / (sec / K) / 1e12 / fp64_peak if fp64_peak else None,
+                                     peak_source="measured live: FP64 FMA chains (afx_measure_fp64_peak), "
+                                                 "2 flops per FMA; the bit-exact path is compiled without FMA "
+                                                 "contraction, so at most half of it is reachable")
         result[precision] = entry
         del g
-    return dict(N=N, F=F, setup_s=setup_s, res=result)
+    return dict(N=N, F=F, setup_s=setup_s, res=result, fp64_peak=fp64_peak)
 
 
 def time_to_cl(budget_s=60.0):
@@ -560,30 +611,51 @@ def cpu_baseline(budget_s=12.0):
                             "path's count, bit-identical arithmetic) x the measured time per iteration"}
 
 
+def workload_config(n, f, world=1):
+    """The config object both arms print (the same workload)."""
+    return {"workload": "channel 2048x1024 quads -> %d shuffled triangles, M 0.3 density bump, explicit "
+                        "second-order residual (Green-Gauss, Venkatakrishnan K 5, Roe), CFL 1" % n,
+            "cells": n, "faces": f, "l2": "inputs larger than L2 (~1 GB touched per step)",
+            "parallelism": "replicas" if world > 1 else "single GPU"}
+
+
 def run_reference(args):
+    """The reference's CPU implementation of the path on the machine's host
+    cores: the oracle port (bit-identical to the reference's own code on the
+    committed pins; the reference's tree is not on the box), all host
+    threads, on the full channel mesh of the GPU arm.  One step = one
+    second-order residual evaluation of every cell (time step, gradient,
+    limiter, face loop), the unit the GPU arm counts three times per
+    iteration."""
     from aeroflex_gb300 import meshgen
     from oracle import oracle
 
-    marr = meshgen.channel(SAMPLE_NX, SAMPLE_NY, jitter=0.2, seed=1, shuffle_seed=2)
-    s = oracle.Solver(oracle.Mesh.from_arrays(marr), oracle.default_settings(cfl=1.0), {
+    marr = meshgen.channel(args.nx, args.ny, jitter=0.2, seed=1, shuffle_seed=2)
+    om = oracle.Mesh.from_arrays(marr)
+    s = oracle.Solver(om, oracle.default_settings(cfl=1.0), {
         "farfield": dict(type="farfield", T=1.0, mach=MACH, angle=0.0, p=1.0), "wall": dict(type="slip-wall")})
     s.init()
     s.set_q(meshgen.density_bump_state(marr, mach=MACH))
-    n = SAMPLE_NX * SAMPLE_NY * 2
-    for _ in range(args.warmup):
+    n, f = om.n_real, om.n_edges
+    oracle.set_threads(0)
+    t_first = s.time_residuals(1)
+    for _ in range(args.warmup - 1):
         s.time_residuals(1)
-    sec = s.time_residuals(args.steps)
-    v = n * args.steps / sec
+    # a step is a full-mesh evaluation (about 2 s on 16 cores): large step
+    # counts are cut to what fits in about two minutes, and the line says so
+    steps = max(1, min(args.steps, int(120.0 / max(t_first, 1e-3))))
+    sec = s.time_residuals(steps)
+    v = n * steps / sec
     line = {"metric": "cell-residual evals/s", "value": v, "unit": "cell-residual evals/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec / args.steps * 1e3,
+            "steps": steps, "steps_requested": args.steps, "warmup": args.warmup,
+            "ms_per_step": sec / steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": "channel 2048x1024 -> 4,194,304 shuffled triangles, M 0.3 density bump; "
-                                   "reference step = one second-order residual evaluation (dt, gradient, "
-                                   "limiter, face loop) on the %dx%d sample (%d cells)" % (SAMPLE_NX, SAMPLE_NY, n)},
+            "config": workload_config(n, f),
             "cpu_baseline": {"value": v, "unit": "cell-residual evals/s", "cores": os.cpu_count(), "kind": "port",
-                             "sample": "%d residual evaluations on the %dx%d channel sample" %
-                                       (args.steps, SAMPLE_NX, SAMPLE_NY)},
+                             "sample": "%d second-order residual evaluations of the full %d-cell channel, all %d "
+                                       "host threads (OpenMP per-cell loops, serial face loops, as the reference)"
+                                       % (steps, n, os.cpu_count())},
             "e2e": {"value": v, "unit": "cell-residual evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -651,19 +723,19 @@ def main():
         "steps": f32["steps"], "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32-mixed (f32 flux/gradient/limiter, f64 update/norm)",
         "data": "synthetic",
-        "config": {"workload": "channel 2048x1024 quads -> %d shuffled triangles, M 0.3 density bump, explicit "
-                               "RK3 second order, CFL 1" % r["N"], "cells": r["N"], "faces": r["F"],
-                   "precision": "fp32-mixed", "l2": "inputs larger than L2 (~1 GB touched per step)",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": workload_config(r["N"], r["F"], world),
         "roofline": {k: f32["roofline"][k] for k in ("bound", "achieved", "peak", "unit", "frac", "traffic")},
         "roofline_kernel": f32["roofline"],
+        "roofline_evaluation": f32["roofline_evaluation"],
         "kernels": f32["kernels"],
         "clocks": f32["clocks"],
         "e2e": f32["e2e"],
         "gpu_launches": f32["gpu_launches"],
         "tuned": f32["tuned"],
-        "fp64": {"value": f64["value"], "ms_per_step": f64["ms_per_step"], "steps": f64["steps"],
-                 "tuned": f64["tuned"],
+        # the bit-exact FP64 path (the reference's arithmetic), same workload
+        "fp64": {"value": f64["value"], "unit": "cell-residual evals/s", "ms_per_step": f64["ms_per_step"],
+                 "steps": f64["steps"], "dtype": "f64", "e2e": f64["e2e"], "tuned": f64["tuned"],
+                 "fp64_ops": f64["fp64_ops"], "roofline_evaluation": f64["roofline_evaluation"],
                  "roofline_kernel": f64["roofline"], "kernels": f64["kernels"], "gpu_launches": f64["gpu_launches"]},
         "setup_s": r["setup_s"],
     }
