@@ -276,3 +276,24 @@ def test_wall_distance_bitexact(afx, orc, case):
     so = oracle_solver(orc, m, bcs)
     g = gpu_solver(afx, m, bcs)
     np.testing.assert_array_equal(g.wall_distance(), so.wall_distance())
+
+
+def test_full_size_channel_fp64_bitexact(afx, orc):
+    """The benchmark's workload at full size (2048 x 1024 quads -> 4,194,304
+    shuffled triangles, density bump): the FP64 residual and one explicit
+    iteration bit for bit against the oracle, face-flux and tile variants."""
+    m, bcs, q = channel_case(2048, 1024)
+    so = oracle_solver(orc, m, bcs)
+    so.init()
+    so.set_q(q)
+    R0 = so.residual()
+    so.iterate(1)
+    q1 = so.q()
+    for kv in ("face", "tile"):
+        g = gpu_solver(afx, m, bcs, kernel_variant=kv)
+        g.init()
+        g.set_q(q)
+        assert np.array_equal(g.residual(), R0), kv
+        g.iterate(1)
+        assert np.array_equal(g.get_q(), q1), kv
+        del g

@@ -50,13 +50,13 @@ def test_gpu_explicit_path_reproduces_the_reference(afx, kv):
             ok = _close(g, v, 1e-12)
         if not ok:
             bad.append(k)
-    assert not bad, bad
+    assert not bad, " ".join(bad)
 
 
 def test_gpu_implicit_rhs_reproduces_the_reference(afx):
     got = refpins.implicit_rhs_pins(refpins.GpuDriver(afx))
     bad = [k for k, v in PINS["implicit_rhs"].items() if got[k] != v]
-    assert not bad, bad
+    assert not bad, " ".join(bad)
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32-mixed"])
