@@ -272,3 +272,122 @@ def polar_sweep_cases(n_cases=256, seed=4, n_min=5000, n_max=200000, split=False
         mesh = airfoil_omesh(n_surf=n_surf, n_rad=n_rad, m=m, p=p, t=t, split=split, fade=2)
         out.append(dict(mesh=mesh, m=m, t=t, p=p, aoa_deg=aoa, mach=mach, n_cells=len(mesh["cells"])))
     return out
+
+
+def _inside_polygon(px, py, vx, vy):
+    """Even-odd test of points (px, py) against the closed polygon (vx, vy)."""
+    inside = np.zeros(px.shape, bool)
+    n = len(vx)
+    for i in range(n):
+        x0, y0, x1, y1 = vx[i], vy[i], vx[(i + 1) % n], vy[(i + 1) % n]
+        crosses = (y0 > py) != (y1 > py)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            xi = x0 + (py - y0) * (x1 - x0) / (y1 - y0)
+        inside ^= crosses & (px < xi)
+    return inside
+
+
+def hybrid_airfoil(n_surf=512, bl_layers=60, first=1e-6, growth=1.1, r_far=100.0, fill_cells=170000, t=0.12,
+                   seed=2, shuffle_seed=2):
+    """Hybrid RANS mesh around a NACA 4-digit airfoil of chord 1: a
+    structured boundary layer of ``bl_layers`` quad layers (first height
+    ``first`` chords, geometric ``growth``) on ``n_surf`` cosine-spaced
+    surface nodes, inside an unstructured triangular fill out to a circular
+    far field of radius ``r_far`` chords centred at mid-chord.
+
+    The fill is the Delaunay triangulation of the boundary layer's outer
+    ring and of rings of points between it and the far-field circle (ring
+    spacing growing geometrically, point counts decreasing outward so the
+    triangles stay close to isotropic, tangential jitter from ``seed``),
+    with the triangles inside the boundary layer removed; the ring growth is
+    chosen so the fill has about ``fill_cells`` triangles.  Cells are
+    shuffled with ``shuffle_seed``.  Patches: "wall" and "farfield"."""
+    from scipy.spatial import Delaunay
+
+    sx, sy = naca4_surface(n_surf, 0.0, 0.4, t)
+    tx = np.roll(sx, -1) - np.roll(sx, 1)
+    ty = np.roll(sy, -1) - np.roll(sy, 1)
+    tn = np.hypot(tx, ty)
+    nx_, ny_ = ty / tn, -tx / tn
+    h = first * (growth ** np.arange(bl_layers + 1) - 1.0) / (growth - 1.0)
+    BX = sx[None, :] + h[:, None] * nx_[None, :]
+    BY = sy[None, :] + h[:, None] * ny_[None, :]
+    H, last = h[-1], h[-1] - h[-2]
+    ex, ey = BX[-1], BY[-1]  # outer ring of the boundary layer
+    ang0 = np.arctan2(ey, ex - 0.5)
+    n_far = 128
+
+    def rings(ratio):
+        """Fill rings at distance d from the layer's edge, blended from the
+        normal offset to the far-field circle, then the far-field ring."""
+        rng = np.random.default_rng(seed)
+        pts, d, step = [], 0.0, last * growth
+        while True:
+            d += step
+            s = min(d / r_far, 1.0)
+            if s >= 1.0:
+                break
+            per = 2 * np.pi * (0.5 + s * r_far)
+            n_k = int(min(n_surf, max(32, round(per / step))))
+            if n_k == n_surf:
+                px = (1 - s) * (ex + d * nx_) + s * (0.5 + r_far * np.cos(ang0))
+                py = (1 - s) * (ey + d * ny_) + s * (r_far * np.sin(ang0))
+            else:
+                a = ang0[0] + 2 * np.pi * (np.arange(n_k) + rng.uniform(-0.25, 0.25, n_k)) / n_k
+                rad = np.interp(np.mod(a - ang0[0], 2 * np.pi), np.mod(ang0 - ang0[0], 2 * np.pi),
+                                np.hypot(ex - 0.5, ey), period=2 * np.pi)
+                px = 0.5 + ((1 - s) * (rad + d) + s * r_far) * np.cos(a)
+                py = ((1 - s) * (rad + d) + s * r_far) * np.sin(a)
+            pts.append((px, py))
+            step *= ratio
+        a = 2 * np.pi * np.arange(n_far) / n_far
+        pts.append((0.5 + r_far * np.cos(a), r_far * np.sin(a)))
+        return pts
+
+    lo, hi = 1.005, 1.5
+    for _ in range(40):  # ring growth ratio for the requested fill size (points ~ triangles / 2)
+        mid = 0.5 * (lo + hi)
+        n_pts = sum(len(p[0]) for p in rings(mid))
+        lo, hi = (mid, hi) if n_pts > fill_cells / 2 else (lo, mid)
+    rr = rings(0.5 * (lo + hi))
+    fx = np.concatenate([ex] + [p[0] for p in rr])
+    fy = np.concatenate([ey] + [p[1] for p in rr])
+    tri = Delaunay(np.stack([fx, fy], -1)).simplices
+    keep = ~_inside_polygon(fx[tri].mean(1), fy[tri].mean(1), ex, ey)
+    tri = tri[keep]
+    # every edge of the layer's outer ring and of the far-field circle must be
+    # an edge of exactly one kept triangle (a conforming mesh)
+    e = np.sort(np.concatenate([tri[:, [0, 1]], tri[:, [1, 2]], tri[:, [2, 0]]]), 1)
+    key = e[:, 0].astype(np.int64) * len(fx) + e[:, 1]
+    uniq, cnt = np.unique(key, return_counts=True)
+    cmap = dict(zip(uniq.tolist(), cnt.tolist()))
+    j = np.arange(n_surf)
+    ring_e = np.sort(np.stack([j, (j + 1) % n_surf], -1), 1)
+    far0 = len(fx) - n_far
+    k = np.arange(n_far)
+    far_e = np.sort(np.stack([far0 + k, far0 + (k + 1) % n_far], -1), 1)
+    for name, edges in (("boundary-layer edge", ring_e), ("far field", far_e)):
+        bad = [tuple(x) for x in edges if cmap.get(int(x[0]) * len(fx) + int(x[1]), 0) != 1]
+        if bad:
+            raise RuntimeError("hybrid_airfoil: %d %s edges not recovered by the triangulation" % (len(bad), name))
+    # assemble: boundary-layer nodes (ring-major), then the fill's own nodes
+    nbl = (bl_layers + 1) * n_surf
+    fill_map = np.concatenate([bl_layers * n_surf + j, nbl + np.arange(len(fx) - n_surf)])
+    x = np.concatenate([BX.reshape(-1), fx[n_surf:]])
+    y = np.concatenate([BY.reshape(-1), fy[n_surf:]])
+    kk, jj = np.meshgrid(np.arange(bl_layers), np.arange(n_surf), indexing="ij")
+    a = kk * n_surf + jj
+    b = kk * n_surf + (jj + 1) % n_surf
+    c = (kk + 1) * n_surf + (jj + 1) % n_surf
+    d = (kk + 1) * n_surf + jj
+    quads = np.stack([a, b, c, d], -1).reshape(-1, 4)
+    tris = np.concatenate([fill_map[tri], np.full((len(tri), 1), -1)], 1)
+    cells = np.concatenate([quads, tris]).astype(np.int32)
+    if shuffle_seed is not None:
+        cells = cells[np.random.default_rng(shuffle_seed).permutation(len(cells))]
+    wall = np.stack([j, (j + 1) % n_surf], -1)
+    far = np.stack([fill_map[far0 + k], fill_map[far0 + (k + 1) % n_far]], -1)
+    bedges = np.concatenate([wall, far]).astype(np.int32)
+    bpatch = np.concatenate([np.zeros(n_surf), np.ones(n_far)]).astype(np.int32)
+    return dict(x=x, y=y, cells=cells, bedges=bedges, bpatch=bpatch, names=["wall", "farfield"],
+                n_bl_quads=len(quads), n_fill_triangles=len(tri), bl_thickness=H)

@@ -13,7 +13,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "liboracle.so")
-SOURCES = ["rans_oracle.cpp", "oracle_capi.cpp"]
+SOURCES = ["rans_oracle.cpp", "sa_oracle.cpp", "oracle_capi.cpp"]
 
 
 def _stale():

@@ -51,6 +51,8 @@ def lib():
         L.orc_refill_bcs.argtypes = [vp]
         L.orc_set_farfield.argtypes = [vp, cp, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double]
         L.orc_set_q.argtypes = [vp, vp]
+        L.orc_set_nu.argtypes = [vp, vp]
+        L.orc_sa_source.argtypes = [ctypes.c_double] * 4 + [vp, vp]
         L.orc_prolongate.argtypes = [vp, vp]
         L.orc_set_threads.argtypes = [ip]
         L.orc_wall_distance.restype = ctypes.c_longlong
@@ -223,6 +225,19 @@ class Solver:
     def q(self):
         return self.get("q")[: 4 * self.n_real].copy()
 
+    def set_nu(self, nu):
+        """nu~ of the real cells (Spalart-Allmaras)."""
+        nu = np.ascontiguousarray(nu, np.float64).reshape(-1)
+        assert nu.size == self.n_real
+        lib().orc_set_nu(self.h, _ptr(nu))
+
+    def nu(self):
+        return self.get("nu")[: self.n_real].copy()
+
+    def nu_residual(self):
+        """nuW of the last residual or stage (per real cell)."""
+        return self.get("nuW")[: self.n_real].copy()
+
     def residual(self):
         R = np.empty(4 * self.n_real, np.float64)
         if lib().orc_residual(self.h, _ptr(R)):
@@ -261,6 +276,13 @@ class Solver:
 
     def time_residuals(self, n):
         return lib().orc_time_residuals(self.h, n)
+
+
+def sa_source(nut, nul, omega, d):
+    """Spalart-Allmaras source P - D of one cell and its derivative in nu~."""
+    src, dsrc = ctypes.c_double(), ctypes.c_double()
+    lib().orc_sa_source(float(nut), float(nul), float(omega), float(d), ctypes.byref(src), ctypes.byref(dsrc))
+    return src.value, dsrc.value
 
 
 def set_threads(n):

@@ -171,7 +171,6 @@ void* orc_solver_create(void* mp, const orc_settings* s, int n_bc, const char** 
         st.relaxation = s->relaxation;
         st.tolerance = s->tolerance;
         st.max_iterations = s->max_iterations;
-        if (st.viscosity == VISC_SA) throw std::runtime_error("SA model not in the oracle yet");
         for (int i = 0; i < n_bc; ++i) {
             BoundaryCondition bc;
             bc.type = types[i];
@@ -195,6 +194,7 @@ void orc_init(void* sp) {
     auto* s = (ExplicitSolver*)sp;
     s->init();
     s->refill_bcs();
+    if (s->st.viscosity == VISC_SA) s->sa_init();
 }
 
 void orc_refill_bcs(void* sp) { ((ExplicitSolver*)sp)->refill_bcs(); }
@@ -235,6 +235,17 @@ long long orc_wall_distance(void* sp, double* out) {
     return (long long)s->m.wall_dist.size();
 }
 
+// nu~ of the real cells (Spalart-Allmaras solvers).
+void orc_set_nu(void* sp, const double* nu_real) {
+    auto* s = (ExplicitSolver*)sp;
+    std::memcpy(s->nu.data(), nu_real, (size_t)s->m.nRealCells * sizeof(double));
+}
+
+// The Spalart-Allmaras source of one cell and its derivative.
+void orc_sa_source(double nut, double nul, double omega, double d, double* src, double* dsrc) {
+    sa_source(nut, nul, omega, d, src, dsrc);
+}
+
 void orc_set_q(void* sp, const double* q_real) {
     auto* s = (ExplicitSolver*)sp;
     std::memcpy(s->q.data(), q_real, 4 * (size_t)s->m.nRealCells * sizeof(double));
@@ -250,6 +261,9 @@ long long orc_get(void* sp, const char* what, double* out) {
     else if (w == "gx") v = &s->gx;
     else if (w == "gy") v = &s->gy;
     else if (w == "lim") v = &s->limiters;
+    else if (w == "nu" && s->st.viscosity == VISC_SA) v = &s->nu;
+    else if (w == "nuW" && s->st.viscosity == VISC_SA) v = &s->nuW;
+    else if (w == "mut" && s->st.viscosity == VISC_SA) v = &s->mut;
     if (!v) return -1;
     if (out) std::memcpy(out, v->data(), v->size() * sizeof(double));
     return (long long)v->size();
@@ -268,7 +282,10 @@ int orc_residual(void* sp, double* R_out) {
             s->calc_gradients();
             if (s->st.second_order) s->calc_limiters(s->qk);
         }
+        const bool sa = s->st.viscosity == VISC_SA;
+        if (sa) s->calc_mut(s->qk, s->nu);
         s->calc_residual(s->qk);
+        if (sa) s->calc_nu_residual(s->qk, s->nu);
         if (R_out) std::memcpy(R_out, s->qW.data(), 4 * (size_t)s->m.nRealCells * sizeof(double));
         return 0;
     } catch (const std::exception& e) {

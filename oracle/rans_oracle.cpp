@@ -346,36 +346,41 @@ void internal_flux(const Gas& g, double nx, double ny, int viscous_type, const d
     f[3] -= 0.5 * (kF1 * (h - c * V) + kF234_0 * q2 * 0.5 + kF234_1 * (u * (uR - uL) + v * (vR - vL) - V * (VR - VL)) +
                    kF5 * (h + c * V));
 
-    if (viscous_type == 1) {
-        double qc[4];
-        for (int k = 0; k < 4; ++k) qc[k] = 0.5 * (qL[k] + qR[k]);
-        // calc_grad_temp -> calc_p, calc_grad_p (physics.h:33-68)
-        const double p = (g.gamma - 1) * (qc[3] - 0.5 / qc[0] * (qc[1] * qc[1] + qc[2] * qc[2]));
-        double gp0 = 2. * gx[3];
-        gp0 -= gx[1] * qc[1] / qc[0] + qc[1] * (gx[1] * qc[0] - gx[0] * qc[1]) / (qc[0] * qc[0]);
-        gp0 -= gx[2] * qc[2] / qc[0] + qc[2] * (gx[2] * qc[0] - gx[0] * qc[2]) / (qc[0] * qc[0]);
-        gp0 *= 0.5 * (g.gamma - 1);
-        double gp1 = 2. * gy[3];
-        gp1 -= gy[1] * qc[1] / qc[0] + qc[1] * (gy[1] * qc[0] - gy[0] * qc[1]) / (qc[0] * qc[0]);
-        gp1 -= gy[2] * qc[2] / qc[0] + qc[2] * (gy[2] * qc[0] - gy[0] * qc[2]) / (qc[0] * qc[0]);
-        gp1 *= 0.5 * (g.gamma - 1);
-        const double gT0 = (1. / g.R) * ((gp0 * qc[0] - gx[0] * p) / (qc[0] * qc[0]));
-        const double gT1 = (1. / g.R) * ((gp1 * qc[0] - gy[0] * p) / (qc[0] * qc[0]));
-        // calc_grad_u / calc_grad_v (physics.h:70-82)
-        const double gu0 = (qc[0] * gx[1] - qc[1] * gx[0]) / (qc[0] * qc[0]);
-        const double gu1 = (qc[0] * gy[1] - qc[1] * gy[0]) / (qc[0] * qc[0]);
-        const double gv0 = (qc[0] * gx[2] - qc[2] * gx[0]) / (qc[0] * qc[0]);
-        const double gv1 = (qc[0] * gy[2] - qc[2] * gy[0]) / (qc[0] * qc[0]);
-        const double div_v = gu0 + gv1;
-        const double tau_xx = 2. * g.mu_L * (gu0 - div_v / 3.);
-        const double tau_yy = 2. * g.mu_L * (gv1 - div_v / 3.);
-        const double tau_xy = g.mu_L * (gu1 + gv0);
-        const double phi0 = qc[1] / qc[0] * tau_xx + qc[2] / qc[0] * tau_xy + g.k() * gT0;
-        const double phi1 = qc[1] / qc[0] * tau_xy + qc[2] / qc[0] * tau_yy + g.k() * gT1;
-        f[1] -= nx * tau_xx + ny * tau_xy;
-        f[2] -= nx * tau_xy + ny * tau_yy;
-        f[3] -= nx * phi0 + ny * phi1;
-    }
+    if (viscous_type == 1) laminar_terms(g, g.mu_L, g.k(), nx, ny, qL, qR, gx, gy, f);
+}
+
+// Laminar branch of internal_flux (physics.h:230-258 with calc_grad_p /
+// temp / u / v, physics.h:33-82) for viscosity mu and heat conductivity
+// kheat: the reference passes g.mu_L and g.k(); the Spalart-Allmaras flux
+// passes the face's mu + mu_t and cp (mu / Pr_L + mu_t / Pr_T).
+void laminar_terms(const Gas& g, double mu, double kheat, double nx, double ny, const double qL[4],
+                   const double qR[4], const double gx[4], const double gy[4], double f[4]) {
+    double qc[4];
+    for (int k = 0; k < 4; ++k) qc[k] = 0.5 * (qL[k] + qR[k]);
+    const double p = (g.gamma - 1) * (qc[3] - 0.5 / qc[0] * (qc[1] * qc[1] + qc[2] * qc[2]));
+    double gp0 = 2. * gx[3];
+    gp0 -= gx[1] * qc[1] / qc[0] + qc[1] * (gx[1] * qc[0] - gx[0] * qc[1]) / (qc[0] * qc[0]);
+    gp0 -= gx[2] * qc[2] / qc[0] + qc[2] * (gx[2] * qc[0] - gx[0] * qc[2]) / (qc[0] * qc[0]);
+    gp0 *= 0.5 * (g.gamma - 1);
+    double gp1 = 2. * gy[3];
+    gp1 -= gy[1] * qc[1] / qc[0] + qc[1] * (gy[1] * qc[0] - gy[0] * qc[1]) / (qc[0] * qc[0]);
+    gp1 -= gy[2] * qc[2] / qc[0] + qc[2] * (gy[2] * qc[0] - gy[0] * qc[2]) / (qc[0] * qc[0]);
+    gp1 *= 0.5 * (g.gamma - 1);
+    const double gT0 = (1. / g.R) * ((gp0 * qc[0] - gx[0] * p) / (qc[0] * qc[0]));
+    const double gT1 = (1. / g.R) * ((gp1 * qc[0] - gy[0] * p) / (qc[0] * qc[0]));
+    const double gu0 = (qc[0] * gx[1] - qc[1] * gx[0]) / (qc[0] * qc[0]);
+    const double gu1 = (qc[0] * gy[1] - qc[1] * gy[0]) / (qc[0] * qc[0]);
+    const double gv0 = (qc[0] * gx[2] - qc[2] * gx[0]) / (qc[0] * qc[0]);
+    const double gv1 = (qc[0] * gy[2] - qc[2] * gy[0]) / (qc[0] * qc[0]);
+    const double div_v = gu0 + gv1;
+    const double tau_xx = 2. * mu * (gu0 - div_v / 3.);
+    const double tau_yy = 2. * mu * (gv1 - div_v / 3.);
+    const double tau_xy = mu * (gu1 + gv0);
+    const double phi0 = qc[1] / qc[0] * tau_xx + qc[2] / qc[0] * tau_xy + kheat * gT0;
+    const double phi1 = qc[1] / qc[0] * tau_xy + qc[2] / qc[0] * tau_yy + kheat * gT1;
+    f[1] -= nx * tau_xx + ny * tau_xy;
+    f[2] -= nx * tau_xy + ny * tau_yy;
+    f[3] -= nx * phi0 + ny * phi1;
 }
 
 // Ghost states: slip_wall_flux::vars (physics.h:311-339), wall_flux::vars
@@ -463,6 +468,7 @@ ExplicitSolver::ExplicitSolver(const Mesh& mesh, const Settings& s) : st(s), m(m
     qk.assign(4 * N, 0.);
     set_bcs(st.bcs);
     if (st.gradient == 0) calc_least_squares_matrices();
+    if (st.viscosity == VISC_SA) sa_setup();
 }
 
 void ExplicitSolver::set_bcs(const std::map<std::string, BoundaryCondition>& bcs) {  // solver.h:200-247
@@ -721,7 +727,12 @@ void ExplicitSolver::calc_limiters(const std::vector<double>& q_) {  // solver.h
 void ExplicitSolver::flux(int type, uint e, const double qL[4], const double qR[4], const double gradx[4],
                           const double grady[4], double f[4]) const {
     const double nx = m.edgesNormalsX[e], ny = m.edgesNormalsY[e];
-    if (two_sided(type)) {
+    if (two_sided(type) && st.viscosity == VISC_SA) {
+        internal_flux(st.g, nx, ny, 0, qL, qR, gradx, grady, f);
+        const double mut_f = 0.5 * (mut[m.edgesCells[e][0]] + mut[m.edgesCells[e][1]]);
+        laminar_terms(st.g, st.g.mu_L + mut_f, st.g.cp * (st.g.mu_L / st.g.Pr_L + mut_f / st.g.Pr_T), nx, ny, qL, qR,
+                      gradx, grady, f);
+    } else if (two_sided(type)) {
         internal_flux(st.g, nx, ny, flux_visc(), qL, qR, gradx, grady, f);
     } else {  // boundary functors call the internal flux without gradients (physics.h:298,363,431)
         double qb[4];
@@ -752,6 +763,7 @@ void ExplicitSolver::calc_residual(const std::vector<double>& q_) {  // solver.h
         } else {
             flux(edge_type[e], (uint)e, &q_[k0], &q_[k1], gradx, grady, f);
         }
+        if (st.viscosity == VISC_SA && edge_type[e] == BC_WALL) sa_wall_shear((uint)e, &q_[k0], f);
         const double L = m.edgesLengths[e];
         const bool ts = two_sided(edge_type[e]);
         for (int k = 0; k < 4; ++k) {
@@ -774,20 +786,29 @@ static double norm2(const std::vector<double>& v) {
 
 double ExplicitSolver::solve() {  // solver.h:802-828
     static const double alpha[3] = {0.25, 0.5, 1.};
+    const bool sa = st.viscosity == VISC_SA;
     calc_dt();
     qk = q;
+    if (sa) nuk = nu;
     for (double ai : alpha) {
         if (viscous_or_grad() || st.second_order) {
             set_walls_from_internal(qk);
             calc_gradients();
             if (st.second_order) calc_limiters(qk);
         }
+        // Spalart-Allmaras: eddy viscosity of the stage state, then the
+        // mean-flow and turbulence residuals of the same stage state
+        if (sa) calc_mut(qk, nuk);
         calc_residual(qk);
+        if (sa) calc_nu_residual(qk, nuk);
         for (uint i = 0; i < m.nRealCells; ++i)
             for (int j = 0; j < 4; ++j)
                 qk[4 * i + j] = q[4 * i + j] + qW[4 * i + j] * dt[i] * ai * st.relaxation;
+        if (sa)
+            for (uint i = 0; i < m.nRealCells; ++i) nuk[i] = nu[i] + nuW[i] * dt[i] * ai * st.relaxation;
     }
     q = qk;
+    if (sa) nu = nuk;
     return norm2(qW);
 }
 

@@ -150,6 +150,17 @@ class ExplicitSolver {
     double get_uniform_residual();                           // solver.h:636-690
     BoundaryVars get_boundary_variables() const;            // solver.h:597-611
     bool viscous_or_grad() const { return st.viscosity != VISC_INVISCID; }
+
+    // Spalart-Allmaras (VISC_SA, sa_oracle.cpp): nu~ per cell (ghosts
+    // unused), its stage copy and residual, the eddy viscosity mu_t per cell.
+    std::vector<double> nu, nuk, nuW, mut;
+    std::vector<std::array<uint, 4>> cellFaces;  // a real cell's edges, ascending, EDGE_NULL padded
+    double nu_far = 0.;                          // nu~ of the far field: 3 mu_L / rho_inf
+    void sa_setup();
+    void sa_init();                                                        // nu~ = nu_far
+    void calc_mut(const std::vector<double>& q_, const std::vector<double>& nu_);
+    void calc_nu_residual(const std::vector<double>& q_, const std::vector<double>& nu_);
+    void sa_wall_shear(uint e, const double q0[4], double f[4]) const;
     int flux_visc() const { return st.viscosity == VISC_LAMINAR ? 1 : 0; }
 
     // One explicit update as the driver loop does it, returning ‖qW‖₂.
@@ -174,6 +185,15 @@ WallProfile get_wall_profile(const ExplicitSolver& s, const std::string& patch);
 // multigrid::run, multigrid.h:295-363): coarse.bcs_from_internal(), fine.q =
 // mapper * coarse.q, fine.refill_bcs().
 void prolongate(ExplicitSolver& coarse, ExplicitSolver& fine);
+
+// Spalart-Allmaras source of one cell (sa_oracle.cpp): src = P - D and its
+// derivative with respect to nu~.
+void sa_source(double nut, double nul, double omega, double d, double* src, double* dsrc);
+double sa_cbrt(double x);
+
+// Laminar terms of internal_flux with viscosity mu and heat conductivity kheat.
+void laminar_terms(const Gas& g, double mu, double kheat, double nx, double ny, const double qL[4],
+                   const double qR[4], const double gx[4], const double gy[4], double f[4]);
 
 // Face-flux functors, physics.h:160-530.
 void internal_flux(const Gas& g, double nx, double ny, int viscous_type, const double qL[4],
