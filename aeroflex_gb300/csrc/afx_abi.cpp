@@ -433,10 +433,23 @@ struct afx_solver_s {
     // fill + compute + solve(relaxation, tol, rhs_iterations) of
     // implicitSolver (solver.h:1000-1213) at the given CFL; returns the final
     // ||RhoVector||, or -1 if the system could not be solved
+    // the mean-flow implicit iteration, then (Spalart-Allmaras) the
+    // segregated point-implicit nu~ updates at the new state
     double implicit_iteration(double cfl, double tol_abs) {
+        const double r = implicit_iteration_mean(cfl, tol_abs);
+        if (a.visc == 2 && r == r && r >= 0) {
+            StepArgs m = A64();
+            m.cfl = cfl;
+            enqueue_sa_implicit_f64(m, parity, 3, stream);
+        }
+        return r;
+    }
+
+    double implicit_iteration_mean(double cfl, double tol_abs) {
         StepArgs m = A64();
         m.cfl = cfl;
         if (a.n_cases > 0) m.ctrl = a.ctrl;  // a case stopped during the fill is counted on the run's control block
+        if (a.visc == 2) enqueue_sa_mut_f64(m, parity, stream);  // the frozen eddy viscosity of the fill
         implicit_fill(imp, m, parity, stream);
         imp_lin_iters = 0;
         auto solve_update = [&]() {
@@ -463,6 +476,71 @@ struct afx_solver_s {
             if (!solve_update()) return -1;
         }
         return imp_rhs(parity);
+    }
+
+    // Spalart-Allmaras arrays of machine x (device cell order): the FP64
+    // nu~ buffers are allocated once (own) and shared; the wall distance,
+    // centroids, ghost centroids and mu_t are in x's arithmetic type.
+    void sa_setup(StepArgs& x, bool f32, bool own) {
+        const size_t N = hl.n_cells, B = hl.n_bnd;
+        if (own) {
+            for (int p = 0; p < 2; ++p) {
+                x.sa_nu[p] = dalloc(N * 8);
+                x.sa_nus[p] = dalloc(N * 8);
+            }
+            x.sa_nuW = dalloc(N * 8);
+            double q[4];
+            conservative(st, freestream(), q);
+            x.sa_nu_far = 3. * st.mu_L / q[0];  // 3 nu_inf
+            std::vector<double> nu(N, x.sa_nu_far);
+            for (int p = 0; p < 2; ++p)
+                AFX_CUDA(cudaMemcpyAsync(x.sa_nu[p], nu.data(), N * 8, cudaMemcpyHostToDevice, stream));
+            AFX_CUDA(cudaStreamSynchronize(stream));
+        }
+        std::vector<double> wd_all = wall_distance_all();
+        std::vector<double> wd(N), cxy(2 * N), gxy(2 * std::max<size_t>(B, 1));
+        for (size_t i = 0; i < N; ++i) {
+            wd[i] = wd_all[hl.cell_old[i]];
+            cxy[2 * i] = dev_cx[i];
+            cxy[2 * i + 1] = dev_cy[i];
+        }
+        for (size_t b = 0; b < B; ++b) {  // the ghost of boundary edge b (mesh.h:744-787)
+            const uint32_t g = hm.edgesCells[hm.boundaryEdges[b]][1];
+            gxy[2 * b] = geo_cx[g];
+            gxy[2 * b + 1] = geo_cy[g];
+        }
+        x.sa_mut = dalloc(N * (f32 ? 4 : 8));
+        x.sa_wd = f32 ? dupload(cast_vec<float>(wd)) : dupload(wd);
+        x.sa_cxy = f32 ? dupload(cast_vec<float>(cxy)) : dupload(cxy);
+        x.sa_gxy = f32 ? dupload(cast_vec<float>(gxy)) : dupload(gxy);
+    }
+
+    // mesh::compute_wall_dist (mesh.h:794-830) on the GPU: every cell,
+    // ghosts included, reference order
+    std::vector<double> wall_distance_all() {
+        const int nc = (int)geo_area.size();
+        std::vector<double> w, wy;  // wall edge centres in boundary order, then x / y
+        for (size_t b = 0; b < bedges.size(); ++b)
+            if (boundary_type[b] == BC_WALL || boundary_type[b] == BC_SLIP_WALL) {
+                w.push_back(bedges[b].ex);
+                wy.push_back(bedges[b].ey);
+            }
+        const int nw = (int)w.size();
+        w.insert(w.end(), wy.begin(), wy.end());
+        std::vector<double> c(2 * (size_t)nc);
+        std::copy(geo_cx.begin(), geo_cx.end(), c.begin());
+        std::copy(geo_cy.begin(), geo_cy.end(), c.begin() + nc);
+        DevBuf dc, dw, dout;
+        dc.upload(c.data(), c.size() * 8, stream);
+        dw.upload(w.data(), std::max<size_t>(w.size(), 1) * 8, stream);
+        dout.alloc((size_t)nc * 8);
+        const double* pc = (const double*)dc.p;
+        const double* pw = (const double*)dw.p;
+        enqueue_wall_dist(nc, pc, pc + nc, nw, pw, pw + nw, (double*)dout.p, stream);
+        std::vector<double> out((size_t)nc);
+        AFX_CUDA(cudaMemcpyAsync(out.data(), dout.p, (size_t)nc * 8, cudaMemcpyDeviceToHost, stream));
+        AFX_CUDA(cudaStreamSynchronize(stream));
+        return out;
     }
 
     // after FP64 updates of the master state, the FP32 shadow follows
@@ -1012,8 +1090,6 @@ static std::unique_ptr<afx_solver_s> make_solver(const HostMesh& m, const Device
             throw Error(AFX_ERR_CUDA, "no CUDA device available");
         auto s = std::make_unique<afx_solver_s>();
         s->st = st0;
-        if (s->st.viscosity_code() == VISC_SA)
-            throw Error(AFX_ERR_CONFIG, "spalart-allmaras is not available in this build");
         s->hm = m;
         s->hl = L;
         s->host_geometry();
@@ -1061,7 +1137,12 @@ static std::unique_ptr<afx_solver_s> make_solver(const HostMesh& m, const Device
         a.cfl = st.start_cfl;
         a.relax = st.relaxation;
         const int vc = st.viscosity_code();
-        a.visc = vc == VISC_LAMINAR ? 1 : 0;
+        a.visc = vc == VISC_LAMINAR ? 1 : (vc == VISC_SA ? 2 : 0);
+        a.cp = st.cp;
+        a.Pr_L = st.Pr_L;
+        a.Pr_T = st.Pr_T;
+        if (a.visc == 2 && (st.fp64_correction_interval > 0 || st.fp64_finish))
+            throw Error(AFX_ERR_CONFIG, "spalart-allmaras: fp64_correction_interval and fp64_finish are not available");
         a.second = st.second_order ? 1 : 0;
         a.need_grad = (st.second_order || vc != VISC_INVISCID) ? 1 : 0;
         a.limiter = st.limiter == "michalak" ? 1 : 0;
@@ -1099,7 +1180,10 @@ static std::unique_ptr<afx_solver_s> make_solver(const HostMesh& m, const Device
         a.ctrl = (Ctrl*)s->dalloc(sizeof(Ctrl));
         a.hist = (double*)s->dalloc(HIST_CAP * sizeof(double));
         s->d_cell_old.upload(L.cell_old.data(), N * sizeof(int), s->stream);
-        s->set_launch(variant, block);
+        // Spalart-Allmaras has the face and tile variants (the gather variant
+        // would re-form the eddy-viscous face terms on both sides)
+        s->set_launch(a.visc == 2 && variant == 0 ? 1 : variant, block);
+        if (a.visc == 2) s->sa_setup(a, !s->fp64, true);
         const bool implicit = st.solver == "implicit";
         if (!s->fp64 && (st.fp64_correction_interval > 0 || st.fp64_finish || implicit)) {
             // FP64 residual machine on the same FP64 master state
@@ -1131,6 +1215,7 @@ static std::unique_ptr<afx_solver_s> make_solver(const HostMesh& m, const Device
                 b.feL = s->dalloc(F * 8);
             }
             b.corr = nullptr;
+            if (a.visc == 2) s->sa_setup(b, false, false);  // FP64 copies of the typed SA arrays
             b.ctrl = (Ctrl*)s->dalloc(sizeof(Ctrl));  // zeroed, never set to done
             s->R32buf = s->dalloc(N * 32);
             if (s->corr_interval > 0) a.corr = s->dalloc(N * 16);
@@ -1201,10 +1286,57 @@ int afx_init_freestream(afx_solver s) {
         const size_t N = s->a.n_cells;
         for (size_t i = 0; i < N; ++i) std::memcpy(s->h_stage + 4 * i, q, 32);
         AFX_CUDA(cudaMemcpyAsync(s->a.qm[s->parity], s->h_stage, N * 32, cudaMemcpyHostToDevice, s->stream));
+        if (s->a.visc == 2) {  // nu~ = 3 nu_inf everywhere
+            AFX_CUDA(cudaStreamSynchronize(s->stream));
+            for (size_t i = 0; i < N; ++i) s->h_stage[i] = s->a.sa_nu_far;
+            AFX_CUDA(cudaMemcpyAsync(s->a.sa_nu[s->parity], s->h_stage, N * 8, cudaMemcpyHostToDevice, s->stream));
+        }
         s->sync_shadow(s->parity);
         s->shadow_stale = false;
         s->reset_phase();
         s->refill_bcs();
+        AFX_CUDA(cudaStreamSynchronize(s->stream));
+    });
+}
+
+// The reference's nu array (solver.h:55), unused there: nu~ of the
+// Spalart-Allmaras model per real cell, reference order.
+int afx_set_turbulence(afx_solver s, const double* nu, long long n) {
+    return guarded([&] {
+        if (!s || !nu) throw Error(AFX_ERR_ARG, "null argument");
+        if (s->a.visc != 2) throw Error(AFX_ERR_CONFIG, "not a spalart-allmaras solver");
+        const size_t N = s->a.n_cells;
+        if (n != (long long)N) throw Error(AFX_ERR_ARG, "size must be n_real_cells");
+        AFX_CUDA(cudaMemcpyAsync(s->d_stage.p, nu, N * 8, cudaMemcpyDefault, s->stream));
+        enqueue_permute_in1((int)N, (const int*)s->d_cell_old.p, s->d_stage.p, s->a.sa_nu[s->parity], s->stream);
+        s->reset_phase();
+        AFX_CUDA(cudaStreamSynchronize(s->stream));
+    });
+}
+
+int afx_get_turbulence(afx_solver s, double* nu, long long n) {
+    return guarded([&] {
+        if (!s || !nu) throw Error(AFX_ERR_ARG, "null argument");
+        if (s->a.visc != 2) throw Error(AFX_ERR_CONFIG, "not a spalart-allmaras solver");
+        const size_t N = s->a.n_cells;
+        if (n != (long long)N) throw Error(AFX_ERR_ARG, "size must be n_real_cells");
+        enqueue_permute_out1((int)N, (const int*)s->d_cell_old.p, s->a.sa_nu[s->parity], s->d_stage.p, s->stream);
+        AFX_CUDA(cudaMemcpyAsync(nu, s->d_stage.p, N * 8, cudaMemcpyDefault, s->stream));
+        AFX_CUDA(cudaStreamSynchronize(s->stream));
+    });
+}
+
+// nu~ residual R/A of the last evaluation (afx_residual: the current state;
+// an iteration: its last stage), reference order.
+int afx_turbulence_residual(afx_solver s, double* nuW, long long n) {
+    return guarded([&] {
+        if (!s || !nuW) throw Error(AFX_ERR_ARG, "null argument");
+        if (s->a.visc != 2) throw Error(AFX_ERR_CONFIG, "not a spalart-allmaras solver");
+        const size_t N = s->a.n_cells;
+        if (n != (long long)N) throw Error(AFX_ERR_ARG, "size must be n_real_cells");
+        enqueue_permute_out1((int)N, (const int*)s->d_cell_old.p, s->a.sa_nuW, s->d_stage.p, s->stream);
+        AFX_CUDA(cudaMemcpyAsync(nuW, s->d_stage.p, N * 8, cudaMemcpyDefault, s->stream));
+        AFX_CUDA(cudaStreamSynchronize(s->stream));
     });
 }
 
@@ -1586,9 +1718,13 @@ static void autotune_impl(afx_solver_s* s, int iters, char* variant, int cap, in
         s->materialize_qW();
         s->ensure_shadow();
         // keep the state: the timing runs start from it and it is put back after
-        DevBuf save, saveR;
+        DevBuf save, saveR, saveNu;
         save.alloc(N * 32);
         AFX_CUDA(cudaMemcpyAsync(save.p, a.qm[s->parity], N * 32, cudaMemcpyDeviceToDevice, s->stream));
+        if (a.visc == 2) {
+            saveNu.alloc(N * 8);
+            AFX_CUDA(cudaMemcpyAsync(saveNu.p, a.sa_nu[s->parity], N * 8, cudaMemcpyDeviceToDevice, s->stream));
+        }
         if (a.n_cases > 0) {  // a batch's iterations write qW
             saveR.alloc(N * 32);
             AFX_CUDA(cudaMemcpyAsync(saveR.p, a.Rq, N * 32, cudaMemcpyDeviceToDevice, s->stream));
@@ -1600,11 +1736,13 @@ static void autotune_impl(afx_solver_s* s, int iters, char* variant, int cap, in
         double best = 1e300;
         int best_var = a.variant, best_block = a.block;
         const int blocks[3] = {64, 128, 256};
-        for (int var = 0; var < 3; ++var) {
+        for (int var = a.visc == 2 ? 1 : 0; var < 3; ++var) {
             for (int bi = 0; bi < 3; ++bi) {
                 s->set_launch(var, blocks[bi]);
                 s->set_ctrl(0, 0, 0);
                 AFX_CUDA(cudaMemcpyAsync(a.qm[p0], save.p, N * 32, cudaMemcpyDeviceToDevice, s->stream));
+                if (a.visc == 2)
+                    AFX_CUDA(cudaMemcpyAsync(a.sa_nu[p0], saveNu.p, N * 8, cudaMemcpyDeviceToDevice, s->stream));
                 s->sync_shadow(p0);
                 int p = p0;
                 s->enqueue_iteration(p);  // warm-up
@@ -1631,6 +1769,7 @@ static void autotune_impl(afx_solver_s* s, int iters, char* variant, int cap, in
         for (auto& g : s->graphs) cudaGraphExecDestroy(g.second);
         s->graphs.clear();
         AFX_CUDA(cudaMemcpyAsync(a.qm[p0], save.p, N * 32, cudaMemcpyDeviceToDevice, s->stream));
+        if (a.visc == 2) AFX_CUDA(cudaMemcpyAsync(a.sa_nu[p0], saveNu.p, N * 8, cudaMemcpyDeviceToDevice, s->stream));
         if (a.n_cases > 0) AFX_CUDA(cudaMemcpyAsync(a.Rq, saveR.p, N * 32, cudaMemcpyDeviceToDevice, s->stream));
         s->sync_shadow(p0);
         s->set_ctrl(0, 0, 0);
@@ -1749,6 +1888,8 @@ int afx_batch_create(int n_cases, const afx_mesh* meshes, const afx_config* conf
         b->n = n_cases;
         // the scheme is shared: every case must agree with case 0 on it
         const Settings& s0 = configs[0] ? configs[0]->s : throw Error(AFX_ERR_ARG, "null config");
+        if (s0.viscosity_code() == VISC_SA)
+            throw Error(AFX_ERR_CONFIG, "spalart-allmaras cases run one solver each (no batch)");
         Settings st = s0;
         st.bcs.clear();
         st.bc_order.clear();

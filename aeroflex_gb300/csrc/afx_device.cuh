@@ -108,6 +108,10 @@ struct KM {
     int lsq;                          // least-squares gradient
     const V2<T>* __restrict__ lsqw;   // 4 per cell: (M d_j) of local edge j
     const int* __restrict__ lsqs;     // per cell: slot of local edge j (2 bits each), edge count << 8
+    // Spalart-Allmaras (VISC 2): eddy viscosity of the stage state per cell,
+    // and the gas constants of the turbulent heat conductivity
+    const T* __restrict__ mut;
+    T cp, PrL, PrT;
 };
 
 __device__ __forceinline__ bool two_sided(int bt) { return bt == BT_INTERNAL || bt == BT_INOUT; }
@@ -261,17 +265,35 @@ __device__ __forceinline__ void ghost_state(const int type, const T gamma, const
 // laminar term; wall/farfield faces through their ghost state without
 // gradients (physics.h:287-299, 352-364, 417-432).  With zero gradients the
 // laminar term is exactly zero, so boundary faces skip it.
+// VISC 2 (Spalart-Allmaras): the laminar terms with mu_L + mu_t,f and
+// cp (mu_L / Pr_L + mu_t,f / Pr_T), mu_t,f the mean of the face's two cells.
 template <class T, int VISC>
 __device__ __forceinline__ void face_flux(const KM<T>& m, const int bt, const T nx, const T ny, const T* qL,
-                                          const T* qR, const T* fgx, const T* fgy, T* f) {
+                                          const T* qR, const T* fgx, const T* fgy, T* f, const T mut_f = T(0)) {
     if (two_sided(bt)) {
         roe_flux(m.gamma, nx, ny, qL, qR, f);
         if (VISC == 1) laminar_flux(m.gamma, m.R, m.mu, m.kheat, nx, ny, qL, qR, fgx, fgy, f);
+        if (VISC == 2)
+            laminar_flux(m.gamma, m.R, m.mu + mut_f, m.cp * (m.mu / m.PrL + mut_f / m.PrT), nx, ny, qL, qR, fgx, fgy,
+                         f);
     } else {
         T qb[4];
         ghost_state(bt, m.gamma, nx, ny, qL, qR, qb);
         roe_flux(m.gamma, nx, ny, qL, qb, f);
     }
+}
+
+// Spalart-Allmaras no-slip wall: the wall shear mu_L u_t / delta of the cell
+// state q0 (u_t its tangential velocity, delta the distance from its centroid
+// to the wall face, d0 = face centre - centroid), added to the face flux F.
+template <class T>
+__device__ __forceinline__ void sa_wall_shear(const KM<T>& m, const T nx, const T ny, const T d0x, const T d0y,
+                                              const T* q0, T* f) {
+    const T delta = dabs(d0x * nx + d0y * ny);
+    const T u = q0[1] / q0[0], v = q0[2] / q0[0];
+    const T un = u * nx + v * ny;
+    f[1] += m.mu * (u - un * nx) / delta;
+    f[2] += m.mu * (v - un * ny) / delta;
 }
 
 // Spectral radius (c + |V_n|) of one side, solver.h:329-344.

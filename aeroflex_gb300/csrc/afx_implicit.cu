@@ -133,11 +133,14 @@ __device__ __forceinline__ void stop_case(const int* case_of, int* case_done, Ca
 // ------------------------------------------------------------- assembly
 // F of face f for the cell states (no reconstruction; the ghost side is the
 // stored boundary state), as the reference's flux functor evaluates it.
+// Spalart-Allmaras (VISC 2): the eddy viscosity is frozen at its current
+// value (mut_f) and the no-slip wall shear of the cell state is included.
 template <int VISC>
 __device__ __forceinline__ void flux_cells(const KM<double>& m, const int bt, const double nx, const double ny,
                                            const double* qL, const double* qR, const double* fgx, const double* fgy,
-                                           double* F) {
-    face_flux<double, VISC>(m, bt, nx, ny, qL, qR, fgx, fgy, F);
+                                           double* F, const double mut_f = 0.0, const double2 d0 = double2()) {
+    face_flux<double, VISC>(m, bt, nx, ny, qL, qR, fgx, fgy, F, mut_f);
+    if (VISC == 2 && bt == BT_WALL) sa_wall_shear(m, nx, ny, d0.x, d0.y, qL, F);
 }
 
 // calc_convective_jacobian (physics.h:533-578) times the face length:
@@ -163,7 +166,13 @@ __global__ void __launch_bounds__(128) k_imp_jac(const KM<double> m, const int n
         ld4(&m.bq[-cc.y - 1], qR);
     }
     double fgx[4] = {0, 0, 0, 0}, fgy[4] = {0, 0, 0, 0};
-    if (VISC == 1 && two_sided(bt)) {
+    double mut_f = 0.0;
+    double2 d0 = make_double2(0.0, 0.0);
+    if (VISC == 2) {
+        if (two_sided(bt)) mut_f = 0.5 * (__ldg(&m.mut[cc.x]) + __ldg(&m.mut[cc.y]));
+        d0 = __ldg(&m.fd0[f]);
+    }
+    if (VISC >= 1 && two_sided(bt)) {
         double gx0[4], gy0[4], gx1[4] = {0, 0, 0, 0}, gy1[4] = {0, 0, 0, 0};
         ld4(&gx[cc.x], gx0);
         ld4(&gy[cc.x], gy0);
@@ -174,14 +183,14 @@ __global__ void __launch_bounds__(128) k_imp_jac(const KM<double> m, const int n
         face_gradient(qL, qR, gx0, gy0, gx1, gy1, ldv4<double>(&m.ft[f]), fgx, fgy);
     }
     double f0[4];
-    flux_cells<VISC>(m, bt, n.x, n.y, qL, qR, fgx, fgy, f0);
+    flux_cells<VISC>(m, bt, n.x, n.y, qL, qR, fgx, fgy, f0, mut_f, d0);
     T* out = jf + 32 * (size_t)f;
 #pragma unroll 1
     for (int c = 0; c < 4; ++c) {
         const double upd = fmax(1e-6, fabs(qL[c]) * 1e-6);
         qL[c] += upd;
         double fp[4];
-        flux_cells<VISC>(m, bt, n.x, n.y, qL, qR, fgx, fgy, fp);
+        flux_cells<VISC>(m, bt, n.x, n.y, qL, qR, fgx, fgy, fp, mut_f, d0);
         qL[c] -= upd;
 #pragma unroll
         for (int r = 0; r < 4; ++r) out[4 * r + c] = (T)((fp[r] - f0[r]) / upd * L);
@@ -192,7 +201,7 @@ __global__ void __launch_bounds__(128) k_imp_jac(const KM<double> m, const int n
             const double upd = fmax(1e-6, fabs(qR[c]) * 1e-6);
             qR[c] += upd;
             double fp[4];
-            flux_cells<VISC>(m, bt, n.x, n.y, qL, qR, fgx, fgy, fp);
+            flux_cells<VISC>(m, bt, n.x, n.y, qL, qR, fgx, fgy, fp, mut_f, d0);
             qR[c] -= upd;
 #pragma unroll
             for (int r = 0; r < 4; ++r) out[16 + 4 * r + c] = (T)((fp[r] - f0[r]) / upd * L);
@@ -1061,6 +1070,8 @@ void fill_t(ImplicitEngine* e, const StepArgs& a, const dev::KM<double>& m, cons
     const int nf = nb_(a.n_faces, 128), nc = nb_(a.n_cells, 128);
     if (a.visc == 1)
         k_imp_jac<T, 1><<<nf, 128, 0, s>>>(m, a.n_faces, q, (const d4*)a.gx, (const d4*)a.gy, (T*)e->jf, a.ctrl);
+    else if (a.visc == 2)
+        k_imp_jac<T, 2><<<nf, 128, 0, s>>>(m, a.n_faces, q, (const d4*)a.gx, (const d4*)a.gy, (T*)e->jf, a.ctrl);
     else
         k_imp_jac<T, 0><<<nf, 128, 0, s>>>(m, a.n_faces, q, (const d4*)a.gx, (const d4*)a.gy, (T*)e->jf, a.ctrl);
     const Ell el = e->ell();
@@ -1080,7 +1091,7 @@ void implicit_fill(ImplicitEngine* e, const StepArgs& a0, int p, cudaStream_t s)
     StepArgs a = a0;
     a.variant = 0;  // the prep that also forms dt
     a.second = 0;   // gradients only when viscous (solver.h:1023-1026)
-    a.need_grad = a.visc == 1 ? 1 : 0;
+    a.need_grad = a.visc >= 1 ? 1 : 0;
     if (a.case_of && e->case_row_src != a.case_of) {
         // a batch: the case of each row, formed once
         if (!e->case_row && cudaMalloc((void**)&e->case_row, (size_t)std::max(e->N, 1) * sizeof(int)) != cudaSuccess)

@@ -487,12 +487,12 @@ __global__ void __launch_bounds__(256) k_resid_gather(const KM<T> m, const V4<S>
         const int4 nb = __ldg(&m.cnbr[i]);
         T qi[4], gxi[4] = {T(0), T(0), T(0), T(0)}, gyi[4] = {T(0), T(0), T(0), T(0)}, phii[4], qmi[4];
         ld4s(&qk[i], qi);
-        if (SECOND || VISC == 1) {
+        if (SECOND || VISC >= 1) {
             ld4c<T>(&gx[i], gxi);
             ld4c<T>(&gy[i], gyi);
         }
         if (SECOND) ld4c<T>(&phi[i], phii);
-        if (VISC == 1) ld4s(&qmem[i], qmi);
+        if (VISC >= 1) ld4s(&qmem[i], qmi);
         // rolled: the face flux is large, four inlined copies thrash the instruction cache
 #pragma unroll 1
         for (int s = 0; s < 4; ++s) {
@@ -520,7 +520,7 @@ __global__ void __launch_bounds__(256) k_resid_gather(const KM<T> m, const V4<S>
                 if (oc >= 0) {
                     T qo[4];
                     ld4s(&qk[oc], qo);
-                    if (SECOND || VISC == 1) {
+                    if (SECOND || VISC >= 1) {
                         ld4c<T>(&gx[oc], gxo);
                         ld4c<T>(&gy[oc], gyo);
                     }
@@ -543,7 +543,7 @@ __global__ void __launch_bounds__(256) k_resid_gather(const KM<T> m, const V4<S>
                     qR[k] = own0 ? qB[k] : qA[k];
                 }
                 T fgx[4] = {T(0), T(0), T(0), T(0)}, fgy[4] = {T(0), T(0), T(0), T(0)};
-                if (VISC == 1 && two_sided(bt)) {
+                if (VISC >= 1 && two_sided(bt)) {
                     T qmo[4];
                     if (oc >= 0) ld4s(&qmem[oc], qmo);
                     else ld4c<T>(&m.bq[-oc - 1], qmo);
@@ -560,7 +560,13 @@ __global__ void __launch_bounds__(256) k_resid_gather(const KM<T> m, const V4<S>
                     face_gradient(qa, qb, gxa, gya, gxb, gyb, ldv4<T>(&m.ft[f]), fgx, fgy);
                 }
                 T F[4];
-                face_flux<T, VISC>(m, bt, n.x, n.y, qL, qR, fgx, fgy, F);
+                T mut_f = T(0);
+                if (VISC == 2 && two_sided(bt)) mut_f = T(0.5) * (__ldg(&m.mut[i]) + __ldg(&m.mut[oc]));
+                face_flux<T, VISC>(m, bt, n.x, n.y, qL, qR, fgx, fgy, F, mut_f);
+                if (VISC == 2 && bt == BT_WALL) {
+                    const V2<T> d0 = __ldg(&m.fd0[f]);
+                    sa_wall_shear(m, n.x, n.y, d0.x, d0.y, qi, F);
+                }
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
                     const T fl = F[k] * L;
@@ -595,7 +601,7 @@ __device__ __forceinline__ void face_flux_at(const KM<T>& m, const int f, const 
     T gx0[4] = {T(0), T(0), T(0), T(0)}, gy0[4] = {T(0), T(0), T(0), T(0)};
     T gx1[4] = {T(0), T(0), T(0), T(0)}, gy1[4] = {T(0), T(0), T(0), T(0)};
     ld4s(&qk[cc.x], q0);
-    if (SECOND || VISC == 1) {
+    if (SECOND || VISC >= 1) {
         ld4c<T>(&gx[cc.x], gx0);
         ld4c<T>(&gy[cc.x], gy0);
     }
@@ -611,7 +617,7 @@ __device__ __forceinline__ void face_flux_at(const KM<T>& m, const int f, const 
     }
     if (cc.y >= 0) {
         ld4s(&qk[cc.y], q1);
-        if (SECOND || VISC == 1) {
+        if (SECOND || VISC >= 1) {
             ld4c<T>(&gx[cc.y], gx1);
             ld4c<T>(&gy[cc.y], gy1);
         }
@@ -642,7 +648,7 @@ __device__ __forceinline__ void face_flux_at(const KM<T>& m, const int f, const 
         *eLp = eig * L;
     }
     T fgx[4] = {T(0), T(0), T(0), T(0)}, fgy[4] = {T(0), T(0), T(0), T(0)};
-    if (VISC == 1 && two_sided(bt)) {
+    if (VISC >= 1 && two_sided(bt)) {
         T qa[4], qb[4];
         ld4s(&qmem[cc.x], qa);
         if (cc.y >= 0) ld4s(&qmem[cc.y], qb);
@@ -650,7 +656,13 @@ __device__ __forceinline__ void face_flux_at(const KM<T>& m, const int f, const 
         face_gradient(qa, qb, gx0, gy0, gx1, gy1, ldv4<T>(&m.ft[f]), fgx, fgy);
     }
     T F[4];
-    face_flux<T, VISC>(m, bt, n.x, n.y, qL, qR, fgx, fgy, F);
+    T mut_f = T(0);
+    if (VISC == 2 && two_sided(bt)) mut_f = T(0.5) * (__ldg(&m.mut[cc.x]) + __ldg(&m.mut[cc.y]));
+    face_flux<T, VISC>(m, bt, n.x, n.y, qL, qR, fgx, fgy, F, mut_f);
+    if (VISC == 2 && bt == BT_WALL) {
+        const V2<T> d0 = __ldg(&m.fd0[f]);
+        sa_wall_shear(m, n.x, n.y, d0.x, d0.y, q0, F);
+    }
 #pragma unroll
     for (int k = 0; k < 4; ++k) fl[k] = F[k] * L;
     *btp = cc.y >= 0 ? -1 : bt;  // -1: interior face
@@ -840,7 +852,7 @@ __global__ void __launch_bounds__(256) k_uniform(const KM<T> m, const V4<S>* __r
                 int bt = BT_INTERNAL;
                 if (oc < 0) bt = __ldg(&m.btype[-oc - 1]);
                 T fgx[4] = {T(0), T(0), T(0), T(0)}, fgy[4] = {T(0), T(0), T(0), T(0)};
-                if (VISC == 1 && two_sided(bt)) {
+                if (VISC >= 1 && two_sided(bt)) {
                     T qi[4], qo[4], gxi[4], gyi[4], gxo[4] = {T(0), T(0), T(0), T(0)},
                                                       gyo[4] = {T(0), T(0), T(0), T(0)};
                     ld4s(&qmem[i], qi);
@@ -866,7 +878,9 @@ __global__ void __launch_bounds__(256) k_uniform(const KM<T> m, const V4<S>* __r
                     face_gradient(qa, qb, gxa, gya, gxb, gyb, ldv4<T>(&m.ft[f]), fgx, fgy);
                 }
                 T F[4];
-                face_flux<T, VISC>(m, bt, n.x, n.y, qf, qf, fgx, fgy, F);
+                T mut_f = T(0);
+                if (VISC == 2 && two_sided(bt)) mut_f = T(0.5) * (__ldg(&m.mut[i]) + __ldg(&m.mut[oc]));
+                face_flux<T, VISC>(m, bt, n.x, n.y, qf, qf, fgx, fgy, F, mut_f);
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
                     const T fl = F[k] * L;

@@ -20,4 +20,11 @@ void enqueue_correction(int n, const void* R64, const void* R32, void* corr, cud
     dev::k_correction<<<(n + 255) / 256, 256, 0, s>>>(n, (const dev::d4*)R64, (const dev::d4*)R32, (float4*)corr);
 }
 
+void enqueue_sa_implicit_f32(const StepArgs& a, int p, int sweeps, cudaStream_t s) {
+    dev::sa_implicit<float, float>(a, p, sweeps, s);
+}
+void enqueue_sa_mut_f32(const StepArgs& a, int p, cudaStream_t s) {
+    dev::sa_mut<float, float>(a, (const dev::V4<float>*)a.qsh[p], a.sa_nu[p], s);
+}
+
 }  // namespace afx

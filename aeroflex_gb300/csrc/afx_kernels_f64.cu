@@ -97,7 +97,25 @@ __global__ void k_forces(const ForceArgs f) {
     }
 }
 
+__global__ void k_permute_in1(int n, const int* __restrict__ cell_old, const double* __restrict__ src,
+                              double* __restrict__ dst) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = src[cell_old[i]];
+}
+__global__ void k_permute_out1(int n, const int* __restrict__ cell_old, const double* __restrict__ src,
+                               double* __restrict__ dst) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[cell_old[i]] = src[i];
+}
+
 }  // namespace dev
+
+void enqueue_permute_in1(int n, const int* cell_old, const void* src, void* dst, cudaStream_t s) {
+    dev::k_permute_in1<<<(n + 255) / 256, 256, 0, s>>>(n, cell_old, (const double*)src, (double*)dst);
+}
+void enqueue_permute_out1(int n, const int* cell_old, const void* src, void* dst, cudaStream_t s) {
+    dev::k_permute_out1<<<(n + 255) / 256, 256, 0, s>>>(n, cell_old, (const double*)src, (double*)dst);
+}
 
 void enqueue_permute_in(int n, const int* cell_old, const void* src, void* dst, cudaStream_t s) {
     dev::k_permute_in<<<(n + 255) / 256, 256, 0, s>>>(n, cell_old, (const dev::d4*)src, (dev::d4*)dst);
@@ -109,5 +127,12 @@ void enqueue_to_f32(int n, const void* src, void* dst, cudaStream_t s) {
     dev::k_to_f32<<<(n + 255) / 256, 256, 0, s>>>(n, (const dev::d4*)src, (float4*)dst);
 }
 void enqueue_forces(const ForceArgs& f, cudaStream_t s) { dev::k_forces<<<1, 256, 0, s>>>(f); }
+
+void enqueue_sa_implicit_f64(const StepArgs& a, int p, int sweeps, cudaStream_t s) {
+    dev::sa_implicit<double, double>(a, p, sweeps, s);
+}
+void enqueue_sa_mut_f64(const StepArgs& a, int p, cudaStream_t s) {
+    dev::sa_mut<double, double>(a, (const dev::V4<double>*)a.qsh[p], a.sa_nu[p], s);
+}
 
 }  // namespace afx

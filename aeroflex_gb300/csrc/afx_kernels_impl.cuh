@@ -3,6 +3,7 @@
 #pragma once
 
 #include "afx_kernels.cuh"
+#include "afx_sa.cuh"
 
 namespace afx {
 namespace dev {
@@ -32,6 +33,10 @@ KM<T> make_km(const StepArgs& a) {
     m.lsq = a.lsq;
     m.lsqw = (const V2<T>*)a.lsqw;
     m.lsqs = a.lsqs;
+    m.mut = (const T*)a.sa_mut;
+    m.cp = (T)a.cp;
+    m.PrL = (T)a.Pr_L;
+    m.PrT = (T)a.Pr_T;
     return m;
 }
 
@@ -116,13 +121,52 @@ void launch_stage_v(const StepArgs& a, const KM<T>& m, const V4<S>* qk, const V4
 template <class T, class S>
 void launch_stage(const StepArgs& a, const KM<T>& m, const V4<S>* qk, const V4<S>* qmem, const StageOut<T, S>& o,
                   bool first, cudaStream_t s) {
-    if (a.visc == 1) {
+    if (a.visc == 2) {
+        if (a.second) launch_stage_v<T, S, 2, true>(a, m, qk, qmem, o, first, s);
+        else launch_stage_v<T, S, 2, false>(a, m, qk, qmem, o, first, s);
+    } else if (a.visc == 1) {
         if (a.second) launch_stage_v<T, S, 1, true>(a, m, qk, qmem, o, first, s);
         else launch_stage_v<T, S, 1, false>(a, m, qk, qmem, o, first, s);
     } else {
         if (a.second) launch_stage_v<T, S, 0, true>(a, m, qk, qmem, o, first, s);
         else launch_stage_v<T, S, 0, false>(a, m, qk, qmem, o, first, s);
     }
+}
+
+// Spalart-Allmaras: the view of one evaluation, mu_t of a stage state, one
+// stage of nu~ (see afx_sa.cuh).
+template <class T>
+SaView<T> sa_view(const StepArgs& a) {
+    SaView<T> v;
+    v.nu0 = v.nuk = nullptr;
+    v.nu_next = nullptr;
+    v.nuW = (double*)a.sa_nuW;
+    v.wd = (const T*)a.sa_wd;
+    v.cxy = (const V2<T>*)a.sa_cxy;
+    v.gxy = (const V2<T>*)a.sa_gxy;
+    v.dt = (const T*)a.dt;
+    v.nu_far = (T)a.sa_nu_far;
+    v.alpha = 1.0;
+    v.relax = a.relax;
+    return v;
+}
+
+template <class T, class S>
+void sa_mut(const StepArgs& a, const V4<S>* qk, const void* nuk, cudaStream_t s) {
+    k_sa_mut<T, S><<<nblocks(a.n_cells, 256), 256, 0, s>>>(a.n_cells, qk, (const double*)nuk, (T)a.mu,
+                                                           (T*)a.sa_mut, a.ctrl);
+}
+
+template <class T, class S>
+void sa_stage(const StepArgs& a, const KM<T>& m, const V4<S>* qk, const void* nu0, const void* nuk, void* nu_next,
+              double alpha, cudaStream_t s) {
+    SaView<T> v = sa_view<T>(a);
+    v.nu0 = (const double*)nu0;
+    v.nuk = (const double*)nuk;
+    v.nu_next = (double*)nu_next;
+    v.alpha = alpha;
+    k_sa_stage<T, S><<<nblocks(a.n_cells, 256), 256, 0, s>>>(m, qk, (const V4<T>*)a.gx, (const V4<T>*)a.gy, v,
+                                                             a.ctrl);
 }
 
 template <class T, class S>
@@ -163,6 +207,9 @@ void iteration(const StepArgs& a, int p, cudaStream_t s) {
                 m, qk, (const V4<T>*)a.gx, (const V4<T>*)a.gy, (V4<T>*)a.phi, a.ctrl);
             mark(a, K_LIMITER, s);
         }
+        // Spalart-Allmaras: eddy viscosity of the stage state first
+        const void* nuk = st == 0 ? a.sa_nu[p] : a.sa_nus[st - 1];
+        if (a.visc == 2) sa_mut<T, S>(a, qk, nuk, s);
         o.alpha = alpha[st];
         if (st < 2) {
             o.mode = 0;
@@ -174,6 +221,10 @@ void iteration(const StepArgs& a, int p, cudaStream_t s) {
             o.qsh_next = SHADOW ? (V4<S>*)a.qsh[p ^ 1] : nullptr;
         }
         launch_stage<T, S>(a, m, qk, q, o, st == 0, s);
+        // ... then its nu~ stage from the same stage state (the time step
+        // was formed by the first stage's mean-flow launch)
+        if (a.visc == 2)
+            sa_stage<T, S>(a, m, qk, a.sa_nu[p], nuk, st < 2 ? a.sa_nus[st] : a.sa_nu[p ^ 1], alpha[st], s);
     }
     if (a.n_cases > 0) {
         k_case_control<<<a.n_cases, 1024, 0, s>>>(a.cell_sq, a.case_off, a.cctrl, a.case_done, a.chist, a.ctrl,
@@ -191,9 +242,11 @@ void residual(const StepArgs& a, int p, cudaStream_t s) {
     const KM<T> m = make_km<T>(a);
     const V4<S>* q = (const V4<S>*)a.qsh[p];
     launch_prep<T, S>(a, m, q, s);
+    if (a.visc == 2) sa_mut<T, S>(a, q, a.sa_nu[p], s);
     StageOut<T, S> o = base_out<T, S>(a, p);
     o.mode = 2;
     launch_stage<T, S>(a, m, q, q, o, false, s);
+    if (a.visc == 2) sa_stage<T, S>(a, m, q, a.sa_nu[p], a.sa_nu[p], nullptr, 1.0, s);
 }
 
 // Implicit right-hand side of state parity p (first-stage reconstruction,
@@ -203,6 +256,7 @@ void rhs(const StepArgs& a, int p, cudaStream_t s) {
     const KM<T> m = make_km<T>(a);
     const V4<S>* q = (const V4<S>*)a.qsh[p];
     launch_prep<T, S>(a, m, q, s);
+    if (a.visc == 2) sa_mut<T, S>(a, q, a.sa_nu[p], s);
     StageOut<T, S> o = base_out<T, S>(a, p);
     o.mode = 3;
     launch_stage<T, S>(a, m, q, q, o, false, s);
@@ -215,6 +269,7 @@ void last_stage_residual(const StepArgs& a, int p, cudaStream_t s) {
     const KM<T> m = make_km<T>(a);
     StageOut<T, S> o = base_out<T, S>(a, p);
     o.mode = 2;
+    if (a.visc == 2) sa_mut<T, S>(a, (const V4<S>*)a.qs[1], a.sa_nus[1], s);
     launch_stage<T, S>(a, m, (const V4<S>*)a.qs[1], (const V4<S>*)a.qsh[p], o, false, s);
 }
 
@@ -223,7 +278,12 @@ void uniform(const StepArgs& a, int p, const double* qf, cudaStream_t s) {
     const KM<T> m = make_km<T>(a);
     const int nb = nblocks(a.n_cells, a.block);
     const V4<S>* q = (const V4<S>*)a.qsh[p];
-    if (a.visc == 1)
+    if (a.visc == 2) {
+        sa_mut<T, S>(a, q, a.sa_nu[p], s);
+        k_uniform<T, S, 2><<<nb, a.block, 0, s>>>(m, q, (const V4<T>*)a.gx, (const V4<T>*)a.gy, qf[0], qf[1],
+                                                   qf[2], qf[3], (d4*)a.Rq, a.partials, a.qfar_case, a.case_of,
+                                                   a.cell_sq);
+    } else if (a.visc == 1)
         k_uniform<T, S, 1><<<nb, a.block, 0, s>>>(m, q, (const V4<T>*)a.gx, (const V4<T>*)a.gy, qf[0], qf[1],
                                                    qf[2], qf[3], (d4*)a.Rq, a.partials, a.qfar_case, a.case_of,
                                                    a.cell_sq);
@@ -236,6 +296,29 @@ void uniform(const StepArgs& a, int p, const double* qf, cudaStream_t s) {
                                                  a.n_cases, 1);
     else
         k_control<<<1, 1024, 0, s>>>(a.partials, nb, a.ctrl, a.hist, nullptr, 1);
+}
+
+// Implicit solver, Spalart-Allmaras: `sweeps` point-implicit nu~ updates
+// from the state of parity p (gradients formed here), in place in sa_nu[p]
+// through the stage buffer; mu_t of the final nu~ last.
+template <class T, class S>
+void sa_implicit(const StepArgs& a0, int p, int sweeps, cudaStream_t s) {
+    StepArgs a = a0;
+    a.variant = 0;  // dt with the prep (the CFL in a.cfl)
+    a.second = 0;
+    a.need_grad = 1;
+    const KM<T> m = make_km<T>(a);
+    const V4<S>* q = (const V4<S>*)a.qsh[p];
+    launch_prep<T, S>(a, m, q, s);
+    SaView<T> v = sa_view<T>(a);
+    for (int k = 0; k < sweeps; ++k) {
+        v.nuk = (const double*)a.sa_nu[p];
+        v.nu_next = (double*)a.sa_nus[0];
+        k_sa_implicit<T, S><<<nblocks(a.n_cells, 256), 256, 0, s>>>(m, q, (const V4<T>*)a.gx, (const V4<T>*)a.gy,
+                                                                    v, a.ctrl);
+        cudaMemcpyAsync(a.sa_nu[p], a.sa_nus[0], (size_t)a.n_cells * 8, cudaMemcpyDeviceToDevice, s);
+    }
+    sa_mut<T, S>(a, q, a.sa_nu[p], s);
 }
 
 }  // namespace dev

@@ -117,6 +117,16 @@ struct StepArgs {
     CaseCtrl* cctrl = nullptr;        // [n_cases]
     double* chist = nullptr;          // [n_cases * CASE_HIST_CAP]
     const double* qfar_case = nullptr;  // [4 * n_cases] freestream state of each case
+    // Spalart-Allmaras (visc == 2), device cell order
+    void* sa_nu[2] = {nullptr, nullptr};   // nu~, FP64, ping-pong with the master state
+    void* sa_nus[2] = {nullptr, nullptr};  // nu~ of the RK stages, FP64
+    void* sa_mut = nullptr;                // T [N] eddy viscosity of the stage state
+    void* sa_nuW = nullptr;                // FP64 [N] nu~ residual of the last evaluation
+    const void* sa_wd = nullptr;           // T [N] wall distance
+    const void* sa_cxy = nullptr;          // T2 [N] centroids
+    const void* sa_gxy = nullptr;          // T2 [B] ghost-cell centroids
+    double cp = 1., Pr_L = 0.72, Pr_T = 0.9;
+    double sa_nu_far = 0.;                 // nu~ of the far field, 3 mu_L / rho_inf
     Prof* prof = nullptr;      // eager profiling only (never inside a graph)
 };
 
@@ -140,6 +150,16 @@ void enqueue_last_stage_residual_f32(const StepArgs& a, int p, cudaStream_t s);
 // get_uniform_residual: qW += freestream face fluxes, ‖qW‖₂ -> ctrl->err0.
 void enqueue_uniform_f64(const StepArgs& a, int p, const double* qfar, cudaStream_t s);
 void enqueue_uniform_f32(const StepArgs& a, int p, const double* qfar, cudaStream_t s);
+
+// Spalart-Allmaras: `sweeps` point-implicit nu~ updates of the implicit
+// solver at the state of parity p (then mu_t), and mu_t alone.
+void enqueue_sa_implicit_f64(const StepArgs& a, int p, int sweeps, cudaStream_t s);
+void enqueue_sa_implicit_f32(const StepArgs& a, int p, int sweeps, cudaStream_t s);
+void enqueue_sa_mut_f64(const StepArgs& a, int p, cudaStream_t s);
+void enqueue_sa_mut_f32(const StepArgs& a, int p, cudaStream_t s);
+// Scalar permutes between reference and device cell order (FP64 [N]).
+void enqueue_permute_in1(int n, const int* cell_old, const void* src_ref, void* dst_dev, cudaStream_t s);
+void enqueue_permute_out1(int n, const int* cell_old, const void* src_dev, void* dst_ref, cudaStream_t s);
 
 // Pressure forces over one boundary patch (post.h:301-387).
 struct ForceArgs {

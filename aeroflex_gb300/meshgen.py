@@ -14,6 +14,29 @@ import math
 import numpy as np
 
 
+
+def _libm(fn, x):
+    """fn (a function of Python's math module, i.e. the C library) applied
+    element by element.  NumPy's own vectorised transcendental functions
+    differ between CPU architectures in the last bit; the C library's agree,
+    so meshes generated on different hosts are bit-identical."""
+    x = np.asarray(x, np.float64)
+    return np.fromiter((fn(v) for v in x.ravel().tolist()), np.float64, count=x.size).reshape(x.shape)
+
+
+def _cos(x):
+    return _libm(math.cos, x)
+
+
+def _sin(x):
+    return _libm(math.sin, x)
+
+
+def _pow(base, k):
+    """base ** k for each (integer) exponent k, by the C library's pow."""
+    return _libm(lambda e: math.pow(base, e), np.asarray(k, np.float64))
+
+
 def naca4_thickness(x, t):
     """NACA 4-digit half thickness with the closed trailing edge (-0.1036)."""
     return 5.0 * t * (0.2969 * np.sqrt(x) - 0.1260 * x - 0.3516 * x ** 2 + 0.2843 * x ** 3 - 0.1036 * x ** 4)
@@ -24,7 +47,7 @@ def naca4_surface(n_surf, m=0.0, p=0.4, t=0.12):
     edge over the upper surface, cosine-clustered at both edges."""
     j = np.arange(n_surf)
     beta = 2.0 * np.pi * j / n_surf
-    xc = 0.5 * (1.0 + np.cos(beta))
+    xc = 0.5 * (1.0 + _cos(beta))
     yt = naca4_thickness(xc, t)
     if m > 0.0:
         yc = np.where(xc < p, m / p ** 2 * (2 * p * xc - xc ** 2),
@@ -33,10 +56,10 @@ def naca4_surface(n_surf, m=0.0, p=0.4, t=0.12):
     else:
         yc = np.zeros_like(xc)
         dyc = np.zeros_like(xc)
-    th = np.arctan(dyc)
+    th = _libm(math.atan, dyc)
     sgn = np.where(j <= n_surf // 2, 1.0, -1.0)
-    x = xc - sgn * yt * np.sin(th)
-    y = yc + sgn * yt * np.cos(th)
+    x = xc - sgn * yt * _sin(th)
+    y = yc + sgn * yt * _cos(th)
     # exact closure at the trailing edge and leading edge
     x[0], y[0] = 1.0, 0.0
     return x, y
@@ -59,8 +82,8 @@ def airfoil_omesh(n_surf=128, n_rad=64, r_far=20.0, growth=None, first=2e-3, m=0
     """
     sx, sy = naca4_surface(n_surf, m, p, t)
     ang = 2.0 * np.pi * np.arange(n_surf) / n_surf
-    fx = 0.5 + r_far * np.cos(ang)
-    fy = r_far * np.sin(ang)
+    fx = 0.5 + r_far * _cos(ang)
+    fy = r_far * _sin(ang)
     # outward normals: rotate the central-difference tangent (CCW surface -> outward = (ty, -tx))
     tx = np.roll(sx, -1) - np.roll(sx, 1)
     ty = np.roll(sy, -1) - np.roll(sy, 1)
@@ -75,7 +98,7 @@ def airfoil_omesh(n_surf=128, n_rad=64, r_far=20.0, growth=None, first=2e-3, m=0
             lo, hi = (lo, mid) if h1 < first else (mid, hi)
         growth = 0.5 * (lo + hi)
     k = np.arange(n_rad + 1)
-    s = (growth ** k - 1.0) / (growth ** n_rad - 1.0)
+    s = (_pow(growth, k) - 1.0) / (math.pow(growth, n_rad) - 1.0)
     S = s[:, None]
     if fade == 1:
         X = (1.0 - S) * (sx[None, :] + r_far * S * nx_[None, :]) + S * fx[None, :]
@@ -179,7 +202,7 @@ def density_bump_state(m, mach=0.3, amp=0.05, width=0.1, center=(0.5, 0.5), gamm
     u = mach * c
     rho_inf = 1.0 / (R * 1.0)
     r2 = (cx - center[0]) ** 2 + (cy - center[1]) ** 2
-    rho = rho_inf * (1.0 + amp * np.exp(-r2 / width ** 2))
+    rho = rho_inf * (1.0 + amp * _libm(math.exp, -r2 / width ** 2))
     q = np.empty((len(cx), 4))
     q[:, 0] = rho
     q[:, 1] = rho * u
@@ -309,12 +332,12 @@ def hybrid_airfoil(n_surf=512, bl_layers=60, first=1e-6, growth=1.1, r_far=100.0
     ty = np.roll(sy, -1) - np.roll(sy, 1)
     tn = np.hypot(tx, ty)
     nx_, ny_ = ty / tn, -tx / tn
-    h = first * (growth ** np.arange(bl_layers + 1) - 1.0) / (growth - 1.0)
+    h = first * (_pow(growth, np.arange(bl_layers + 1)) - 1.0) / (growth - 1.0)
     BX = sx[None, :] + h[:, None] * nx_[None, :]
     BY = sy[None, :] + h[:, None] * ny_[None, :]
     H, last = h[-1], h[-1] - h[-2]
     ex, ey = BX[-1], BY[-1]  # outer ring of the boundary layer
-    ang0 = np.arctan2(ey, ex - 0.5)
+    ang0 = np.fromiter((math.atan2(a, b) for a, b in zip(ey.tolist(), (ex - 0.5).tolist())), np.float64)
     n_far = 128
 
     def rings(ratio):
@@ -330,18 +353,18 @@ def hybrid_airfoil(n_surf=512, bl_layers=60, first=1e-6, growth=1.1, r_far=100.0
             per = 2 * np.pi * (0.5 + s * r_far)
             n_k = int(min(n_surf, max(32, round(per / step))))
             if n_k == n_surf:
-                px = (1 - s) * (ex + d * nx_) + s * (0.5 + r_far * np.cos(ang0))
-                py = (1 - s) * (ey + d * ny_) + s * (r_far * np.sin(ang0))
+                px = (1 - s) * (ex + d * nx_) + s * (0.5 + r_far * _cos(ang0))
+                py = (1 - s) * (ey + d * ny_) + s * (r_far * _sin(ang0))
             else:
                 a = ang0[0] + 2 * np.pi * (np.arange(n_k) + rng.uniform(-0.25, 0.25, n_k)) / n_k
                 rad = np.interp(np.mod(a - ang0[0], 2 * np.pi), np.mod(ang0 - ang0[0], 2 * np.pi),
                                 np.hypot(ex - 0.5, ey), period=2 * np.pi)
-                px = 0.5 + ((1 - s) * (rad + d) + s * r_far) * np.cos(a)
-                py = ((1 - s) * (rad + d) + s * r_far) * np.sin(a)
+                px = 0.5 + ((1 - s) * (rad + d) + s * r_far) * _cos(a)
+                py = ((1 - s) * (rad + d) + s * r_far) * _sin(a)
             pts.append((px, py))
             step *= ratio
         a = 2 * np.pi * np.arange(n_far) / n_far
-        pts.append((0.5 + r_far * np.cos(a), r_far * np.sin(a)))
+        pts.append((0.5 + r_far * _cos(a), r_far * _sin(a)))
         return pts
 
     lo, hi = 1.005, 1.5

@@ -27,7 +27,7 @@ ABI_SYMBOLS = [
     "afx_solver_free", "afx_init_freestream", "afx_set_state", "afx_get_state", "afx_residual", "afx_iterate",
     "afx_run_to_convergence", "afx_residual_history", "afx_forces", "afx_set_farfield", "afx_request_stop",
     "afx_last_device_seconds", "afx_profile_iterations", "afx_kernel_name", "afx_autotune",
-    "afx_residual_noalloc", "afx_implicit_rhs", "afx_measure_fp64_peak", "afx_batch_create", "afx_batch_free", "afx_batch_counts", "afx_batch_init_freestream",
+    "afx_residual_noalloc", "afx_implicit_rhs", "afx_set_turbulence", "afx_get_turbulence", "afx_turbulence_residual", "afx_measure_fp64_peak", "afx_batch_create", "afx_batch_free", "afx_batch_counts", "afx_batch_init_freestream",
     "afx_batch_set_state", "afx_batch_get_state", "afx_batch_iterate", "afx_batch_run_to_convergence",
     "afx_batch_case_history", "afx_batch_forces", "afx_batch_set_farfield", "afx_batch_autotune",
     "afx_batch_last_device_seconds", "afx_residual_vjp", "afx_boundary_states", "afx_adjoint_solve",
@@ -96,6 +96,9 @@ def lib():
         "afx_autotune": (i, [vp, i, ctypes.c_char_p, i, P(i), P(d)]),
         "afx_residual_noalloc": (i, [vp, vp, vp, ll]),
         "afx_implicit_rhs": (i, [vp, vp, ll]),
+        "afx_set_turbulence": (i, [vp, vp, ll]),
+        "afx_get_turbulence": (i, [vp, vp, ll]),
+        "afx_turbulence_residual": (i, [vp, vp, ll]),
         "afx_measure_fp64_peak": (i, [ctypes.c_int, vp]),
         "afx_batch_create": (i, [i, vp, vp, P(vp)]),
         "afx_batch_free": (None, [vp]),
@@ -295,6 +298,22 @@ class Solver:
         R = np.empty(4 * self.n_real, np.float64)
         _check(lib().afx_residual(self.h, _ptr(R), R.size))
         return R
+
+    def set_nu(self, nu):
+        """nu~ of the Spalart-Allmaras model per real cell (reference order)."""
+        nu = np.ascontiguousarray(nu, np.float64).reshape(-1)
+        _check(lib().afx_set_turbulence(self.h, _ptr(nu), nu.size))
+
+    def nu(self):
+        out = np.empty(self.n_real, np.float64)
+        _check(lib().afx_get_turbulence(self.h, _ptr(out), out.size))
+        return out
+
+    def nu_residual(self):
+        """nu~ residual R/A of the last evaluation."""
+        out = np.empty(self.n_real, np.float64)
+        _check(lib().afx_turbulence_residual(self.h, _ptr(out), out.size))
+        return out
 
     def implicit_rhs(self):
         """fillRhoRHS (solver.h:1079-1152) of the current state (implicit

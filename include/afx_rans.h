@@ -120,6 +120,14 @@ int afx_init_freestream(afx_solver s);
  * AoS FP64 [4*n_real]; ghost states keep their boundary values. */
 int afx_set_state(afx_solver s, const double* q, long long n);
 int afx_get_state(afx_solver s, double* q, long long n);
+/* Spalart-Allmaras solvers (viscosity "spalart-allmaras"; the reference's
+ * nu array, solver.h:55, which it leaves unused): nu~ per real cell,
+ * reference order.  afx_init_freestream sets nu~ = 3 mu_L / rho_inf. */
+int afx_set_turbulence(afx_solver s, const double* nu, long long n);
+int afx_get_turbulence(afx_solver s, double* nu, long long n);
+/* nu~ residual R/A of the last evaluation (afx_residual: the current state;
+ * afx_iterate: the last stage of the last iteration), reference order. */
+int afx_turbulence_residual(afx_solver s, double* nuW, long long n);
 /* Residual of the current state as the first RK stage forms it: ghosts,
  * Green-Gauss gradient, limiter, face loop, /area (solver.h:745-799).
  * R gets AoS FP64 [4*n_real]. */
