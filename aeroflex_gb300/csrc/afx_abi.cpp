@@ -434,13 +434,16 @@ struct afx_solver_s {
     // implicitSolver (solver.h:1000-1213) at the given CFL; returns the final
     // ||RhoVector||, or -1 if the system could not be solved
     // the mean-flow implicit iteration, then (Spalart-Allmaras) the
-    // segregated point-implicit nu~ updates at the new state
+    // segregated point-implicit nu~ updates at the new state; the norm
+    // returned is then that of the right-hand side with the updated eddy
+    // viscosity, so a run converges only once nu~ has stopped moving too
     double implicit_iteration(double cfl, double tol_abs) {
-        const double r = implicit_iteration_mean(cfl, tol_abs);
+        double r = implicit_iteration_mean(cfl, tol_abs);
         if (a.visc == 2 && r == r && r >= 0) {
             StepArgs m = A64();
             m.cfl = cfl;
             enqueue_sa_implicit_f64(m, parity, 3, stream);
+            r = imp_rhs(parity);
         }
         return r;
     }

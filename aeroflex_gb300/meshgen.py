@@ -39,7 +39,9 @@ def _pow(base, k):
 
 def naca4_thickness(x, t):
     """NACA 4-digit half thickness with the closed trailing edge (-0.1036)."""
-    return 5.0 * t * (0.2969 * np.sqrt(x) - 0.1260 * x - 0.3516 * x ** 2 + 0.2843 * x ** 3 - 0.1036 * x ** 4)
+    x = np.asarray(x, np.float64)
+    return 5.0 * t * (0.2969 * np.sqrt(x) - 0.1260 * x - 0.3516 * x * x + 0.2843 * _libm(lambda v: math.pow(v, 3), x)
+                      - 0.1036 * _libm(lambda v: math.pow(v, 4), x))
 
 
 def naca4_surface(n_surf, m=0.0, p=0.4, t=0.12):
