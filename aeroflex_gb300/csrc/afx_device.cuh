@@ -277,8 +277,10 @@ __device__ __forceinline__ void face_flux(const KM<T>& m, const int bt, const T 
             laminar_flux(m.gamma, m.R, m.mu + mut_f, m.cp * (m.mu / m.PrL + mut_f / m.PrT), nx, ny, qL, qR, fgx, fgy,
                          f);
     } else {
+        // VISC 2: the inviscid part of a no-slip wall takes the slip-wall
+        // ghost (pressure only); the caller adds the wall shear
         T qb[4];
-        ghost_state(bt, m.gamma, nx, ny, qL, qR, qb);
+        ghost_state(VISC == 2 && bt == BT_WALL ? BT_SLIP : bt, m.gamma, nx, ny, qL, qR, qb);
         roe_flux(m.gamma, nx, ny, qL, qb, f);
     }
 }

@@ -19,6 +19,11 @@
 // boundary faces); grad nu~ by Green-Gauss with face means; Omega =
 // |dv/dx - du/dy| from the mean flow's cell gradients; ghost nu~ = -nu~_i at
 // no-slip walls, nu~_i at slip walls, 3 mu_L / rho_inf at the far field.
+// Mean flow (afx_device.cuh, face_flux with VISC 2): the reference's laminar
+// terms with mu_L + mu_t; at no-slip walls the inviscid flux of the slip-wall
+// ghost (the reflected ghost's Roe dissipation on the tangential velocity
+// would outweigh the physical shear at high Reynolds numbers) plus the wall
+// shear mu_L u_t / delta.
 #pragma once
 
 #include "afx_kernels.cuh"

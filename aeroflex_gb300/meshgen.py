@@ -89,7 +89,7 @@ def airfoil_omesh(n_surf=128, n_rad=64, r_far=20.0, growth=None, first=2e-3, m=0
     # outward normals: rotate the central-difference tangent (CCW surface -> outward = (ty, -tx))
     tx = np.roll(sx, -1) - np.roll(sx, 1)
     ty = np.roll(sy, -1) - np.roll(sy, 1)
-    tn = np.hypot(tx, ty)
+    tn = np.sqrt(tx * tx + ty * ty)
     nx_, ny_ = ty / tn, -tx / tn
     if growth is None:
         # geometric ratio r with r_far*(r - 1)/(r^n - 1) = first (bisection)
@@ -332,7 +332,7 @@ def hybrid_airfoil(n_surf=512, bl_layers=60, first=1e-6, growth=1.1, r_far=100.0
     sx, sy = naca4_surface(n_surf, 0.0, 0.4, t)
     tx = np.roll(sx, -1) - np.roll(sx, 1)
     ty = np.roll(sy, -1) - np.roll(sy, 1)
-    tn = np.hypot(tx, ty)
+    tn = np.sqrt(tx * tx + ty * ty)
     nx_, ny_ = ty / tn, -tx / tn
     h = first * (_pow(growth, np.arange(bl_layers + 1)) - 1.0) / (growth - 1.0)
     BX = sx[None, :] + h[:, None] * nx_[None, :]
@@ -360,7 +360,7 @@ def hybrid_airfoil(n_surf=512, bl_layers=60, first=1e-6, growth=1.1, r_far=100.0
             else:
                 a = ang0[0] + 2 * np.pi * (np.arange(n_k) + rng.uniform(-0.25, 0.25, n_k)) / n_k
                 rad = np.interp(np.mod(a - ang0[0], 2 * np.pi), np.mod(ang0 - ang0[0], 2 * np.pi),
-                                np.hypot(ex - 0.5, ey), period=2 * np.pi)
+                                np.sqrt((ex - 0.5) * (ex - 0.5) + ey * ey), period=2 * np.pi)
                 px = 0.5 + ((1 - s) * (rad + d) + s * r_far) * _cos(a)
                 py = ((1 - s) * (rad + d) + s * r_far) * _sin(a)
             pts.append((px, py))

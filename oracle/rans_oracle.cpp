@@ -737,7 +737,10 @@ void ExplicitSolver::flux(int type, uint e, const double qL[4], const double qR[
     } else {  // boundary functors call the internal flux without gradients (physics.h:298,363,431)
         double qb[4];
         const double zero[4] = {0, 0, 0, 0};
-        boundary_state(st.g, type, nx, ny, qL, qR, qb);
+        // Spalart-Allmaras: the inviscid part of a no-slip wall takes the
+        // slip-wall ghost (pressure only); calc_residual adds the wall shear
+        const int gt = (st.viscosity == VISC_SA && type == BC_WALL) ? BC_SLIP_WALL : type;
+        boundary_state(st.g, gt, nx, ny, qL, qR, qb);
         internal_flux(st.g, nx, ny, flux_visc(), qL, qb, zero, zero, f);
     }
 }

@@ -39,9 +39,13 @@
 //   the boundary functors' ghost state (physics.h:311-530).
 // Mean flow: the reference's laminar terms (physics.h:230-258) with
 // mu_L + mu_t,f and cp (mu_L/Pr_L + mu_t,f/Pr_T), mu_t,f the mean of the two
-// cells; at no-slip walls, where the reference's boundary flux has no
-// viscous part, the wall shear mu_L u_t / delta (u_t the cell's tangential
-// velocity, delta the distance from its centroid to the wall face).
+// cells.  At no-slip walls the reference's boundary flux has no viscous
+// part, and its reflected ghost (momentum negated) puts a Roe dissipation on
+// the tangential velocity that at high Reynolds numbers outweighs the
+// physical shear several times.  Here the inviscid part takes the slip-wall
+// ghost (tangential momentum kept: only the pressure acts) and the wall shear
+// mu_L u_t / delta is added (u_t the cell's tangential velocity, delta the
+// distance from its centroid to the wall face).
 // Cube roots (f_w) by Newton-Raphson on y^3 = m after splitting off the
 // exponent: only +, -, *, / and sqrt, so the GPU reproduces them bit for bit.
 #include <algorithm>
