@@ -34,6 +34,8 @@ void enqueue_prolong(int nc, const double* cx, const double* cy, const double* c
                      const double* fx, const double* fy, void* fine_q, cudaStream_t s);
 void enqueue_full_state(int n, int nb, const int* cell_old, const int* owner_dev, const void* q, void* full,
                         cudaStream_t s);
+void enqueue_wall_seg_dist(int nc, const double* cx, const double* cy, int nw, const double* seg, double* out,
+                           cudaStream_t s);
 void enqueue_wall_dist(int nc, const double* cx, const double* cy, int nw, const double* wx, const double* wy,
                        double* out, cudaStream_t s);
 struct ImplicitEngine;
@@ -500,10 +502,10 @@ struct afx_solver_s {
                 AFX_CUDA(cudaMemcpyAsync(x.sa_nu[p], nu.data(), N * 8, cudaMemcpyHostToDevice, stream));
             AFX_CUDA(cudaStreamSynchronize(stream));
         }
-        std::vector<double> wd_all = wall_distance_all();
+        std::vector<double> wd_ref = sa_wall_distance();
         std::vector<double> wd(N), cxy(2 * N), gxy(2 * std::max<size_t>(B, 1));
         for (size_t i = 0; i < N; ++i) {
-            wd[i] = wd_all[hl.cell_old[i]];
+            wd[i] = wd_ref[hl.cell_old[i]];
             cxy[2 * i] = dev_cx[i];
             cxy[2 * i + 1] = dev_cy[i];
         }
@@ -518,28 +520,26 @@ struct afx_solver_s {
         x.sa_gxy = f32 ? dupload(cast_vec<float>(gxy)) : dupload(gxy);
     }
 
-    // mesh::compute_wall_dist (mesh.h:794-830) on the GPU: every cell,
-    // ghosts included, reference order
-    std::vector<double> wall_distance_all() {
-        const int nc = (int)geo_area.size();
-        std::vector<double> w, wy;  // wall edge centres in boundary order, then x / y
+    // Spalart-Allmaras wall distance on the GPU: from each real cell's
+    // centroid to the nearest no-slip wall face (a segment), reference order
+    std::vector<double> sa_wall_distance() {
+        const int nc = (int)hl.n_cells;
+        std::vector<double> seg;  // ax, ay, bx, by per no-slip wall face, boundary order
         for (size_t b = 0; b < bedges.size(); ++b)
-            if (boundary_type[b] == BC_WALL || boundary_type[b] == BC_SLIP_WALL) {
-                w.push_back(bedges[b].ex);
-                wy.push_back(bedges[b].ey);
+            if (boundary_type[b] == BC_WALL) {
+                const auto& en = hm.edgesNodes[hm.boundaryEdges[b]];
+                seg.insert(seg.end(), {hm.nodesX[en[0]], hm.nodesY[en[0]], hm.nodesX[en[1]], hm.nodesY[en[1]]});
             }
-        const int nw = (int)w.size();
-        w.insert(w.end(), wy.begin(), wy.end());
+        const int nw = (int)(seg.size() / 4);
         std::vector<double> c(2 * (size_t)nc);
-        std::copy(geo_cx.begin(), geo_cx.end(), c.begin());
-        std::copy(geo_cy.begin(), geo_cy.end(), c.begin() + nc);
+        std::copy(geo_cx.begin(), geo_cx.begin() + nc, c.begin());
+        std::copy(geo_cy.begin(), geo_cy.begin() + nc, c.begin() + nc);
         DevBuf dc, dw, dout;
         dc.upload(c.data(), c.size() * 8, stream);
-        dw.upload(w.data(), std::max<size_t>(w.size(), 1) * 8, stream);
+        dw.upload(seg.data(), std::max<size_t>(seg.size(), 1) * 8, stream);
         dout.alloc((size_t)nc * 8);
         const double* pc = (const double*)dc.p;
-        const double* pw = (const double*)dw.p;
-        enqueue_wall_dist(nc, pc, pc + nc, nw, pw, pw + nw, (double*)dout.p, stream);
+        enqueue_wall_seg_dist(nc, pc, pc + nc, nw, (const double*)dw.p, (double*)dout.p, stream);
         std::vector<double> out((size_t)nc);
         AFX_CUDA(cudaMemcpyAsync(out.data(), dout.p, (size_t)nc * 8, cudaMemcpyDeviceToHost, stream));
         AFX_CUDA(cudaStreamSynchronize(stream));

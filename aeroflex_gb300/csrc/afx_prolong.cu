@@ -133,7 +133,48 @@ __global__ void __launch_bounds__(256) k_wall_dist(const int nc, const double* _
     if (act) out[i] = mind;
 }
 
+// Spalart-Allmaras wall distance: for every cell, the least distance from its
+// centroid to a no-slip wall face (segment a-b, seg = ax, ay, bx, by per
+// face), faces scanned in boundary order (std::min); 1e15 without a wall.
+__global__ void __launch_bounds__(256) k_wall_seg_dist(const int nc, const double* __restrict__ cx,
+                                                       const double* __restrict__ cy, const int nw,
+                                                       const double* __restrict__ seg, double* __restrict__ out) {
+    __shared__ double ss[4 * PT];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool act = i < nc;
+    const double xi = act ? cx[i] : 0.0, yi = act ? cy[i] : 0.0;
+    double mind = 1e15;
+    bool first = true;
+    for (int t0 = 0; t0 < nw; t0 += PT) {
+        const int tn = min(PT, nw - t0);
+        __syncthreads();
+        for (int t = threadIdx.x; t < 4 * tn; t += blockDim.x) ss[t] = seg[4 * t0 + t];
+        __syncthreads();
+        if (act)
+            for (int t = 0; t < tn; ++t) {
+                const double ex = ss[4 * t + 2] - ss[4 * t], ey = ss[4 * t + 3] - ss[4 * t + 1];
+                const double px = xi - ss[4 * t], py = yi - ss[4 * t + 1];
+                double u = (px * ex + py * ey) / (ex * ex + ey * ey);
+                u = u < 0.0 ? 0.0 : (u > 1.0 ? 1.0 : u);
+                const double dx = px - u * ex, dy = py - u * ey;
+                const double d = sqrt(dx * dx + dy * dy);
+                if (first) {
+                    mind = d;
+                    first = false;
+                } else {
+                    mind = (d < mind) ? d : mind;
+                }
+            }
+    }
+    if (act) out[i] = mind;
+}
+
 }  // namespace dev
+
+void enqueue_wall_seg_dist(int nc, const double* cx, const double* cy, int nw, const double* seg, double* out,
+                           cudaStream_t s) {
+    dev::k_wall_seg_dist<<<(nc + 255) / 256, 256, 0, s>>>(nc, cx, cy, nw, seg, out);
+}
 
 void enqueue_wall_dist(int nc, const double* cx, const double* cy, int nw, const double* wx, const double* wy,
                        double* out, cudaStream_t s) {

@@ -156,7 +156,9 @@ class ExplicitSolver {
     std::vector<double> nu, nuk, nuW, mut;
     std::vector<std::array<uint, 4>> cellFaces;  // a real cell's edges, ascending, EDGE_NULL padded
     double nu_far = 0.;                          // nu~ of the far field: 3 mu_L / rho_inf
+    std::vector<double> sa_wd;                   // distance to the nearest no-slip wall face, per real cell
     void sa_setup();
+    void sa_wall_distance();
     void sa_init();                                                        // nu~ = nu_far
     void calc_mut(const std::vector<double>& q_, const std::vector<double>& nu_);
     void calc_nu_residual(const std::vector<double>& q_, const std::vector<double>& nu_);

@@ -33,7 +33,10 @@
 //   (nu_f + f_n nu~_f) from the face means, (nu~_j - nu~_i)(d.n)/(d.d);
 // - c_b2 term with the Green-Gauss gradient of nu~ (face value = mean);
 // - source with Omega = |dv/dx - du/dy| from the mean-flow cell gradients
-//   and d the wall distance of mesh::compute_wall_dist (mesh.h:794-830);
+//   and d the distance from the centroid to the nearest no-slip wall face
+//   (point to segment; the reference's compute_wall_dist, mesh.h:794-830,
+//   measures to face centres, which overstates d near a wall by half a face
+//   length and weakens the destruction term there);
 // - ghosts: nu~ = -nu~_i at no-slip walls (zero on the wall), nu~_i at slip
 //   walls, 3 mu_L/rho_inf at the far field; ghost velocity and density from
 //   the boundary functors' ghost state (physics.h:311-530).
@@ -138,11 +141,48 @@ void ExplicitSolver::sa_setup() {
         std::sort(f.begin(), f.end());  // EDGE_NULL (the largest value) sorts last
         cellFaces[i] = f;
     }
-    m.compute_wall_dist(st.bcs);
+    sa_wall_distance();
     double qf[4];
     get_boundary_variables().conservative(st.g, qf);
     nu_far = 3. * st.g.mu_L / qf[0];
     sa_init();
+}
+
+// Distance from each real cell's centroid to the nearest no-slip wall face
+// (a segment), faces scanned in boundary order; 1e15 without a wall.
+void ExplicitSolver::sa_wall_distance() {
+    std::vector<double> seg;  // ax, ay, bx, by per wall face
+    for (size_t b = 0; b < m.boundaryEdges.size(); ++b)
+        if (st.bcs.at(m.boundaryEdgesPhysicals[b]).type == BC_WALL) {
+            const uint e = m.boundaryEdges[b];
+            seg.push_back(m.nodesX[m.edgesNodes[e][0]]);
+            seg.push_back(m.nodesY[m.edgesNodes[e][0]]);
+            seg.push_back(m.nodesX[m.edgesNodes[e][1]]);
+            seg.push_back(m.nodesY[m.edgesNodes[e][1]]);
+        }
+    const int NR = (int)m.nRealCells;
+    sa_wd.assign(NR, 1e15);
+#pragma omp parallel for
+    for (int i = 0; i < NR; ++i) {
+        const double cx = m.cellsCentersX[i], cy = m.cellsCentersY[i];
+        double mind = 1e15;
+        bool first = true;
+        for (size_t k = 0; k < seg.size(); k += 4) {
+            const double ex = seg[k + 2] - seg[k], ey = seg[k + 3] - seg[k + 1];
+            const double px = cx - seg[k], py = cy - seg[k + 1];
+            double t = (px * ex + py * ey) / (ex * ex + ey * ey);
+            t = t < 0. ? 0. : (t > 1. ? 1. : t);
+            const double dx = px - t * ex, dy = py - t * ey;
+            const double d = std::sqrt(dx * dx + dy * dy);
+            if (first) {
+                mind = d;
+                first = false;
+            } else {
+                mind = std::min(mind, d);
+            }
+        }
+        sa_wd[i] = mind;
+    }
 }
 
 void ExplicitSolver::sa_init() {
@@ -237,7 +277,7 @@ void ExplicitSolver::calc_nu_residual(const std::vector<double>& q_, const std::
         const double A = m.cellsAreas[i];
         const double gnx = ggx / A, gny = ggy / A;
         double src, dsrc;
-        sa_source(nut_i, nul_i, omega, m.wall_dist[i], &src, &dsrc);
+        sa_source(nut_i, nul_i, omega, sa_wd[i], &src, &dsrc);
         const double R = -conv + diff / SA_SIGMA + SA_CB2 / SA_SIGMA * (gnx * gnx + gny * gny) * A + src * A;
         nuW[i] = R / A;
     }
