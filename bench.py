@@ -513,18 +513,20 @@ def batch_sweep(n_cases=256, K=100, K64=10, warmup=3):
     return out
 
 
-def batch_converge(n_cases=16, tol=1e-10, max_it=200):
-    """Polar sweep to convergence: ``n_cases`` cases of the batched polar-sweep
-    generator (seed 4) solved to err/err_0 <= tol by the implicit solver, as
-    one FP32-mixed batch (FP32 Jacobians and Krylov vectors, FP64 residual)
-    and as the FP64 per-case loop.  Reports both device times and the largest
-    C_L / C_D difference between them (the FP32-mixed batch converges to the
-    FP64 fixed point of every case)."""
+def batch_converge(n_cases=16, tol=1e-10, max_it=300, max_cells=40000):
+    """Batched polar sweep to convergence (the same implicit solver in every
+    arm): ``n_cases`` subsonic cases (M <= 0.5, AoA <= 8 deg) of the
+    polar-sweep generator (seed 4) with at most ``max_cells`` cells each,
+    solved to err/err_0 <= tol as one FP32-mixed batch (FP32 Jacobians and
+    Krylov vectors, FP64 residual), as one FP64 batch, and as the FP64
+    per-case loop (the reference's polar loop).  Reports device times, the
+    FP32-mixed batch's speed-up over the FP64 batch (same algorithm) and
+    over the per-case loop, and the largest C_L / C_D difference to the FP64
+    batch."""
     from aeroflex_gb300 import meshgen, rans
 
-    # the subsonic, moderate-angle cases (M <= 0.5, AoA <= 8 deg): the
-    # explicit scheme's transonic high-angle cases do not reach a steady state
-    cases = [c for c in meshgen.polar_sweep_cases(256, seed=4) if c["mach"] <= 0.5 and c["aoa_deg"] <= 8.0][:n_cases]
+    cases = [c for c in meshgen.polar_sweep_cases(256, seed=4)
+             if c["mach"] <= 0.5 and c["aoa_deg"] <= 8.0 and c["n_cells"] <= max_cells][:n_cases]
     meshes = [rans.mesh.from_arrays(c["mesh"]) for c in cases]
 
     def settings(c, prec):
@@ -534,37 +536,101 @@ def batch_converge(n_cases=16, tol=1e-10, max_it=200):
         return st
 
     t0 = time.time()
-    b = rans.Batch(meshes, [settings(c, "fp32-mixed") for c in cases])
-    b.init()
-    it_b, err_b, st_b = b.run_solver(tol, max_it)
-    t_batch = b.last_device_seconds()
-    fb = [b.forces(k, "wall") for k in range(n_cases)]
-    del b
-    t64, dcl, dcd, conv = 0.0, 0.0, 0.0, 0
+    out = {"cases": len(cases), "cells_total": int(sum(m.nRealCells for m in meshes)), "tolerance": tol,
+           "workload": "first %d cases with M <= 0.5, AoA <= 8 deg and <= %d cells of the polar-sweep generator "
+                       "(seed 4), Euler, implicit solver, CFL 40 -> 100, to err/err_0 <= %g" % (n_cases, max_cells, tol)}
+    forces = {}
+    for prec in ("fp32-mixed", "fp64"):
+        b = rans.Batch(meshes, [settings(c, prec) for c in cases])
+        b.init()
+        it_b, err_b, st_b = b.run_solver(tol, max_it)
+        key = "batch_" + prec.replace("-", "_")
+        out[key] = {"device_s": b.last_device_seconds(), "iterations": [int(x) for x in it_b],
+                    "converged": int(sum(1 for e in err_b if e <= tol))}
+        forces[prec] = [b.forces(k, "wall") for k in range(len(cases))]
+        del b
+    t64 = 0.0
     its64 = []
-    for k, (c, m) in enumerate(zip(cases, meshes)):
+    for c, m in zip(cases, meshes):
         s = rans.Solver(m, settings(c, "fp64"))
         s.init()
         try:
             n, e = s.run_solver(tol, max_it)
         except rans.AfxError:
-            n, e = max_it, float("nan")
+            n = max_it
         t64 += s.last_device_seconds()
-        its64.append(n)
-        w = rans.get_wall_profile(s, "wall")
-        if e <= tol and err_b[k] <= tol:
-            conv += 1
-            dcl = max(dcl, abs(w["cl"] - fb[k]["cl"]))
-            dcd = max(dcd, abs(w["cd"] - fb[k]["cd"]))
+        its64.append(int(n))
         del s
-    return {"cases": n_cases, "cells_total": int(sum(m.nRealCells for m in meshes)), "tolerance": tol,
-            "workload": "first %d cases with M <= 0.5 and AoA <= 8 deg of the polar-sweep generator (seed 4), "
-                        "implicit solver, CFL 40 -> 100" % n_cases,
-            "batch_fp32_mixed_s": t_batch, "per_case_fp64_s": t64,
-            "speedup_batch_fp32_mixed_vs_per_case_fp64": t64 / t_batch if t_batch > 0 else None,
-            "converged_both": conv, "max_abs_dcl": dcl, "max_abs_dcd": dcd,
-            "batch_iterations": [int(x) for x in it_b], "per_case_iterations": its64,
-            "wall_s": time.time() - t0}
+    out["per_case_fp64"] = {"device_s": t64, "iterations": its64}
+    f32, f64 = forces["fp32-mixed"], forces["fp64"]
+    out["max_abs_dcl_fp32_mixed_vs_fp64"] = max(abs(a["cl"] - b["cl"]) for a, b in zip(f32, f64))
+    out["max_abs_dcd_fp32_mixed_vs_fp64"] = max(abs(a["cd"] - b["cd"]) for a, b in zip(f32, f64))
+    t32 = out["batch_fp32_mixed"]["device_s"]
+    out["speedup_batch_fp32_mixed_vs_batch_fp64"] = out["batch_fp64"]["device_s"] / t32 if t32 > 0 else None
+    out["speedup_batch_fp32_mixed_vs_per_case_fp64"] = t64 / t32 if t32 > 0 else None
+    out["wall_s"] = time.time() - t0
+    return out
+
+
+def c2_time_to_cl(budget32=150.0, budget64=330.0, sample=100):
+    """Config 2: NACA0012 on the hybrid boundary-layer mesh (512 x 60 quads,
+    first height 1e-6 chord, growth 1.1, Delaunay fill to 100 chords, 201k
+    cells), Spalart-Allmaras, Re 6e6, M 0.15, AoA 10 deg, implicit solver
+    (first order: the reference's second-order reconstruction diverges on
+    this mesh at every CFL tried), CFL 5 -> 200.  The FP32-mixed path runs
+    until err/err_0 <= 1e-10 and gives C_L*; the FP64 path runs until its
+    C_L has stayed within 1e-7 of C_L* for two samples.  Time to C_L within
+    1e-6 of C_L* (C_L sampled every ``sample`` iterations, device seconds)
+    for both, and the FP32-mixed speed-up."""
+    from aeroflex_gb300 import meshgen, rans
+
+    t0 = time.time()
+    m = rans.mesh.from_arrays(meshgen.hybrid_airfoil())
+    mach, aoa = 0.15, 10.0
+    mu = 1.4 * mach / 6e6
+
+    def run(prec, budget, stop):
+        st = rans.Settings().set("solver", "implicit").set("precision", prec).set("viscosity", "spalart-allmaras")
+        st.set("mu_L", mu).set("second_order", 0.0).set("start_cfl", 5.0).set("slope_cfl", 5.0).set("max_cfl", 200.0)
+        st.set_bc("farfield", "farfield", 1.0, mach, aoa * 0.01745, 1.0).set_bc("wall", "wall")
+        g = rans.Solver(m, st)
+        g.init()
+        samples, dev, its, t1, err = [], 0.0, 0, time.time(), 1.0
+        while time.time() - t1 < budget:
+            n, err = g.run_solver(1e-10, sample)
+            its += n
+            dev += g.last_device_seconds()
+            w = rans.get_wall_profile(g, "wall")
+            samples.append((its, dev, w["cl"], w["cd"]))
+            if n < sample or stop(samples):
+                break
+        del g
+        return samples, err
+
+    s32, e32 = run("fp32-mixed", budget32, lambda s: False)
+    cl_ref = s32[-1][2]
+    s64, e64 = run("fp64", budget64,
+                   lambda s: len(s) >= 2 and all(abs(x[2] - cl_ref) <= 1e-7 for x in s[-2:]))
+
+    def hit(samples):
+        return next((x for i, x in enumerate(samples) if all(abs(y[2] - cl_ref) <= 1e-6 for y in samples[i:])),
+                    None)
+
+    h32, h64 = hit(s32), hit(s64)
+    out = {"case": "config 2: hybrid mesh %d cells, SA, Re 6e6, M 0.15, AoA 10 deg, implicit first order" %
+                   m.nRealCells,
+           "cl_converged_fp32_mixed": cl_ref, "err_fp32_mixed": e32, "iterations_fp32_mixed": s32[-1][0],
+           "cl_fp64_last": s64[-1][2], "cd_fp64_last": s64[-1][3], "err_fp64": e64, "iterations_fp64": s64[-1][0],
+           "cl_error_fp64_vs_fp32_mixed": abs(s64[-1][2] - cl_ref),
+           "cd_error_fp64_vs_fp32_mixed": abs(s64[-1][3] - s32[-1][3]),
+           "time_to_cl_1e-6_s_fp32_mixed": None if h32 is None else h32[1],
+           "time_to_cl_1e-6_s_fp64": None if h64 is None else h64[1],
+           "iterations_to_cl_1e-6_fp32_mixed": None if h32 is None else h32[0],
+           "iterations_to_cl_1e-6_fp64": None if h64 is None else h64[0]}
+    if h32 and h64:
+        out["speedup_time_to_cl_fp32_mixed_vs_fp64"] = h64[1] / h32[1]
+    out["wall_s"] = time.time() - t0
+    return out
 
 
 def cpu_baseline(budget_s=12.0):
@@ -670,9 +736,9 @@ def main():
     ap.add_argument("--no-cl", action="store_true", help="skip the time-to-C_L leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched polar-sweep leg")
     ap.add_argument("--batch-cases", type=int, default=256)
-    ap.add_argument("--batch-converge", action="store_true",
-                    help="also solve 16 polar-sweep cases to convergence (implicit FP32-mixed batch vs FP64 per case; "
-                         "about 12 minutes)")
+    ap.add_argument("--no-batch-converge", action="store_true",
+                    help="skip the batched polar sweep to convergence (FP32-mixed batch vs FP64 batch vs per case)")
+    ap.add_argument("--no-c2", action="store_true", help="skip the config 2 (SA, hybrid mesh) time-to-C_L leg")
     ap.add_argument("--nx", type=int, default=NX)
     ap.add_argument("--ny", type=int, default=NY)
     ap.add_argument("--lean", action="store_true", help="warm-up + timed iterations only (for ncu)")
@@ -745,8 +811,10 @@ def main():
         line["time_to_cl"] = time_to_cl()
     if not args.no_batch:
         line["batch"] = batch_sweep(args.batch_cases)
-    if args.batch_converge:
+    if not args.no_batch_converge:
         line["batch_converge"] = batch_converge()
+    if not args.no_c2:
+        line["c2_time_to_cl"] = c2_time_to_cl()
     print(json.dumps(line))
 
 
