@@ -9,12 +9,12 @@
 // bit for bit.  Only tests/, __graft_entry__.smoke() and bench.py's CPU
 // baseline may load it, and only as the checker.
 //
-// PARITY STATUS: unpinned.  The reference ships no tests, golden vectors or
-// stored results, and it cannot be built here (it needs Eigen, which is not
-// installed and cannot be fetched).  The restatement is therefore checked
-// against analytic invariants (flux consistency, conservation, freestream
-// preservation, mirror symmetry) and its outputs are committed as regression
-// fixtures, not as reference outputs.
+// PARITY STATUS: pinned to the reference's own code.  oracle/build_ref.py
+// compiles the reference's unmodified rans headers (with the Eigen-API
+// stand-in of oracle/eigen_api) into oracle/_ref; tests/test_ref_pin.py
+// checks that this restatement reproduces, bit for bit, every result that
+// code committed to tests/golden/ref_pins.json, and, where the reference tree
+// is present, that both agree directly on more inputs.
 //
 // Deliberate decisions where the reference is ill-defined:
 //  * unqualified abs() on doubles (mesh.h:435,442; solver.h:335-336,344) is
