@@ -49,6 +49,7 @@ def _units():
         (nv + ["-fmad=false", "-c"], "afx_prolong.cu"),
         (nv + ["-use_fast_math", "-c"], "afx_kernels_f32.cu"),
         (nv + ["-c"], "afx_peak.cu"),
+        (nv + ["-c"], "afx_krylov.cu"),
     ], nvcc
 
 

@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "afx_host.hpp"
+#include "afx_krylov.hpp"
 #include "afx_launch.hpp"
 
 namespace afx {
@@ -46,10 +47,10 @@ void implicit_fill(ImplicitEngine* e, const StepArgs& a, int p, cudaStream_t s);
 int implicit_solve_update(ImplicitEngine* e, const StepArgs& a, int p, const double* b, double relax,
                           cudaStream_t s);
 void implicit_transpose(ImplicitEngine* e, cudaStream_t s);
-void implicit_norm2(ImplicitEngine* e, const StepArgs& a, const double* v, double* out, cudaStream_t s);
-void implicit_adjoint_rho(ImplicitEngine* e, const double* u, const double* g, double* rho, cudaStream_t s);
-int implicit_adjoint_step(ImplicitEngine* e, const StepArgs& a, const double* rho, double relax, double* lam,
-                          cudaStream_t s);
+int implicit_apply_inverse(ImplicitEngine* e, const StepArgs& a, const double* b, const double* area, double scale,
+                           double* out, cudaStream_t s);
+int implicit_apply_sweep(ImplicitEngine* e, const StepArgs& a, const double* b, const double* area, double scale,
+                         double* out, cudaStream_t s);
 }  // namespace afx
 
 using namespace afx;
@@ -260,6 +261,7 @@ struct afx_solver_s {
     // adjoint work arrays (allocated on first use) and the last adjoint state
     struct AdjointBufs {
         DevBuf v, fbar, gbx, gby, qbar, lw, lt, u, bqbar, g, q, lam[2], ls[2], partials;
+        DevBuf lam_obj[2];  // the last implicit adjoint solution of C_L / C_D (initial guess of the next)
         AdjArgs args(const void* v_dev, void* u_dev) const {
             AdjArgs j;
             j.v = v_dev;
@@ -944,6 +946,9 @@ int afx_config_set_double(afx_config c, const char* key, double v) {
             c->s.fp64_finish = v != 0;
         } else if (k == "krylov_graph") {
             c->s.krylov_graph = v != 0;
+        } else if (k == "krylov_preconditioner") {
+            if (v != 0 && v != 1) throw Error(AFX_ERR_CONFIG, "krylov_preconditioner must be 0 or 1");
+            c->s.krylov_preconditioner = (int)v;
         }
         else if (k == "second_order") c->s.second_order = v != 0;
         else if (double* p = dfield(c->s, k)) *p = v;
@@ -961,6 +966,7 @@ int afx_config_get_double(afx_config c, const char* key, double* v) {
         else if (k == "fp64_correction_interval") *v = c->s.fp64_correction_interval;
         else if (k == "fp64_finish") *v = c->s.fp64_finish ? 1 : 0;
         else if (k == "krylov_graph") *v = c->s.krylov_graph ? 1 : 0;
+        else if (k == "krylov_preconditioner") *v = c->s.krylov_preconditioner;
         else if (k == "second_order") *v = c->s.second_order ? 1 : 0;
         else if (double* p = dfield(c->s, k)) *v = *p;
         else throw Error(AFX_ERR_ARG, "unknown numeric setting '" + k + "'");
@@ -1529,6 +1535,139 @@ int afx_iterate(afx_solver s, int n_iters, double* res_norm) {
         if (res_norm) *res_norm = s->h_ctrl->last_norm;
         if (s->h_ctrl->status == 4) throw Error(AFX_ERR_NONFINITE, "residual norm is not finite");
         if (done < 0) throw Error(AFX_ERR_STOPPED, "stopped by request");
+    });
+}
+
+// Newton-Krylov finish of an implicit solver (no counterpart in the
+// reference, whose implicit iteration keeps a pseudo-time term): solve
+// RHS(q) = 0 (fillRhoRHS, the flux balance of every real cell) by inexact
+// Newton steps J dq = RHS(q), J = -dRHS/dq applied matrix-free as a
+// one-sided difference of the right-hand side (step 1e-7 of the state's
+// RMS over the direction's), each solved by flexible GMRES to lin_tol
+// relative, preconditioned by the solver's own linear solve with its matrix
+// at `cfl` (A/dt + the face Jacobians, formed at the Newton iterate).  Each
+// step is backtracked (halved up to 8 times) until ||RHS|| falls; a step
+// that finds no decrease (the round-off floor of the right-hand side) ends
+// the solve at the step's start.  err is ||RHS|| / err_0, err_0 the norm of
+// the freestream state's face fluxes.  record (cap rows of 4, may be null):
+// per Newton step err after it, the step length, its Krylov steps and the
+// linear residual reached.
+static double newton_run(afx_solver_s* s, double tol, int max_newton, double cfl, double lin_tol, int max_krylov,
+                         int* n_newton, int* n_krylov, double* record, int cap) {
+    if (!s->imp) throw Error(AFX_ERR_CONFIG, "newton: needs an implicit solver");
+    if (s->a.visc == 2) throw Error(AFX_ERR_CONFIG, "newton: the Spalart-Allmaras equation is not in its system");
+    if (s->a.n_cases > 0) throw Error(AFX_ERR_CONFIG, "newton: not for batches");
+    s->ensure_shadow();
+    s->materialize_qW();
+    s->set_ctrl(0, 0, 0);
+    StepArgs A = s->A64();
+    if (A.ctrl != s->a.ctrl) AFX_CUDA(cudaMemsetAsync(A.ctrl, 0, sizeof(Ctrl), s->stream));
+    const int p = s->parity;
+    double err0 = 1.0;
+    {
+        // the freestream fluxes alone (qW, which run_solver adds, cleared)
+        double qf[4];
+        conservative(s->st, s->freestream(), qf);
+        AFX_CUDA(cudaMemsetAsync(A.Rq, 0, (size_t)A.n_cells * 32, s->stream));
+        enqueue_uniform_f64(A, p, qf, s->stream);
+        Ctrl c;
+        AFX_CUDA(cudaMemcpyAsync(&c, A.ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, s->stream));
+        AFX_CUDA(cudaStreamSynchronize(s->stream));
+        err0 = c.err0 > 0 ? c.err0 : 1.0;
+    }
+    const size_t N = A.n_cells;
+    const long long n4 = 4LL * (long long)N;
+    KrylovSpace ks(n4, 60);
+    DevBuf q0, b, rp, pc, dq;
+    for (DevBuf* d : {&q0, &b, &rp, &pc, &dq}) d->alloc(N * 32);
+    double* qm = (double*)A.qm[p];
+    StepArgs r = A;
+    r.Rq = rp.p;  // right-hand sides of perturbed states
+    int nn = 0, nk = 0;
+    AFX_CUDA(cudaEventRecord(s->ev0, s->stream));
+    double e = s->imp_rhs(p);
+    try {
+        while (e / err0 > tol && nn < max_newton) {
+            if (!(e == e)) throw Error(AFX_ERR_NONFINITE, "newton: residual norm is not finite");
+            StepArgs m = A;
+            m.cfl = cfl;
+            implicit_fill(s->imp, m, p, s->stream);
+            AFX_CUDA(cudaMemcpyAsync(q0.p, qm, N * 32, cudaMemcpyDeviceToDevice, s->stream));
+            AFX_CUDA(cudaMemcpyAsync(b.p, s->imp_b, N * 32, cudaMemcpyDeviceToDevice, s->stream));
+            const double qrms = std::sqrt(kv_dot(ks, (const double*)q0.p, (const double*)q0.p, s->stream) / n4);
+            const KrylovOp op = [&](const double* v, double* out) {
+                const double vrms = std::sqrt(kv_dot(ks, v, v, s->stream) / n4);
+                if (vrms == 0) {
+                    AFX_CUDA(cudaMemsetAsync(out, 0, N * 32, s->stream));
+                    return;
+                }
+                const double eps = 1e-7 * std::max(1.0, qrms) / vrms;
+                kv_axpby(ks, eps, v, 1.0, (const double*)q0.p, qm, s->stream);
+                enqueue_rhs_f64(r, p, s->stream);
+                kv_axpby(ks, -1.0 / eps, (const double*)rp.p, 1.0 / eps, (const double*)b.p, out, s->stream);
+            };
+            const KrylovOp pre = [&](const double* v, double* out) {
+                AFX_CUDA(cudaMemcpyAsync(pc.p, v, N * 32, cudaMemcpyDeviceToDevice, s->stream));
+                const int rc = s->st.krylov_preconditioner == 1
+                                   ? implicit_apply_inverse(s->imp, A, (const double*)pc.p, nullptr, 1.0, out, s->stream)
+                                   : implicit_apply_sweep(s->imp, A, (const double*)pc.p, nullptr, 1.0, out, s->stream);
+                if (rc < 0) throw Error(AFX_ERR_DIVERGED, "newton: singular diagonal block");
+            };
+            const FgmresResult fr =
+                fgmres(ks, (const double*)b.p, (double*)dq.p, true, lin_tol, max_krylov, op, pre, s->stream);
+            nk += fr.iters;
+            double lam = 1.0, en = 0;
+            bool stalled = false;
+            for (int ls = 0;; ++ls) {
+                kv_axpby(ks, lam, (const double*)dq.p, 1.0, (const double*)q0.p, qm, s->stream);
+                en = s->imp_rhs(p);
+                if (en == en && en < e) break;
+                if (ls == 8) {
+                    AFX_CUDA(cudaMemcpyAsync(qm, q0.p, N * 32, cudaMemcpyDeviceToDevice, s->stream));
+                    en = s->imp_rhs(p);
+                    stalled = true;
+                    break;
+                }
+                lam *= 0.5;
+            }
+            if (record && nn < cap) {
+                double* row = record + 4 * (size_t)nn;
+                row[0] = en / err0;
+                row[1] = stalled ? 0.0 : lam;
+                row[2] = fr.iters;
+                row[3] = fr.res / std::max(fr.b_norm, 1e-300);
+            }
+            e = en;
+            ++nn;
+            if (stalled) break;
+        }
+    } catch (...) {
+        s->imp_sync();
+        throw;
+    }
+    AFX_CUDA(cudaEventRecord(s->ev1, s->stream));
+    AFX_CUDA(cudaEventSynchronize(s->ev1));
+    float ms = 0;
+    AFX_CUDA(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+    s->last_sec = ms * 1e-3;
+    s->imp_sync();
+    if (n_newton) *n_newton = nn;
+    if (n_krylov) *n_krylov = nk;
+    return e / err0;
+}
+
+int afx_newton_solve(afx_solver s, double tol, int max_newton, double cfl, double lin_tol, int max_krylov,
+                     int* newton_iters, int* krylov_iters, double* err, double* record, int record_cap) {
+    return guarded([&] {
+        if (!s) throw Error(AFX_ERR_ARG, "null argument");
+        if (tol <= 0) tol = s->st.tolerance;
+        if (max_newton <= 0) max_newton = 20;
+        if (cfl <= 0) cfl = s->st.max_cfl;
+        if (lin_tol <= 0) lin_tol = 1e-3;
+        if (max_krylov <= 0) max_krylov = 300;
+        const double e = newton_run(s, tol, max_newton, cfl, lin_tol, max_krylov, newton_iters, krylov_iters,
+                                    record, record_cap);
+        if (err) *err = e;
     });
 }
 
@@ -2214,40 +2353,47 @@ int afx_adjoint_solve(afx_solver s, const char* patch, const char* objective, do
         int q = 0, it = 0;
         double r0 = -1, r = 0;
         if (s->imp) {
-            // an implicit solver: defect correction with its own matrix at the
-            // converged state, transposed -- rho = dJ/dq + (dR/dq)^T lam (the
-            // exact vJP), M^T d = rho (GMRES, the transposed ILU(0)), then
-            // lam += relaxation * A d: the primal's implicit iteration for the
-            // adjoint equation (dR/dq)^T lam = -dJ/dq
+            // an implicit solver: (dR/dq)^T lam = -dJ/dq by flexible GMRES on
+            // the exact transposed Jacobian (the vJP kernel), preconditioned
+            // by the solver's own linear solve with its matrix at max_cfl,
+            // transposed: M^T d = v (GMRES, the transposed ILU(0)), then
+            // -A .* d -- the primal's implicit iteration for the adjoint
+            // equation (dR/dq = -M/A as the CFL grows), accelerated
             StepArgs m = a;
             m.cfl = s->st.max_cfl;
             implicit_fill(s->imp, m, p, s->stream);
             implicit_transpose(s->imp, s->stream);
             enqueue_adjoint_prep(a, p, false, s->stream);  // gradients and limiter of the state for the vJP
-            AFX_CUDA(cudaMemsetAsync(J.lam[0].p, 0, N * 32, s->stream));
-            double* nrm = (double*)J.partials.p;
-            auto norm = [&](const void* v) {
-                implicit_norm2(s->imp, a, (const double*)v, nrm, s->stream);
-                double h = 0;
-                AFX_CUDA(cudaMemcpyAsync(&h, nrm, 8, cudaMemcpyDeviceToHost, s->stream));
-                AFX_CUDA(cudaStreamSynchronize(s->stream));
-                return std::sqrt(h);
+            const long long n4 = 4LL * (long long)N;
+            KrylovSpace ks(n4, 60);
+            DevBuf rhs, pc;
+            rhs.alloc(N * 32);
+            pc.alloc(N * 32);
+            kv_axpby(ks, -1.0, (const double*)J.g.p, 0.0, nullptr, (double*)rhs.p, s->stream);
+            DevBuf& last = J.lam_obj[obj == "cl" ? 0 : 1];
+            const bool warm = last.p != nullptr;
+            if (warm) AFX_CUDA(cudaMemcpyAsync(J.lam[0].p, last.p, N * 32, cudaMemcpyDeviceToDevice, s->stream));
+            const KrylovOp op = [&](const double* v, double* out) {
+                enqueue_vjp(a, p, J.args(v, out), s->stream);
+            };
+            const KrylovOp pre = [&](const double* v, double* out) {
+                AFX_CUDA(cudaMemcpyAsync(pc.p, v, N * 32, cudaMemcpyDeviceToDevice, s->stream));
+                const double* area = (const double*)a.area;
+                const int rc = s->st.krylov_preconditioner == 1
+                                   ? implicit_apply_inverse(s->imp, a, (const double*)pc.p, area, -1.0, out, s->stream)
+                                   : implicit_apply_sweep(s->imp, a, (const double*)pc.p, area, -1.0, out, s->stream);
+                if (rc < 0) throw Error(AFX_ERR_NONFINITE, "adjoint: singular diagonal block");
             };
             AFX_CUDA(cudaEventRecord(s->ev0, s->stream));
-            const double g0 = norm(J.g.p);
-            r0 = g0 > 0 ? g0 : 1.0;
-            for (;;) {
-                enqueue_vjp(a, p, J.args(J.lam[0].p, J.u.p), s->stream);
-                implicit_adjoint_rho(s->imp, (const double*)J.u.p, (const double*)J.g.p, (double*)s->imp_b,
-                                     s->stream);
-                r = norm(s->imp_b);
-                if (!(r == r) || r > 1.7976931348623157e308) throw Error(AFX_ERR_NONFINITE, "adjoint diverged");
-                if (r / r0 < tol || it >= max_it || s->stop.load()) break;
-                if (implicit_adjoint_step(s->imp, a, (const double*)s->imp_b, s->st.relaxation, (double*)J.lam[0].p,
-                                          s->stream) < 0)
-                    throw Error(AFX_ERR_NONFINITE, "adjoint: singular diagonal block");
-                ++it;
-            }
+            const FgmresResult fr =
+                fgmres(ks, (const double*)rhs.p, (double*)J.lam[0].p, !warm, tol, max_it, op, pre, s->stream);
+            if (!last.p) last.alloc(N * 32);
+            AFX_CUDA(cudaMemcpyAsync(last.p, J.lam[0].p, N * 32, cudaMemcpyDeviceToDevice, s->stream));
+            if (!(fr.res == fr.res) || fr.res > 1.7976931348623157e308)
+                throw Error(AFX_ERR_NONFINITE, "adjoint diverged");
+            it = fr.iters;
+            r0 = fr.b_norm > 0 ? fr.b_norm : 1.0;
+            r = fr.res;
         } else {
             // gradients, limiter and local time step of the converged state
             enqueue_adjoint_prep(a, p, true, s->stream);
@@ -2400,23 +2546,30 @@ static afx_solver_s::PatchDeform& patch_deform(afx_solver_s* s, const std::strin
     return *s->pdef;
 }
 
-// Node displacement of a unit normal displacement of patch node k (index
-// into pnodes), added with factor c to (x, y)
-static void add_patch_mode(const afx_solver_s* s, const afx_solver_s::PatchDeform& d, int k, double c,
-                           std::vector<double>& x, std::vector<double>& y) {
+// Node displacement of a displacement (cx, cy) of patch node k (index into
+// pnodes), added to (x, y): the node itself moves by (cx, cy), every volume
+// node by its inverse-distance weight of node k times (cx, cy)
+static void add_patch_vec(const afx_solver_s* s, const afx_solver_s::PatchDeform& d, int k, double cx, double cy,
+                          std::vector<double>& x, std::vector<double>& y) {
     const std::vector<double>&X = s->nodes0x, &Y = s->nodes0y;
     const int vk = d.pnodes[k];
-    const double nxk = d.pnx[k], nyk = d.pny[k], p = d.power;
+    const double p = d.power;
     const long V = (long)X.size();
 #pragma omp parallel for
     for (long v = 0; v < V; ++v) {
         if (d.role[v] != 0) continue;
         const double w = std::pow(std::hypot(X[v] - X[vk], Y[v] - Y[vk]), -p) / d.W[v];
-        x[v] += c * w * nxk;
-        y[v] += c * w * nyk;
+        x[v] += w * cx;
+        y[v] += w * cy;
     }
-    x[vk] += c * nxk;
-    y[vk] += c * nyk;
+    x[vk] += cx;
+    y[vk] += cy;
+}
+
+// ... of a normal displacement c of patch node k (along its undeformed normal)
+static void add_patch_mode(const afx_solver_s* s, const afx_solver_s::PatchDeform& d, int k, double c,
+                           std::vector<double>& x, std::vector<double>& y) {
+    add_patch_vec(s, d, k, c * d.pnx[k], c * d.pny[k], x, y);
 }
 
 int afx_patch_nodes(afx_solver s, const char* patch, long long* ids, double* nx, double* ny, int cap, int* n) {
@@ -2447,6 +2600,84 @@ int afx_deform_patch(afx_solver s, const char* patch, const double* a, int n, do
     });
 }
 
+int afx_deform_patch_xy(afx_solver s, const char* patch, const double* dx, const double* dy, int n, double power) {
+    return guarded([&] {
+        if (!s || !patch || !dx || !dy) throw Error(AFX_ERR_ARG, "null argument");
+        if (power <= 0) power = 2.0;
+        const auto& d = patch_deform(s, patch, power);
+        if (n != (int)d.pnodes.size())
+            throw Error(AFX_ERR_ARG, "expected " + std::to_string(d.pnodes.size()) + " patch-node displacements");
+        std::vector<double> x = s->nodes0x, y = s->nodes0y;
+        for (int k = 0; k < n; ++k)
+            if (dx[k] != 0 || dy[k] != 0) add_patch_vec(s, d, k, dx[k], dy[k], x, y);
+        s->materialize_qW();
+        s->set_nodes(x.data(), y.data());
+    });
+}
+
+// d/dt of the Lagrangian J(q; X(a0 + t c)) + lam . R(q; X(a0 + t c)) at t = 0
+// for each direction c (one row of `dirs`, an entry per patch node), by
+// central differences with step h about the current node positions, at the
+// frozen converged state q: the adjoint's shape derivative along c.
+static void shape_directional(afx_solver_s* s, const afx_solver_s::PatchDeform& d, const char* objective, double h,
+                              const double* dirs, int n_dirs, bool xy, double* dJ) {
+    const int n = (int)d.pnodes.size();
+    auto& J = s->adjoint();
+    const size_t N = s->a.n_cells;
+    const std::string patch = d.patch;
+    s->materialize_qW();
+    // lambda (device order) to the host
+    std::vector<double> lam(4 * N), R(4 * N);
+    AFX_CUDA(cudaMemcpyAsync(lam.data(), J.lam[s->adj_parity].p, N * 32, cudaMemcpyDeviceToHost, s->stream));
+    AFX_CUDA(cudaStreamSynchronize(s->stream));
+    const std::vector<double> xc = s->hm.nodesX, yc = s->hm.nodesY;
+    const size_t V = xc.size();
+    const FarfieldVars vf = s->freestream();
+    const bool cl_obj = std::string(objective) == "cl";
+    StepArgs r = s->a;
+    r.Rq = J.u.p;  // scratch: the solver's qW stays
+    // J(q; X) + lambda . R(q; X) at the current state for nodes (x, y)
+    auto lagr = [&](const std::vector<double>& x, const std::vector<double>& y) {
+        s->set_nodes(x.data(), y.data());
+        s->set_ctrl(0, 0, 0);
+        r.area = s->a.area;
+        enqueue_residual_f64(r, s->parity, s->stream);
+        AFX_CUDA(cudaMemcpyAsync(R.data(), J.u.p, N * 32, cudaMemcpyDeviceToHost, s->stream));
+        double cl = 0, cd = 0;
+        forces_impl(s, patch, vf, &cl, &cd, nullptr, nullptr, 0, nullptr);
+        double lr = 0;
+        for (size_t i = 0; i < 4 * N; ++i) lr += lam[i] * R[i];
+        return (cl_obj ? cl : cd) + lr;
+    };
+    try {
+        std::vector<double> dx(V), dy(V), xp(V), yp(V), xm(V), ym(V);
+        for (int j = 0; j < n_dirs; ++j) {
+            std::fill(dx.begin(), dx.end(), 0.);
+            std::fill(dy.begin(), dy.end(), 0.);
+            if (xy) {
+                const double* c = dirs + (size_t)j * 2 * n;
+                for (int k = 0; k < n; ++k)
+                    if (c[2 * k] != 0 || c[2 * k + 1] != 0) add_patch_vec(s, d, k, c[2 * k], c[2 * k + 1], dx, dy);
+            } else {
+                const double* c = dirs + (size_t)j * n;
+                for (int k = 0; k < n; ++k)
+                    if (c[k] != 0) add_patch_mode(s, d, k, c[k], dx, dy);
+            }
+            for (size_t v = 0; v < V; ++v) {
+                xp[v] = xc[v] + h * dx[v];
+                yp[v] = yc[v] + h * dy[v];
+                xm[v] = xc[v] - h * dx[v];
+                ym[v] = yc[v] - h * dy[v];
+            }
+            dJ[j] = (lagr(xp, yp) - lagr(xm, ym)) / (2 * h);
+        }
+    } catch (...) {
+        s->set_nodes(xc.data(), yc.data());
+        throw;
+    }
+    s->set_nodes(xc.data(), yc.data());
+}
+
 int afx_adjoint_patch(afx_solver s, const char* patch, const char* objective, double power, double h, double* dJ,
                       int n) {
     return guarded([&] {
@@ -2458,43 +2689,45 @@ int afx_adjoint_patch(afx_solver s, const char* patch, const char* objective, do
         const auto& d = patch_deform(s, patch, power);
         if (n != (int)d.pnodes.size())
             throw Error(AFX_ERR_ARG, "expected room for " + std::to_string(d.pnodes.size()) + " sensitivities");
-        auto& J = s->adjoint();
-        const size_t N = s->a.n_cells;
-        s->materialize_qW();
-        // lambda (device order) to the host
-        std::vector<double> lam(4 * N), R(4 * N);
-        AFX_CUDA(cudaMemcpyAsync(lam.data(), J.lam[s->adj_parity].p, N * 32, cudaMemcpyDeviceToHost, s->stream));
-        AFX_CUDA(cudaStreamSynchronize(s->stream));
-        const std::vector<double> xc = s->hm.nodesX, yc = s->hm.nodesY;
-        const FarfieldVars vf = s->freestream();
-        const bool cl_obj = std::string(objective) == "cl";
-        StepArgs r = s->a;
-        r.Rq = J.u.p;  // scratch: the solver's qW stays
-        // J(q; X) + lambda . R(q; X) at the current state for nodes (x, y)
-        auto lagr = [&](const std::vector<double>& x, const std::vector<double>& y) {
-            s->set_nodes(x.data(), y.data());
-            s->set_ctrl(0, 0, 0);
-            r.area = s->a.area;
-            enqueue_residual_f64(r, s->parity, s->stream);
-            AFX_CUDA(cudaMemcpyAsync(R.data(), J.u.p, N * 32, cudaMemcpyDeviceToHost, s->stream));
-            double cl = 0, cd = 0;
-            forces_impl(s, patch, vf, &cl, &cd, nullptr, nullptr, 0, nullptr);
-            double lr = 0;
-            for (size_t i = 0; i < 4 * N; ++i) lr += lam[i] * R[i];
-            return (cl_obj ? cl : cd) + lr;
-        };
-        try {
-            for (int k = 0; k < n; ++k) {
-                std::vector<double> xp = xc, yp = yc, xm = xc, ym = yc;
-                add_patch_mode(s, d, k, h, xp, yp);
-                add_patch_mode(s, d, k, -h, xm, ym);
-                dJ[k] = (lagr(xp, yp) - lagr(xm, ym)) / (2 * h);
-            }
-        } catch (...) {
-            s->set_nodes(xc.data(), yc.data());
-            throw;
+        std::vector<double> dirs;  // unit vectors e_k
+        for (int k = 0; k < n; ++k) {
+            std::vector<double> e(n, 0.);
+            e[k] = 1.0;
+            dirs.insert(dirs.end(), e.begin(), e.end());
         }
-        s->set_nodes(xc.data(), yc.data());
+        shape_directional(s, d, objective, h, dirs.data(), n, false, dJ);
+    });
+}
+
+int afx_adjoint_patch_dirs(afx_solver s, const char* patch, const char* objective, double power, double h,
+                           const double* dirs, int n_dirs, int n_patch, double* dJ) {
+    return guarded([&] {
+        if (!s || !patch || !objective || !dirs || !dJ || n_dirs < 0) throw Error(AFX_ERR_ARG, "bad argument");
+        if (s->adj_patch != patch || s->adj_objective != objective)
+            throw Error(AFX_ERR_ARG,
+                        "afx_adjoint_patch_dirs needs afx_adjoint_solve of the same patch and objective first");
+        if (power <= 0) power = 2.0;
+        if (h <= 0) h = 1e-7;
+        const auto& d = patch_deform(s, patch, power);
+        if (n_patch != (int)d.pnodes.size())
+            throw Error(AFX_ERR_ARG, "directions must have " + std::to_string(d.pnodes.size()) + " entries");
+        shape_directional(s, d, objective, h, dirs, n_dirs, false, dJ);
+    });
+}
+
+int afx_adjoint_patch_dirs_xy(afx_solver s, const char* patch, const char* objective, double power, double h,
+                              const double* dirs, int n_dirs, int n_patch, double* dJ) {
+    return guarded([&] {
+        if (!s || !patch || !objective || !dirs || !dJ || n_dirs < 0) throw Error(AFX_ERR_ARG, "bad argument");
+        if (s->adj_patch != patch || s->adj_objective != objective)
+            throw Error(AFX_ERR_ARG,
+                        "afx_adjoint_patch_dirs_xy needs afx_adjoint_solve of the same patch and objective first");
+        if (power <= 0) power = 2.0;
+        if (h <= 0) h = 1e-7;
+        const auto& d = patch_deform(s, patch, power);
+        if (n_patch != (int)d.pnodes.size())
+            throw Error(AFX_ERR_ARG, "directions must have 2 x " + std::to_string(d.pnodes.size()) + " entries");
+        shape_directional(s, d, objective, h, dirs, n_dirs, true, dJ);
     });
 }
 

@@ -61,6 +61,9 @@ struct Settings {
     // loops (true), or drive the same kernels from a host loop (false: every
     // kernel is a plain launch that a profiler can list)
     bool krylov_graph = true;
+    // preconditioner of the Newton finish and of the implicit adjoint's
+    // flexible GMRES: 0 one ILU(0) sweep, 1 a GMRES solve with the matrix
+    int krylov_preconditioner = 1;
 
     int viscosity_code() const;
     static int bc_code(const std::string& t);

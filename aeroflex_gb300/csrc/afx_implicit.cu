@@ -898,24 +898,6 @@ __global__ void __launch_bounds__(128) k_imp_transpose(const int N, const Ell e,
         }
 }
 
-// rho = u + g over the real cells (AoS FP64)
-__global__ void __launch_bounds__(256) k_imp_adj_rho(const int n, const double* __restrict__ u,
-                                                     const double* __restrict__ g, double* __restrict__ rho) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) rho[i] = u[i] + g[i];
-}
-
-// lam += relax * A .* d (d in row order, lam in device cell order)
-__global__ void __launch_bounds__(256) k_imp_adj_update(const int n, const double* __restrict__ d,
-                                                        const int* __restrict__ perm,
-                                                        const double* __restrict__ area, const double relax,
-                                                        double* __restrict__ lam) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int c = __ldg(&perm[i >> 2]);
-    lam[4 * (size_t)c + (i & 3)] += relax * area[c] * d[i];
-}
-
 }  // namespace dev
 
 // ----------------------------------------------------------------- host
@@ -1354,6 +1336,63 @@ int implicit_solve_update(ImplicitEngine* e, const StepArgs& a, int p, const dou
     return it;
 }
 
+// out = scale * (area .* x) (area null: 1) in device order, x the engine's
+// last GMRES solution (row order)
+namespace dev {
+template <class T>
+__global__ void __launch_bounds__(256) k_imp_scatter(const int n, const T* __restrict__ x,
+                                                     const int* __restrict__ perm, const double* __restrict__ area,
+                                                     const double scale, double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int c = __ldg(&perm[i >> 2]);
+    out[4 * (size_t)c + (i & 3)] = scale * (area ? area[c] : 1.0) * (double)x[i];
+}
+}  // namespace dev
+
+// The engine's linear solve as an operator: M x = b (M^T after
+// implicit_transpose) by the same GMRES the implicit iteration uses, then
+// out = scale * (area .* x) in device order.  b must stay at one address
+// between calls (the solve graph is captured for it).  Returns the Krylov
+// iterations, -1 if a diagonal block was singular.
+int implicit_apply_inverse(ImplicitEngine* e, const StepArgs& a, const double* b, const double* area, double scale,
+                           double* out, cudaStream_t s) {
+    int sing = 0;
+    cudaMemcpyAsync(&sing, e->singular, sizeof(int), cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    if (sing) return -1;
+    const int it = e->f32 ? gmres<float>(e, a, b, s, 500) : gmres<double>(e, a, b, s, 500);
+    dev::k_imp_scatter<double><<<nb_(e->n4, 256), 256, 0, s>>>(e->n4, e->x, e->perm, area, scale, out);
+    e->last_iters = it;
+    return it;
+}
+
+namespace {
+template <class T>
+void sweep_t(ImplicitEngine* e, const StepArgs& a, const double* b, const double* area, double scale, double* out,
+             cudaStream_t s) {
+    Ops<T> o(e, a, s);
+    o.gather_b(b, (T*)e->t);
+    o.precond((const T*)e->t, nullptr, (T*)e->z, nullptr);
+    dev::k_imp_scatter<T><<<nb_(e->n4, 256), 256, 0, s>>>(e->n4, (const T*)e->z, e->perm, area, scale, out);
+}
+}  // namespace
+
+// The engine's preconditioner alone as an operator: one symmetric
+// multicolour block Gauss-Seidel sweep with the ILU(0) factors (of M, or of
+// M^T after implicit_transpose), out = scale * (area .* x) in device order.
+// Returns -1 if a diagonal block was singular, else 0.
+int implicit_apply_sweep(ImplicitEngine* e, const StepArgs& a, const double* b, const double* area, double scale,
+                         double* out, cudaStream_t s) {
+    int sing = 0;
+    cudaMemcpyAsync(&sing, e->singular, sizeof(int), cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    if (sing) return -1;
+    if (e->f32) sweep_t<float>(e, a, b, area, scale, out, s);
+    else sweep_t<double>(e, a, b, area, scale, out, s);
+    return 0;
+}
+
 // The filled system transposed in place (M -> M^T, the ILU(0) factors ->
 // those of M^T) for the adjoint's linear solves.  The next implicit_fill
 // forms M again.  FP64 engines.
@@ -1364,32 +1403,6 @@ void implicit_transpose(ImplicitEngine* e, cudaStream_t s) {
     cudaMemcpyAsync(e->V, e->off, (size_t)e->N * 64 * sizeof(double), cudaMemcpyDeviceToDevice, s);
     k_imp_transpose<double><<<nb_(e->N, 128), 128, 0, s>>>(e->N, e->ell(), (const double*)e->V, (double*)e->off,
                                                            (double*)e->dblk, (double*)e->dinv);
-}
-
-// ||v||^2 of an AoS FP64 vector over the real cells into out (device)
-void implicit_norm2(ImplicitEngine* e, const StepArgs& a, const double* v, double* out, cudaStream_t s) {
-    Ops<double> o(e, a, s);
-    o.template dots<0>(1, nullptr, v, const_cast<double*>(v), nullptr, out, nullptr);
-}
-
-// rho = g + (dR/dq)^T lam, u being the vJP (AoS FP64, device order)
-void implicit_adjoint_rho(ImplicitEngine* e, const double* u, const double* g, double* rho, cudaStream_t s) {
-    dev::k_imp_adj_rho<<<nb_(e->n4, 256), 256, 0, s>>>(e->n4, u, g, rho);
-}
-
-// One defect-correction step of the adjoint with the transposed system:
-// M^T d = rho by GMRES, then lam += relax * A .* d.  Returns the Krylov
-// iterations, -1 if a diagonal block was singular.
-int implicit_adjoint_step(ImplicitEngine* e, const StepArgs& a, const double* rho, double relax, double* lam,
-                          cudaStream_t s) {
-    int sing = 0;
-    cudaMemcpyAsync(&sing, e->singular, sizeof(int), cudaMemcpyDeviceToHost, s);
-    cudaStreamSynchronize(s);
-    if (sing) return -1;
-    const int it = gmres<double>(e, a, rho, s, 500);
-    dev::k_imp_adj_update<<<nb_(e->n4, 256), 256, 0, s>>>(e->n4, e->x, e->perm, (const double*)a.area, relax, lam);
-    e->last_iters = it;
-    return it;
 }
 
 }  // namespace afx

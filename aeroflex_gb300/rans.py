@@ -27,12 +27,15 @@ ABI_SYMBOLS = [
     "afx_solver_free", "afx_init_freestream", "afx_set_state", "afx_get_state", "afx_residual", "afx_iterate",
     "afx_run_to_convergence", "afx_residual_history", "afx_forces", "afx_set_farfield", "afx_request_stop",
     "afx_last_device_seconds", "afx_profile_iterations", "afx_kernel_name", "afx_autotune",
-    "afx_residual_noalloc", "afx_implicit_rhs", "afx_set_turbulence", "afx_get_turbulence", "afx_turbulence_residual", "afx_measure_fp64_peak", "afx_batch_create", "afx_batch_free", "afx_batch_counts", "afx_batch_init_freestream",
+    "afx_residual_noalloc", "afx_implicit_rhs", "afx_set_turbulence", "afx_get_turbulence",
+    "afx_turbulence_residual", "afx_measure_fp64_peak", "afx_newton_solve", "afx_batch_create", "afx_batch_free",
+    "afx_batch_counts", "afx_batch_init_freestream",
     "afx_batch_set_state", "afx_batch_get_state", "afx_batch_iterate", "afx_batch_run_to_convergence",
     "afx_batch_case_history", "afx_batch_forces", "afx_batch_set_farfield", "afx_batch_autotune",
     "afx_batch_last_device_seconds", "afx_residual_vjp", "afx_boundary_states", "afx_adjoint_solve",
     "afx_adjoint_state", "afx_linear_iterations", "afx_prolongate", "afx_patch_nodes", "afx_deform_patch",
-    "afx_adjoint_patch", "afx_wall_distance", "afx_mesh_set_nodes", "afx_batch_linear_iterations",
+    "afx_adjoint_patch", "afx_adjoint_patch_dirs", "afx_deform_patch_xy", "afx_adjoint_patch_dirs_xy",
+    "afx_wall_distance", "afx_mesh_set_nodes", "afx_batch_linear_iterations",
     "afx_write_vtu", "afx_save_vtu",
 ]
 N_KERNEL_KINDS = 7
@@ -123,6 +126,10 @@ def lib():
         "afx_patch_nodes": (i, [vp, cp, vp, vp, vp, i, P(i)]),
         "afx_deform_patch": (i, [vp, cp, vp, i, d]),
         "afx_adjoint_patch": (i, [vp, cp, cp, d, d, vp, i]),
+        "afx_adjoint_patch_dirs": (i, [vp, cp, cp, d, d, vp, i, i, vp]),
+        "afx_newton_solve": (i, [vp, d, i, d, d, i, P(i), P(i), P(d), vp, i]),
+        "afx_deform_patch_xy": (i, [vp, cp, vp, vp, i, d]),
+        "afx_adjoint_patch_dirs_xy": (i, [vp, cp, cp, d, d, vp, i, i, vp]),
         "afx_wall_distance": (i, [vp, vp, ll]),
         "afx_mesh_set_nodes": (i, [vp, vp, vp, ll]),
         "afx_write_vtu": (i, [vp, vp, vp, ll, d, d, cp]),
@@ -340,6 +347,20 @@ class Solver:
         _check(lib().afx_residual_history(self.h, _ptr(out), n.value, ctypes.byref(n)))
         return out
 
+    def newton_solve(self, tol=0.0, max_newton=0, cfl=0.0, lin_tol=0.0, max_krylov=0):
+        """Newton-Krylov finish of an implicit solver: (Newton steps,
+        Krylov steps, err), err = ||RHS|| / err_0; the per-step record
+        (err, step length, Krylov steps, linear residual) is kept in
+        self.newton_record."""
+        nn, nk, err = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        cap = max(int(max_newton), 20)
+        rec = np.zeros((cap, 4), np.float64)
+        _check(lib().afx_newton_solve(self.h, float(tol), int(max_newton), float(cfl), float(lin_tol),
+                                      int(max_krylov), ctypes.byref(nn), ctypes.byref(nk), ctypes.byref(err),
+                                      _ptr(rec), cap))
+        self.newton_record = rec[: min(nn.value, cap)].copy()
+        return nn.value, nk.value, err.value
+
     def set_farfield(self, patch, mach, angle, T=1.0, p=1.0):
         _check(lib().afx_set_farfield(self.h, patch.encode(), mach, angle, T, p))
 
@@ -428,6 +449,34 @@ class Solver:
         out = np.empty(n, np.float64)
         _check(lib().afx_adjoint_patch(self.h, patch.encode(), objective.encode(), float(power), float(h), _ptr(out),
                                        n))
+        return out
+
+    def adjoint_patch_dirs(self, dirs, patch="wall", objective="cl", power=2.0, h=0.0):
+        """dJ/dt along each row c of `dirs` (a = a0 + t c over the patch
+        nodes), after adjoint_solve of the same J: two residual evaluations
+        per direction."""
+        dirs = np.ascontiguousarray(np.atleast_2d(dirs), np.float64)
+        out = np.empty(dirs.shape[0], np.float64)
+        _check(lib().afx_adjoint_patch_dirs(self.h, patch.encode(), objective.encode(), float(power), float(h),
+                                            _ptr(dirs), dirs.shape[0], dirs.shape[1], _ptr(out)))
+        return out
+
+    def deform_patch_xy(self, dx, dy, patch="wall", power=2.0):
+        """Patch node k displaced by (dx[k], dy[k]), relative to the
+        undeformed mesh; the volume follows by inverse-distance weighting."""
+        dx = np.ascontiguousarray(dx, np.float64)
+        dy = np.ascontiguousarray(dy, np.float64)
+        _check(lib().afx_deform_patch_xy(self.h, patch.encode(), _ptr(dx), _ptr(dy), dx.size, float(power)))
+
+    def adjoint_patch_dirs_xy(self, dirs, patch="wall", objective="cl", power=2.0, h=0.0):
+        """dJ/dt along displacement-vector directions: dirs (n_dirs,
+        n_patch, 2), (dx_k, dy_k) per patch node."""
+        dirs = np.ascontiguousarray(dirs, np.float64)
+        if dirs.ndim == 2:
+            dirs = dirs[None]
+        out = np.empty(dirs.shape[0], np.float64)
+        _check(lib().afx_adjoint_patch_dirs_xy(self.h, patch.encode(), objective.encode(), float(power), float(h),
+                                               _ptr(dirs), dirs.shape[0], dirs.shape[1], _ptr(out)))
         return out
 
     def adjoint_state(self):

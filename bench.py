@@ -634,6 +634,228 @@ def c2_time_to_cl(budget32=150.0, budget64=330.0, sample=100):
     return out
 
 
+def c5_adjoint_coupling(n_fd_dirs=4):
+    """Config 5: adjoint sensitivities of C_L and C_D and the aeroelastic
+    coupling they drive (Euler, first order, M 0.15, AoA 10 deg).
+
+    - Config 2's full hybrid mesh (201k cells): the FP64 vJP kernel against
+      central differences of the residual (steps 1e-7 and 1e-6) along 16
+      random unit directions (seed 3) at a generic state.
+    - The config 2 generator at 8k cells: the flow to the round-off floor
+      (implicit iteration to 1e-6, then the Newton-Krylov finish), both
+      adjoints, dC_L/dalpha and the normal-displacement gradients along the
+      first ``n_fd_dirs`` of 16 random unit directions (seed 3) against
+      central differences (step 1e-7) of converged solutions, then 5
+      coupling iterations with the 50-element Euler-Bernoulli beam
+      (EI = 1e4 N m^2, clamped at the leading edge) at sea-level q_inf."""
+    import math as _m
+
+    import numpy as np
+
+    from aeroflex_gb300 import coupling, meshgen, rans
+
+    t0 = time.time()
+    mach, aoa = 0.15, 10.0 * _m.pi / 180
+    out = {"case": "config 5: Euler, first order, M 0.15, AoA 10 deg"}
+
+    def settings(solver, prec="fp64"):
+        st = rans.Settings().set("solver", solver).set("precision", prec).set("viscosity", "inviscid")
+        st.set("second_order", 0.0).set("start_cfl", 10.0 if solver == "implicit" else 1.0)
+        st.set("slope_cfl", 20.0).set("max_cfl", 200.0)
+        st.set_bc("farfield", "farfield", 1.0, mach, aoa, 1.0).set_bc("wall", "slip-wall")
+        return st
+
+    # full mesh: vJP against differences of the residual
+    m = meshgen.hybrid_airfoil()
+    M = rans.mesh.from_arrays(m)
+    g = rans.Solver(M, settings("explicit"))
+    g.init()
+    g.iterate(20)
+    rng = np.random.default_rng(3)
+    q = g.get_q()
+    q = q * (1 + 1e-3 * rng.standard_normal(q.size))
+    v = rng.standard_normal(q.size)
+    t = time.time()
+    u, _ = g.residual_vjp(v, q=q)
+    t_vjp = time.time() - t
+    errs, uncs = [], []
+    for _ in range(16):
+        e = rng.standard_normal(q.size)
+        e /= np.linalg.norm(e)
+        d = []
+        for h in (1e-7, 1e-6):
+            g.set_q(q + h * e)
+            Rp = g.residual()
+            g.set_q(q - h * e)
+            Rm = g.residual()
+            d.append(float(v @ (Rp - Rm)) / (2 * h))
+        errs.append(abs(float(u @ e) - d[0]) / abs(d[0]))
+        uncs.append(abs(d[0] - d[1]) / abs(d[0]))
+    out["vjp_full_mesh"] = {"cells": M.nRealCells, "directions": 16, "fd_step": 1e-7,
+                            "max_rel_diff_vs_fd": max(errs), "max_rel_fd_step_disagreement": max(uncs),
+                            "vjp_call_s": t_vjp}
+    del g
+
+    # reduced mesh: converged gradients and the coupling
+    ms = meshgen.hybrid_airfoil(n_surf=128, bl_layers=16, first=1e-3, growth=1.2, r_far=20.0, fill_cells=6000)
+    Ms = rans.mesh.from_arrays(ms)
+
+    def solver():
+        g = rans.Solver(Ms, settings("implicit"))
+        g.init()
+        return g
+
+    def converge(g):
+        it, _ = g.run_solver(1e-6, 2000)
+        d0 = g.last_device_seconds()
+        nn, nk, err = g.newton_solve(3e-12, 30)
+        return it, nn, nk, err, d0 + g.last_device_seconds()
+
+    g = solver()
+    it, nn, nk, err, dev = converge(g)
+    red = {"cells": Ms.nRealCells, "implicit_iterations": it, "newton_steps": nn, "krylov_steps": nk,
+           "err": err, "flow_device_s": dev}
+    D = rng.standard_normal((16, len(g.patch_nodes("wall")[0])))
+    D = D / np.linalg.norm(D, axis=1)[:, None]
+    adj = {}
+    for obj in ("cl", "cd"):
+        (da, dm), ait, ares = g.adjoint_solve("wall", obj, tol=1e-12, max_it=600)
+        adj[obj] = {"dalpha": da, "dmach": dm, "krylov_steps": ait, "residual": ares,
+                    "device_s": g.last_device_seconds(),
+                    "dirs": g.adjoint_patch_dirs(D[:n_fd_dirs], "wall", obj).tolist()}
+    fd = {"cl": [], "cd": []}
+
+    def central(deform, h):
+        vals = []
+        for sg in (1, -1):
+            deform(sg * h)
+            converge(g)
+            vals.append(rans.get_wall_profile(g))
+        return {o: (vals[0][o] - vals[1][o]) / (2 * h) for o in ("cl", "cd")}
+
+    da = central(lambda t_: g.set_farfield("farfield", mach, aoa + t_), 1e-5)
+    g.set_farfield("farfield", mach, aoa)
+    fd5 = {"cl": [], "cd": []}
+    for j in range(n_fd_dirs):
+        r = central(lambda t_: g.deform_patch(t_ * D[j], "wall"), 1e-7)
+        r5 = central(lambda t_: g.deform_patch(t_ * D[j], "wall"), 1e-5)
+        for o in ("cl", "cd"):
+            fd[o].append(r[o])
+            fd5[o].append(r5[o])
+    g.deform_patch(np.zeros(D.shape[1]), "wall")
+    converge(g)
+    red["adjoint"] = {o: {k: adj[o][k] for k in ("dalpha", "dmach", "krylov_steps", "residual", "device_s")}
+                      for o in adj}
+    red["dalpha_vs_fd"] = {o: {"adjoint": adj[o]["dalpha"], "fd_step_1e-5": da[o],
+                               "rel_diff": abs(adj[o]["dalpha"] - da[o]) / abs(da[o])} for o in ("cl", "cd")}
+    red["surface_gradient_vs_fd"] = {
+        o: {"directions": n_fd_dirs,
+            "max_rel_diff_fd_step_1e-7": max(abs(a - b) / abs(b) for a, b in zip(adj[o]["dirs"], fd[o])),
+            "max_rel_diff_fd_step_1e-5": max(abs(a - b) / abs(b) for a, b in zip(adj[o]["dirs"], fd5[o]))}
+        for o in ("cl", "cd")}
+    red["note"] = ("the converged objectives carry a round-off floor of ~5e-13 (the right-hand side's norm "
+                   "stops at ~1e-12 of its freestream value), so a central difference with step 1e-7 is "
+                   "uncertain by ~1e-4 relative; step 1e-5 brings that to ~1e-6")
+    # coupling
+    t = time.time()
+    cpl = coupling.Coupling(g, Ms, ms, coupling.Beam(50, 1e4), coupling.sea_level_dynamic_pressure(mach),
+                            tol=3e-12)
+    hist, final = cpl.run(aoa, 5)
+    keep = ("cl", "cd", "cy", "tip_deflection_m", "dcl_pred", "dcd_pred", "alpha_equivalent_deg", "step_norm_m",
+            "flow_residual", "load_N_per_m")
+    red["coupling"] = {"beam": "50 Euler-Bernoulli elements, EI 1e4 N m^2, clamped at the leading edge",
+                       "q_inf_Pa": coupling.sea_level_dynamic_pressure(mach),
+                       "history": [{k: e[k] for k in keep} for e in hist], "final": final,
+                       "wall_s": time.time() - t}
+    out["reduced"] = red
+    out["wall_s"] = time.time() - t0
+    return out
+
+
+def c5_full(iterations=5, n_fd_dirs=2):
+    """Config 5 at its stated size: config 2's hybrid mesh (201k cells),
+    Euler, first order, M 0.15, AoA 10 deg.  The primal on an FP32-mixed
+    implicit solver (its right-hand side, update and Newton finish are FP64,
+    so it converges to the FP64 solution: implicit iteration to 1e-6, then
+    the Newton-Krylov finish with its matrix at CFL 2000 to 3e-11, the
+    round-off floor there), the adjoints on an FP64 solver of the same mesh
+    (FGMRES preconditioned with the transposed matrix at CFL 2e4) from that
+    state; gradients of C_L and C_D along 16 random unit normal-displacement
+    directions (seed 3), the first ``n_fd_dirs`` against central differences
+    (step 1e-5) of converged solutions; then ``iterations`` coupling
+    iterations with the 50-element beam."""
+    import math as _m
+
+    import numpy as np
+
+    from aeroflex_gb300 import coupling, meshgen, rans
+
+    t0 = time.time()
+    mach, aoa = 0.15, 10.0 * _m.pi / 180
+
+    def solver(M, prec, max_cfl):
+        st = rans.Settings().set("solver", "implicit").set("precision", prec).set("viscosity", "inviscid")
+        st.set("second_order", 0.0).set("start_cfl", 10.0).set("slope_cfl", 20.0).set("max_cfl", max_cfl)
+        st.set_bc("farfield", "farfield", 1.0, mach, aoa, 1.0).set_bc("wall", "slip-wall")
+        g = rans.Solver(M, st)
+        g.init()
+        return g
+
+    m = meshgen.hybrid_airfoil()
+    M = rans.mesh.from_arrays(m)
+    s32 = solver(M, "fp32-mixed", 200.0)
+    s64 = solver(M, "fp64", 2e4)
+    out = {"case": "config 5 at size: hybrid mesh %d cells, Euler, first order, M 0.15, AoA 10 deg" % M.nRealCells}
+
+    def converge():
+        it, _ = s32.run_solver(1e-6, 3000)
+        d0 = s32.last_device_seconds()
+        nn, nk, err = s32.newton_solve(3e-11, 30, 2000.0)
+        s64.set_q(s32.get_q())
+        return {"implicit": it, "newton": nn, "krylov": nk, "err": err,
+                "device_s": d0 + s32.last_device_seconds()}
+
+    out["flow"] = converge()
+    ids = s64.patch_nodes("wall")[0]
+    rng = np.random.default_rng(3)
+    D = rng.standard_normal((16, len(ids)))
+    D = D / np.linalg.norm(D, axis=1)[:, None]
+    grads = {}
+    for obj in ("cl", "cd"):
+        (da, dm), it, res = s64.adjoint_solve("wall", obj, tol=1e-10, max_it=600)
+        t = time.time()
+        gd = s64.adjoint_patch_dirs(D, "wall", obj)
+        grads[obj] = gd
+        out["adjoint_" + obj] = {"dalpha": da, "dmach": dm, "krylov_steps": it, "residual": res,
+                                 "device_s": s64.last_device_seconds(), "gradient_16_dirs_s": time.time() - t}
+    fd = {"cl": [], "cd": []}
+    for j in range(n_fd_dirs):
+        vals = []
+        for sg in (1, -1):
+            for g in (s32, s64):
+                g.deform_patch(sg * 1e-5 * D[j], "wall")
+            converge()
+            vals.append(rans.get_wall_profile(s64))
+        for o in ("cl", "cd"):
+            fd[o].append((vals[0][o] - vals[1][o]) / 2e-5)
+    for g in (s32, s64):
+        g.deform_patch(np.zeros(len(ids)), "wall")
+    converge()
+    out["surface_gradient_vs_fd"] = {
+        o: [{"adjoint": float(grads[o][j]), "fd_step_1e-5": fd[o][j],
+             "rel_diff": abs(grads[o][j] - fd[o][j]) / abs(fd[o][j])} for j in range(n_fd_dirs)] for o in fd}
+    t = time.time()
+    cpl = coupling.Coupling(s64, M, m, coupling.Beam(50, 1e4), coupling.sea_level_dynamic_pressure(mach),
+                            tol=3e-11, adjoint_tol=1e-10, flow_solver=s32, newton_cfl=2000.0)
+    hist, final = cpl.run(aoa, iterations)
+    keep = ("cl", "cd", "cy", "tip_deflection_m", "dcl_pred", "dcd_pred", "alpha_equivalent_deg", "step_norm_m",
+            "flow_iterations", "flow_residual", "adjoint_cl", "adjoint_cd")
+    out["coupling"] = {"history": [{k: e[k] for k in keep} for e in hist], "final": final,
+                       "wall_s": time.time() - t}
+    out["wall_s"] = time.time() - t0
+    return out
+
+
 def cpu_baseline(budget_s=12.0):
     """The oracle (plain-C++ restatement of the reference's explicit solver:
     serial face loops, OpenMP per-cell loops as the reference) on a 512 x 256
@@ -740,6 +962,10 @@ def main():
     ap.add_argument("--no-batch-converge", action="store_true",
                     help="skip the batched polar sweep to convergence (FP32-mixed batch vs FP64 batch vs per case)")
     ap.add_argument("--no-c2", action="store_true", help="skip the config 2 (SA, hybrid mesh) time-to-C_L leg")
+    ap.add_argument("--no-c5", action="store_true", help="skip the config 5 (adjoint + coupling) leg")
+    ap.add_argument("--c5-only", action="store_true", help="run the config 5 leg alone and print it")
+    ap.add_argument("--c5-full", action="store_true",
+                    help="run config 5 at its stated size (201k cells; about 12 minutes) alone and print it")
     ap.add_argument("--nx", type=int, default=NX)
     ap.add_argument("--ny", type=int, default=NY)
     ap.add_argument("--lean", action="store_true", help="warm-up + timed iterations only (for ncu)")
@@ -765,6 +991,12 @@ def main():
     __graft_entry__.build()
     if args.lean:
         run_lean(args)
+        return
+    if args.c5_only:
+        print(json.dumps({"c5_adjoint_coupling": c5_adjoint_coupling()}))
+        return
+    if args.c5_full:
+        print(json.dumps({"c5_full": c5_full()}))
         return
     # replicas only: each rank runs the full workload on its own GPU
     if world > 1:
@@ -816,6 +1048,8 @@ def main():
         line["batch_converge"] = batch_converge()
     if not args.no_c2:
         line["c2_time_to_cl"] = c2_time_to_cl()
+    if not args.no_c5:
+        line["c5_adjoint_coupling"] = c5_adjoint_coupling()
     print(json.dumps(line))
 
 

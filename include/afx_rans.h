@@ -89,7 +89,10 @@ int afx_config_from_ini_string(const char* text, afx_config* out);
  * fp64_finish (FP32-mixed: afx_run_to_convergence continues with FP64
  * iterations once the FP32 residual stops falling, 0/1) and krylov_graph
  * (implicit solver: 1 = each GMRES solve is one CUDA graph with device-side
- * loops, 0 = the same kernels driven from a host loop, for profilers). */
+ * loops, 0 = the same kernels driven from a host loop, for profilers) and
+ * krylov_preconditioner (the flexible GMRES of afx_newton_solve and of the
+ * implicit adjoint: 1 = a GMRES solve with the implicit matrix, 0 = one
+ * ILU(0) sweep with it). */
 int afx_config_set_double(afx_config c, const char* key, double v);
 int afx_config_get_double(afx_config c, const char* key, double* v);
 /* String fields: solver ("explicit"/"implicit"), gradient ("green-gauss"/
@@ -143,6 +146,25 @@ int afx_iterate(afx_solver s, int n_iters, double* res_norm);
  * get_uniform_residual (solver.h:636-690), iterate until err <= tolerance,
  * max_iterations, or afx_request_stop.  tol/max_it <= 0 take the config's. */
 int afx_run_to_convergence(afx_solver s, double tol, int max_it, int* iters, double* err);
+/* Newton-Krylov finish of an implicit solver (not in the reference, whose
+ * implicit iteration keeps its pseudo-time term at max_cfl): inexact Newton
+ * on the implicit right-hand side (fillRhoRHS) with matrix-free
+ * Jacobian-vector products (one-sided differences of the right-hand side),
+ * flexible GMRES to lin_tol relative (<= 0: 1e-3; at most max_krylov steps
+ * per Newton step, <= 0: 300) preconditioned by the solver's own linear
+ * solve with its matrix at `cfl` (<= 0: max_cfl), backtracking on ||RHS||.
+ * Stops at err = ||RHS|| / err_0 <= tol (<= 0: the settings' tolerance;
+ * err_0 the norm of the freestream state's face fluxes, the
+ * normalisation of afx_run_to_convergence without its last-update term) or
+ * after max_newton steps (<= 0: 20).
+ * A step that finds no decrease after 8 halvings (the round-off floor of
+ * the right-hand side) ends the solve at its start; compare err with tol.
+ * record (record_cap rows of 4, may be NULL): per Newton step err after it,
+ * the step length taken (0: none), its Krylov steps, the relative linear
+ * residual reached.  Start it from a state the implicit iteration has
+ * brought near the solution.  Not for Spalart-Allmaras solvers or batches. */
+int afx_newton_solve(afx_solver s, double tol, int max_newton, double cfl, double lin_tol, int max_krylov,
+                     int* newton_iters, int* krylov_iters, double* err, double* record, int record_cap);
 /* Residual history as run_solver stores it (every 10th iteration). */
 int afx_residual_history(afx_solver s, double* out, int cap, int* n);
 /* get_wall_profile(solver&, patch) (src/rans/include/rans/post.h:301-387):
@@ -259,10 +281,12 @@ int afx_boundary_states(afx_solver s, double* bq, long long n);
  * (dR/dq)^T lam = -(dJ/dq)^T until ||(dR/dq)^T lam + dJ/dq|| falls below
  * tol * ||dJ/dq|| (tol <= 0: 1e-10) or max_it iterations (<= 0: 100000).
  * An explicit solver iterates in pseudo-time with its own local time step
- * and three stages.  An implicit solver runs its own implicit iteration
- * transposed: the matrix at max_cfl and the converged state, transposed
- * with its ILU(0) factors, GMRES for M^T d = dJ/dq + (dR/dq)^T lam, then
- * lam += relaxation * A d (iterations = these steps).  dJ[0] = dJ/d(angle) per radian of the farfield angle,
+ * and three stages.  An implicit solver solves it by flexible GMRES
+ * (restarts every 60 steps) on the exact transposed Jacobian (the vJP),
+ * preconditioned by its own linear solve with its matrix at max_cfl and the
+ * converged state, transposed with its ILU(0) factors (M^T d = v, then
+ * -A .* d); iterations = Krylov steps, and the solve starts from the last
+ * solution of the same objective on this solver.  dJ[0] = dJ/d(angle) per radian of the farfield angle,
  * dJ[1] = dJ/d(Mach), both for every farfield-type boundary together.
  * iters, res: iterations run and the final relative adjoint residual. */
 int afx_adjoint_solve(afx_solver s, const char* patch, const char* objective, double tol, int max_it, double* dJ,
@@ -289,6 +313,22 @@ int afx_deform_patch(afx_solver s, const char* patch, const double* a, int n, do
  * (h <= 0: 1e-7), no re-convergence.  FP64 solvers. */
 int afx_adjoint_patch(afx_solver s, const char* patch, const char* objective, double power, double h, double* dJ,
                       int n);
+/* The same derivative along n_dirs directions at once: dJ[j] = dJ/dt of
+ * a = a0 + t * dirs[j*n_patch .. (j+1)*n_patch), each by one central
+ * difference (two residual evaluations per direction, not per node).  A
+ * structural model with fewer degrees of freedom than patch nodes takes its
+ * gradient this way (the directions are its modes' surface displacements).
+ * n_patch must equal the number of patch nodes. */
+int afx_adjoint_patch_dirs(afx_solver s, const char* patch, const char* objective, double power, double h,
+                           const double* dirs, int n_dirs, int n_patch, double* dJ);
+/* Displacement vectors instead of normal displacements: patch node k moves
+ * by (dx[k], dy[k]), the volume by the same inverse-distance weights (a
+ * structural model moving the wall along its own axes, e.g. a beam's
+ * deflection), and the adjoint derivative along such directions, each row
+ * of dirs holding (dx_k, dy_k) for every patch node (2 n_patch entries). */
+int afx_deform_patch_xy(afx_solver s, const char* patch, const double* dx, const double* dy, int n, double power);
+int afx_adjoint_patch_dirs_xy(afx_solver s, const char* patch, const char* objective, double power, double h,
+                              const double* dirs, int n_dirs, int n_patch, double* dJ);
 
 /* ---- Batched load cases.  No single counterpart in the reference: its
  * polar sweep runs one case after another (src/rans/include/rans/rans.h:
