@@ -781,9 +781,16 @@ def c5_full(iterations=5, n_fd_dirs=2):
     round-off floor there), the adjoints on an FP64 solver of the same mesh
     (FGMRES preconditioned with the transposed matrix at CFL 2e4) from that
     state; gradients of C_L and C_D along 16 random unit normal-displacement
-    directions (seed 3), the first ``n_fd_dirs`` against central differences
-    (step 1e-5) of converged solutions; then ``iterations`` coupling
-    iterations with the 50-element beam."""
+    directions (seed 3).  Central differences of converged solutions check
+    them two ways: along the first ``n_fd_dirs`` random directions with
+    step 1e-5 (the largest that leaves the boundary layer's first cells,
+    1e-6 chord high, uninverted under node-to-node random displacements; the
+    residual's round-off floor, ~1e-11 of its freestream value, is then
+    reached after about two orders of reduction of what the step perturbs,
+    so this difference is short by up to ~1e-2), and along two smooth
+    vertical-displacement directions (random sine series over the chord,
+    unit norm) with steps 1e-3 and 3e-4, where it is accurate; then
+    ``iterations`` coupling iterations with the 50-element beam."""
     import math as _m
 
     import numpy as np
@@ -820,30 +827,47 @@ def c5_full(iterations=5, n_fd_dirs=2):
     rng = np.random.default_rng(3)
     D = rng.standard_normal((16, len(ids)))
     D = D / np.linalg.norm(D, axis=1)[:, None]
-    grads = {}
+    xk = m["x"][ids]
+    S = np.zeros((2, len(ids), 2))
+    for j in range(2):
+        c = rng.standard_normal(6)
+        S[j, :, 1] = sum(c[k] * np.sin((k + 1) * np.pi * xk) for k in range(6))
+        S[j] /= np.linalg.norm(S[j])
+    grads, gsm = {}, {}
     for obj in ("cl", "cd"):
         (da, dm), it, res = s64.adjoint_solve("wall", obj, tol=1e-10, max_it=600)
         t = time.time()
-        gd = s64.adjoint_patch_dirs(D, "wall", obj)
-        grads[obj] = gd
+        grads[obj] = s64.adjoint_patch_dirs(D, "wall", obj)
+        t_dirs = time.time() - t
+        gsm[obj] = s64.adjoint_patch_dirs_xy(S, "wall", obj)
         out["adjoint_" + obj] = {"dalpha": da, "dmach": dm, "krylov_steps": it, "residual": res,
-                                 "device_s": s64.last_device_seconds(), "gradient_16_dirs_s": time.time() - t}
-    fd = {"cl": [], "cd": []}
-    for j in range(n_fd_dirs):
+                                 "device_s": s64.last_device_seconds(), "gradient_16_dirs_s": t_dirs}
+
+    def central(deform, h):
         vals = []
         for sg in (1, -1):
             for g in (s32, s64):
-                g.deform_patch(sg * 1e-5 * D[j], "wall")
+                deform(g, sg * h)
             converge()
             vals.append(rans.get_wall_profile(s64))
-        for o in ("cl", "cd"):
-            fd[o].append((vals[0][o] - vals[1][o]) / 2e-5)
+        return {o: (vals[0][o] - vals[1][o]) / (2 * h) for o in ("cl", "cd")}
+
+    rnd = []
+    for j in range(n_fd_dirs):
+        r = central(lambda g, t_: g.deform_patch(t_ * D[j], "wall"), 1e-5)
+        rnd.append({o: {"adjoint": float(grads[o][j]), "fd_step_1e-5": r[o],
+                        "rel_diff": abs(grads[o][j] - r[o]) / abs(r[o])} for o in r})
+    smooth = []
+    for j in range(2):
+        r3 = central(lambda g, t_: g.deform_patch_xy(0 * S[j, :, 0], t_ * S[j, :, 1], "wall"), 1e-3)
+        r4 = central(lambda g, t_: g.deform_patch_xy(0 * S[j, :, 0], t_ * S[j, :, 1], "wall"), 3e-4)
+        smooth.append({o: {"adjoint": float(gsm[o][j]), "fd_step_1e-3": r3[o], "fd_step_3e-4": r4[o],
+                           "rel_diff_vs_fd_3e-4": abs(gsm[o][j] - r4[o]) / abs(r4[o]),
+                           "rel_fd_step_disagreement": abs(r3[o] - r4[o]) / abs(r4[o])} for o in r3})
     for g in (s32, s64):
         g.deform_patch(np.zeros(len(ids)), "wall")
     converge()
-    out["surface_gradient_vs_fd"] = {
-        o: [{"adjoint": float(grads[o][j]), "fd_step_1e-5": fd[o][j],
-             "rel_diff": abs(grads[o][j] - fd[o][j]) / abs(fd[o][j])} for j in range(n_fd_dirs)] for o in fd}
+    out["gradient_vs_fd"] = {"random_normal_directions": rnd, "smooth_vertical_directions": smooth}
     t = time.time()
     cpl = coupling.Coupling(s64, M, m, coupling.Beam(50, 1e4), coupling.sea_level_dynamic_pressure(mach),
                             tol=3e-11, adjoint_tol=1e-10, flow_solver=s32, newton_cfl=2000.0)

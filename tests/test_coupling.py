@@ -12,8 +12,9 @@ aeroelastic coupling they drive (aeroflex_gb300/coupling.py).
   differences of converged solutions (steps 2e-5 and 1e-5: at the
   converged objectives' round-off floor, ~5e-13, a step of 1e-7 leaves
   the difference uncertain by ~1e-4 relative), 1e-6 relative plus the two
-  steps' disagreement; then 5 coupling iterations with the 50-element beam
-  (EI = 1e4 N m^2) at sea-level dynamic pressure.
+  steps' disagreement taken twice (the disagreement is itself a noisy
+  estimate of the difference's error); then 5 coupling iterations with the
+  50-element beam (EI = 1e4 N m^2) at sea-level dynamic pressure.
 - GPU, config 2's full 201k-cell mesh: the vJP kernel against central
   differences (step 1e-7) along 16 random unit directions (seed 3).
 """
@@ -154,12 +155,12 @@ def test_config5_gradients_match_converged_differences(afx):
     angle(0.0)
     for obj in ("cl", "cd"):
         ref, unc = fd[obj]
-        assert abs(dalpha[obj] - ref) <= 1e-6 * abs(ref) + unc + 1e-9, (obj, dalpha[obj], ref, unc)
+        assert abs(dalpha[obj] - ref) <= 1e-6 * abs(ref) + 2 * unc + 1e-9, (obj, dalpha[obj], ref, unc)
     for j in range(16):
         fd = _fd(afx, g, lambda t: g.deform_patch(t * D[j], "wall"), ("cl", "cd"), steps=(2e-5, 1e-5))
         for obj in ("cl", "cd"):
             ref, unc = fd[obj]
-            assert abs(grad[obj][j] - ref) <= 1e-6 * abs(ref) + unc + 1e-9, (j, obj, grad[obj][j], ref, unc)
+            assert abs(grad[obj][j] - ref) <= 1e-6 * abs(ref) + 2 * unc + 1e-9, (j, obj, grad[obj][j], ref, unc)
 
 
 @pytest.mark.gpu
