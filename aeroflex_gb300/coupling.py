@@ -6,7 +6,7 @@ airfoil section with the adjoint gradients driving the update.
 
 - Beam: Euler-Bernoulli elements along the chord, two degrees of freedom
   per node (deflection w, slope dw/dx): the bending block of the structure
-  module's bar element (element.hpp:81-98: 12EI/L^3, 6EI/L^2, 4EI/L,
+  module's bar element (element.hpp:77-110: 12EI/L^3, 6EI/L^2, 4EI/L,
   2EI/L), assembled as MODEL::set_K_global does, clamped as
   set_K_Final_sparse does (constrained rows and columns zeroed, unit
   diagonal, load zeroed), loaded through set_load_vector_from_vector

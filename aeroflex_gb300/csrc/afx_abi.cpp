@@ -262,8 +262,10 @@ struct afx_solver_s {
     struct AdjointBufs {
         DevBuf v, fbar, gbx, gby, qbar, lw, lt, u, bqbar, g, q, lam[2], ls[2], partials;
         DevBuf lam_obj[2];  // the last implicit adjoint solution of C_L / C_D (initial guess of the next)
+        int dirs = 4;       // input directions per pass of the face kernel
         AdjArgs args(const void* v_dev, void* u_dev) const {
             AdjArgs j;
+            j.dirs_per_pass = dirs;
             j.v = v_dev;
             j.fbar = fbar.p;
             j.gbx = gbx.p;
@@ -296,6 +298,7 @@ struct afx_solver_s {
         if (!adj) {
             const size_t N = a.n_cells, F = a.n_faces, B = std::max(a.n_bnd, 1);
             auto b = std::make_unique<AdjointBufs>();
+            b->dirs = st.adjoint_directions;
             for (DevBuf* d : {&b->v, &b->gbx, &b->gby, &b->qbar, &b->u, &b->g, &b->q, &b->lam[0], &b->lam[1],
                               &b->ls[0], &b->ls[1]})
                 d->alloc(N * 32);
@@ -949,6 +952,9 @@ int afx_config_set_double(afx_config c, const char* key, double v) {
         } else if (k == "krylov_preconditioner") {
             if (v != 0 && v != 1) throw Error(AFX_ERR_CONFIG, "krylov_preconditioner must be 0 or 1");
             c->s.krylov_preconditioner = (int)v;
+        } else if (k == "adjoint_directions") {
+            if (v != 1 && v != 2 && v != 4) throw Error(AFX_ERR_CONFIG, "adjoint_directions must be 1, 2 or 4");
+            c->s.adjoint_directions = (int)v;
         }
         else if (k == "second_order") c->s.second_order = v != 0;
         else if (double* p = dfield(c->s, k)) *p = v;
@@ -967,6 +973,7 @@ int afx_config_get_double(afx_config c, const char* key, double* v) {
         else if (k == "fp64_finish") *v = c->s.fp64_finish ? 1 : 0;
         else if (k == "krylov_graph") *v = c->s.krylov_graph ? 1 : 0;
         else if (k == "krylov_preconditioner") *v = c->s.krylov_preconditioner;
+        else if (k == "adjoint_directions") *v = c->s.adjoint_directions;
         else if (k == "second_order") *v = c->s.second_order ? 1 : 0;
         else if (double* p = dfield(c->s, k)) *v = *p;
         else throw Error(AFX_ERR_ARG, "unknown numeric setting '" + k + "'");
@@ -1545,13 +1552,17 @@ int afx_iterate(afx_solver s, int n_iters, double* res_norm) {
 // one-sided difference of the right-hand side (step 1e-7 of the state's
 // RMS over the direction's), each solved by flexible GMRES to lin_tol
 // relative, preconditioned by the solver's own linear solve with its matrix
-// at `cfl` (A/dt + the face Jacobians, formed at the Newton iterate).  Each
-// step is backtracked (halved up to 8 times) until ||RHS|| falls; a step
-// that finds no decrease (the round-off floor of the right-hand side) ends
-// the solve at the step's start.  err is ||RHS|| / err_0, err_0 the norm of
-// the freestream state's face fluxes.  record (cap rows of 4, may be null):
-// per Newton step err after it, the step length, its Krylov steps and the
-// linear residual reached.
+// at `cfl` (A/dt + the face Jacobians, formed at the Newton iterate).
+// Rows are scaled by the cell's perimeter: the unscaled norm is dominated
+// by the far field's large faces (and by their round-off, ~1e-11 of the
+// freestream norm on a 100-chord hybrid mesh) while the wall's thin cells,
+// which set the forces, hardly count; per unit face length every cell
+// weighs alike.  Each step is backtracked (halved up to 8 times) until the
+// scaled norm falls; a step that finds no decrease (the round-off floor)
+// ends the solve at the step's start.  err is ||RHS / perimeter|| over the
+// same norm of the freestream state's face fluxes.  record (cap rows of 4,
+// may be null): per Newton step err after it, the step length, its Krylov
+// steps and the linear residual reached.
 static double newton_run(afx_solver_s* s, double tol, int max_newton, double cfl, double lin_tol, int max_krylov,
                          int* n_newton, int* n_krylov, double* record, int cap) {
     if (!s->imp) throw Error(AFX_ERR_CONFIG, "newton: needs an implicit solver");
@@ -1563,29 +1574,54 @@ static double newton_run(afx_solver_s* s, double tol, int max_newton, double cfl
     StepArgs A = s->A64();
     if (A.ctrl != s->a.ctrl) AFX_CUDA(cudaMemsetAsync(A.ctrl, 0, sizeof(Ctrl), s->stream));
     const int p = s->parity;
+    const size_t N = A.n_cells;
+    const long long n4 = 4LL * (long long)N;
+    KrylovSpace ks(n4, 60);
+    DevBuf q0, b, rp, pc, dq, wsc, psc, tmp;
+    for (DevBuf* d : {&q0, &b, &rp, &pc, &dq, &wsc, &psc, &tmp}) d->alloc(N * 32);
+    {
+        // row scales: 1 / perimeter and perimeter per device cell, 4 rows each
+        const HostMesh& hm = s->hm;
+        std::vector<double> per(hm.nRealCells, 0.0);
+        for (size_t e = 0; e < hm.edgesCells.size(); ++e)
+            for (int k = 0; k < 2; ++k) {
+                const uint32_t c = hm.edgesCells[e][k];
+                if (c < hm.nRealCells) per[c] += hm.edgesLengths[e];
+            }
+        std::vector<double> w(4 * N), pv(4 * N);
+        for (size_t i = 0; i < N; ++i)
+            for (int k = 0; k < 4; ++k) {
+                pv[4 * i + k] = per[s->hl.cell_old[i]];
+                w[4 * i + k] = 1.0 / pv[4 * i + k];
+            }
+        AFX_CUDA(cudaMemcpyAsync(wsc.p, w.data(), N * 32, cudaMemcpyHostToDevice, s->stream));
+        AFX_CUDA(cudaMemcpyAsync(psc.p, pv.data(), N * 32, cudaMemcpyHostToDevice, s->stream));
+        AFX_CUDA(cudaStreamSynchronize(s->stream));
+    }
+    const double* W = (const double*)wsc.p;
+    const double* Pm = (const double*)psc.p;
+    // ||RHS / perimeter|| of a right-hand side v
+    auto scaled_norm = [&](const void* v) {
+        kv_mul(ks, W, (const double*)v, (double*)tmp.p, s->stream);
+        return std::sqrt(kv_dot(ks, (const double*)tmp.p, (const double*)tmp.p, s->stream));
+    };
     double err0 = 1.0;
     {
-        // the freestream fluxes alone (qW, which run_solver adds, cleared)
+        // the freestream state's face fluxes (qW, which run_solver adds, cleared)
         double qf[4];
         conservative(s->st, s->freestream(), qf);
         AFX_CUDA(cudaMemsetAsync(A.Rq, 0, (size_t)A.n_cells * 32, s->stream));
         enqueue_uniform_f64(A, p, qf, s->stream);
-        Ctrl c;
-        AFX_CUDA(cudaMemcpyAsync(&c, A.ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, s->stream));
-        AFX_CUDA(cudaStreamSynchronize(s->stream));
-        err0 = c.err0 > 0 ? c.err0 : 1.0;
+        const double e0 = scaled_norm(A.Rq);
+        err0 = e0 > 0 ? e0 : 1.0;
     }
-    const size_t N = A.n_cells;
-    const long long n4 = 4LL * (long long)N;
-    KrylovSpace ks(n4, 60);
-    DevBuf q0, b, rp, pc, dq;
-    for (DevBuf* d : {&q0, &b, &rp, &pc, &dq}) d->alloc(N * 32);
     double* qm = (double*)A.qm[p];
     StepArgs r = A;
     r.Rq = rp.p;  // right-hand sides of perturbed states
     int nn = 0, nk = 0;
     AFX_CUDA(cudaEventRecord(s->ev0, s->stream));
-    double e = s->imp_rhs(p);
+    s->imp_rhs(p);
+    double e = scaled_norm(s->imp_b);
     try {
         while (e / err0 > tol && nn < max_newton) {
             if (!(e == e)) throw Error(AFX_ERR_NONFINITE, "newton: residual norm is not finite");
@@ -1593,7 +1629,8 @@ static double newton_run(afx_solver_s* s, double tol, int max_newton, double cfl
             m.cfl = cfl;
             implicit_fill(s->imp, m, p, s->stream);
             AFX_CUDA(cudaMemcpyAsync(q0.p, qm, N * 32, cudaMemcpyDeviceToDevice, s->stream));
-            AFX_CUDA(cudaMemcpyAsync(b.p, s->imp_b, N * 32, cudaMemcpyDeviceToDevice, s->stream));
+            // the scaled system (W J) dq = W RHS, W = 1 / perimeter
+            kv_mul(ks, W, (const double*)s->imp_b, (double*)b.p, s->stream);
             const double qrms = std::sqrt(kv_dot(ks, (const double*)q0.p, (const double*)q0.p, s->stream) / n4);
             const KrylovOp op = [&](const double* v, double* out) {
                 const double vrms = std::sqrt(kv_dot(ks, v, v, s->stream) / n4);
@@ -1604,10 +1641,11 @@ static double newton_run(afx_solver_s* s, double tol, int max_newton, double cfl
                 const double eps = 1e-7 * std::max(1.0, qrms) / vrms;
                 kv_axpby(ks, eps, v, 1.0, (const double*)q0.p, qm, s->stream);
                 enqueue_rhs_f64(r, p, s->stream);
+                kv_mul(ks, W, (const double*)rp.p, (double*)rp.p, s->stream);
                 kv_axpby(ks, -1.0 / eps, (const double*)rp.p, 1.0 / eps, (const double*)b.p, out, s->stream);
             };
             const KrylovOp pre = [&](const double* v, double* out) {
-                AFX_CUDA(cudaMemcpyAsync(pc.p, v, N * 32, cudaMemcpyDeviceToDevice, s->stream));
+                kv_mul(ks, Pm, v, (double*)pc.p, s->stream);  // M^-1 (perimeter .* v)
                 const int rc = s->st.krylov_preconditioner == 1
                                    ? implicit_apply_inverse(s->imp, A, (const double*)pc.p, nullptr, 1.0, out, s->stream)
                                    : implicit_apply_sweep(s->imp, A, (const double*)pc.p, nullptr, 1.0, out, s->stream);
@@ -1620,11 +1658,13 @@ static double newton_run(afx_solver_s* s, double tol, int max_newton, double cfl
             bool stalled = false;
             for (int ls = 0;; ++ls) {
                 kv_axpby(ks, lam, (const double*)dq.p, 1.0, (const double*)q0.p, qm, s->stream);
-                en = s->imp_rhs(p);
+                s->imp_rhs(p);
+                en = scaled_norm(s->imp_b);
                 if (en == en && en < e) break;
                 if (ls == 8) {
                     AFX_CUDA(cudaMemcpyAsync(qm, q0.p, N * 32, cudaMemcpyDeviceToDevice, s->stream));
-                    en = s->imp_rhs(p);
+                    s->imp_rhs(p);
+                    en = scaled_norm(s->imp_b);
                     stalled = true;
                     break;
                 }
@@ -1645,6 +1685,9 @@ static double newton_run(afx_solver_s* s, double tol, int max_newton, double cfl
         s->imp_sync();
         throw;
     }
+    // qW (the implicit iteration's last update, which run_solver's err_0
+    // adds to the freestream fluxes) is left at zero
+    AFX_CUDA(cudaMemsetAsync(A.Rq, 0, (size_t)A.n_cells * 32, s->stream));
     AFX_CUDA(cudaEventRecord(s->ev1, s->stream));
     AFX_CUDA(cudaEventSynchronize(s->ev1));
     float ms = 0;

@@ -6,8 +6,10 @@
 // Reverse sweep in three gather kernels, deterministic and atomic-free:
 //   k_adj_face   per face: the face flux's local Jacobians are formed on the
 //                fly by forward-mode dual numbers (8 directions: left state,
-//                right state or boundary state) and contracted with the face
-//                weight L*(v_c1/A_c1 - v_c0/A_c0) -> 8 numbers per face.
+//                right state or boundary state; 1, 2 or 4 of them per pass
+//                as vector duals, which share the value's work) and contracted
+//                with the face weight L*(v_c1/A_c1 - v_c0/A_c0) -> 8 numbers
+//                per face.
 //   k_adj_cell   per cell: gathers its faces' numbers into the state,
 //                limiter and gradient adjoints of the reconstruction
 //                q + phi .* (grad q . d), then reverses its limiter (active
@@ -30,37 +32,49 @@ constexpr int ADJ_NONE = (int)0x80000000;  // limiter target: none / the cell it
 
 __device__ __forceinline__ int pick4(const int4 v, const int k) { return pick(v, k); }
 
-// sum_m dF_m/d(dir) * w_m of the face flux, for input direction `dir`
-// (0-3: left state, 4-7: right state, or the boundary state when one-sided;
-// with the laminar term, 8-11 / 12-15: the face gradient's x / y parts)
-template <int VISC>
-__device__ __forceinline__ double face_flux_dir(const KM<double>& m, const int bt, const double nx, const double ny,
-                                                const double* qL, const double* qR, const double* fgx,
-                                                const double* fgy, const int dir, const double* w) {
-    Dual dL[4], dR[4], F[4];
+// out[j] = sum_m dF_m/d(dir0 + j) * w_m of the face flux, j < K, for input
+// directions dir0 .. dir0+K-1 (0-3: left state, 4-7: right state, or the
+// boundary state when one-sided; with the laminar term, 8-11 / 12-15: the
+// face gradient's x / y parts), all K in one pass of vector duals
+template <int VISC, int K>
+__device__ __forceinline__ void face_flux_dirs(const KM<double>& m, const int bt, const double nx, const double ny,
+                                               const double* qL, const double* qR, const double* fgx,
+                                               const double* fgy, const int dir0, const double* w, double* out) {
+    using D = DualV<K>;
+    D dL[4], dR[4], F[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        dL[k] = Dual(qL[k], dir == k ? 1.0 : 0.0);
-        dR[k] = Dual(qR[k], dir == k + 4 ? 1.0 : 0.0);
+        dL[k] = D(qL[k]);
+        dR[k] = D(qR[k]);
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+            dL[k].d[j] = dir0 + j == k ? 1.0 : 0.0;
+            dR[k].d[j] = dir0 + j == k + 4 ? 1.0 : 0.0;
+        }
     }
     if (two_sided(bt)) {
-        roe_flux<Dual>(Dual(m.gamma), Dual(nx), Dual(ny), dL, dR, F);
+        roe_flux<D>(D(m.gamma), D(nx), D(ny), dL, dR, F);
         if (VISC == 1) {
-            Dual gxd[4], gyd[4];
+            D gxd[4], gyd[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                gxd[k] = Dual(fgx[k], dir == k + 8 ? 1.0 : 0.0);
-                gyd[k] = Dual(fgy[k], dir == k + 12 ? 1.0 : 0.0);
+                gxd[k] = D(fgx[k]);
+                gyd[k] = D(fgy[k]);
+#pragma unroll
+                for (int j = 0; j < K; ++j) {
+                    gxd[k].d[j] = dir0 + j == k + 8 ? 1.0 : 0.0;
+                    gyd[k].d[j] = dir0 + j == k + 12 ? 1.0 : 0.0;
+                }
             }
-            laminar_flux<Dual>(Dual(m.gamma), Dual(m.R), Dual(m.mu), Dual(m.kheat), Dual(nx), Dual(ny), dL, dR,
-                               gxd, gyd, F);
+            laminar_flux<D>(D(m.gamma), D(m.R), D(m.mu), D(m.kheat), D(nx), D(ny), dL, dR, gxd, gyd, F);
         }
     } else {
-        Dual qb[4];
-        ghost_state<Dual>(bt, Dual(m.gamma), Dual(nx), Dual(ny), dL, dR, qb);
-        roe_flux<Dual>(Dual(m.gamma), Dual(nx), Dual(ny), dL, qb, F);
+        D qb[4];
+        ghost_state<D>(bt, D(m.gamma), D(nx), D(ny), dL, dR, qb);
+        roe_flux<D>(D(m.gamma), D(nx), D(ny), dL, qb, F);
     }
-    return F[0].d * w[0] + F[1].d * w[1] + F[2].d * w[2] + F[3].d * w[3];
+#pragma unroll
+    for (int j = 0; j < K; ++j) out[j] = F[0].d[j] * w[0] + F[1].d[j] * w[1] + F[2].d[j] * w[2] + F[3].d[j] * w[3];
 }
 
 // sum_m d ghost_m/d(dir) * w_m (dir 0-3: interior state, 4-7: boundary state)
@@ -80,7 +94,7 @@ __device__ __forceinline__ double ghost_dir(const int bt, const double gamma, co
 // [qL_bar, qR_bar (or the boundary state's), and with the laminar term
 //  gxa_bar, gya_bar, qa_bar, gxb_bar, gyb_bar, qb_bar] -- a/b: the face's
 // cells as the face gradient sees them (solver.h:359-398)
-template <bool SECOND, int VISC>
+template <bool SECOND, int VISC, int ADJ_K>
 __global__ void __launch_bounds__(128) k_adj_face(const KM<double> m, const int n_faces, const d4* __restrict__ q,
                                                   const d4* __restrict__ gx, const d4* __restrict__ gy,
                                                   const d4* __restrict__ phi, const d4* __restrict__ v,
@@ -153,8 +167,17 @@ __global__ void __launch_bounds__(128) k_adj_face(const KM<double> m, const int 
     constexpr int ND = VISC == 1 ? 16 : 8;
     double out[ND];
 #pragma unroll 1
-    for (int dir = 0; dir < ND; ++dir)
-        out[dir] = (dir < 8 || lam) ? face_flux_dir<VISC>(m, bt, n.x, n.y, qL, qR, fgx, fgy, dir, w) : 0.0;
+    for (int dir = 0; dir < ND; dir += ADJ_K) {
+        if (dir < 8 || lam) {
+            double o[ADJ_K];
+            face_flux_dirs<VISC, ADJ_K>(m, bt, n.x, n.y, qL, qR, fgx, fgy, dir, w, o);
+#pragma unroll
+            for (int j = 0; j < ADJ_K; ++j) out[dir + j] = o[j];
+        } else {
+#pragma unroll
+            for (int j = 0; j < ADJ_K; ++j) out[dir + j] = 0.0;
+        }
+    }
     d4* fb = fbar + (size_t)FB * f;
     st4(&fb[0], out);
     st4(&fb[1], out + 4);
@@ -507,7 +530,13 @@ void vjp_launch(const StepArgs& a, int p, const AdjArgs& j, cudaStream_t s) {
     const d4* ph = (const d4*)a.phi;
     const int B = 128;
     const int nf = nblocks(a.n_faces, B), nc = nblocks(a.n_cells, B);
-    k_adj_face<SECOND, VISC><<<nf, B, 0, s>>>(m, a.n_faces, q, gx, gy, ph, (const d4*)j.v, (d4*)j.fbar);
+    // input directions per pass of the face kernel (vector duals)
+    if (j.dirs_per_pass == 1)
+        k_adj_face<SECOND, VISC, 1><<<nf, B, 0, s>>>(m, a.n_faces, q, gx, gy, ph, (const d4*)j.v, (d4*)j.fbar);
+    else if (j.dirs_per_pass == 2)
+        k_adj_face<SECOND, VISC, 2><<<nf, B, 0, s>>>(m, a.n_faces, q, gx, gy, ph, (const d4*)j.v, (d4*)j.fbar);
+    else
+        k_adj_face<SECOND, VISC, 4><<<nf, B, 0, s>>>(m, a.n_faces, q, gx, gy, ph, (const d4*)j.v, (d4*)j.fbar);
     k_adj_cell<SECOND, VISC><<<nc, B, 0, s>>>(m, q, gx, gy, ph, (const d4*)j.fbar, (d4*)j.qbar, (d4*)j.gbx,
                                               (d4*)j.gby, (d4*)j.lw, (int4*)j.lt);
     k_adj_final<SECOND, VISC><<<nc, B, 0, s>>>(m, q, (const d4*)j.fbar, (const d4*)j.qbar, (const d4*)j.gbx,

@@ -44,5 +44,68 @@ __device__ __forceinline__ Dual dsqrt(Dual x) {
 }
 __device__ __forceinline__ Dual dabs(Dual x) { return x.v < 0 ? -x : x; }
 
+// K directions in lockstep: one value and K derivatives, each derivative
+// formed by exactly the operations Dual uses, so direction j of a DualV is
+// bit for bit the Dual of direction j -- the value's work is shared.
+template <int K>
+struct DualV {
+    double v, d[K];
+    __device__ __forceinline__ DualV() : v(0) {
+#pragma unroll
+        for (int j = 0; j < K; ++j) d[j] = 0;
+    }
+    __device__ __forceinline__ DualV(double x) : v(x) {
+#pragma unroll
+        for (int j = 0; j < K; ++j) d[j] = 0;
+    }
+};
+
+template <int K> __device__ __forceinline__ DualV<K> operator+(DualV<K> a, DualV<K> b) {
+    DualV<K> r(a.v + b.v);
+#pragma unroll
+    for (int j = 0; j < K; ++j) r.d[j] = a.d[j] + b.d[j];
+    return r;
+}
+template <int K> __device__ __forceinline__ DualV<K> operator-(DualV<K> a, DualV<K> b) {
+    DualV<K> r(a.v - b.v);
+#pragma unroll
+    for (int j = 0; j < K; ++j) r.d[j] = a.d[j] - b.d[j];
+    return r;
+}
+template <int K> __device__ __forceinline__ DualV<K> operator-(DualV<K> a) {
+    DualV<K> r(-a.v);
+#pragma unroll
+    for (int j = 0; j < K; ++j) r.d[j] = -a.d[j];
+    return r;
+}
+template <int K> __device__ __forceinline__ DualV<K> operator*(DualV<K> a, DualV<K> b) {
+    DualV<K> r(a.v * b.v);
+#pragma unroll
+    for (int j = 0; j < K; ++j) r.d[j] = a.d[j] * b.v + a.v * b.d[j];
+    return r;
+}
+template <int K> __device__ __forceinline__ DualV<K> operator/(DualV<K> a, DualV<K> b) {
+    const double q = a.v / b.v;
+    DualV<K> r(q);
+#pragma unroll
+    for (int j = 0; j < K; ++j) r.d[j] = (a.d[j] - q * b.d[j]) / b.v;
+    return r;
+}
+template <int K> __device__ __forceinline__ DualV<K>& operator+=(DualV<K>& a, DualV<K> b) { return a = a + b; }
+template <int K> __device__ __forceinline__ DualV<K>& operator-=(DualV<K>& a, DualV<K> b) { return a = a - b; }
+template <int K> __device__ __forceinline__ DualV<K>& operator*=(DualV<K>& a, DualV<K> b) { return a = a * b; }
+template <int K> __device__ __forceinline__ bool operator<(DualV<K> a, DualV<K> b) { return a.v < b.v; }
+template <int K> __device__ __forceinline__ bool operator>(DualV<K> a, DualV<K> b) { return a.v > b.v; }
+template <int K> __device__ __forceinline__ bool operator<=(DualV<K> a, DualV<K> b) { return a.v <= b.v; }
+template <int K> __device__ __forceinline__ bool operator>=(DualV<K> a, DualV<K> b) { return a.v >= b.v; }
+template <int K> __device__ __forceinline__ DualV<K> dsqrt(DualV<K> x) {
+    const double s = sqrt(x.v);
+    DualV<K> r(s);
+#pragma unroll
+    for (int j = 0; j < K; ++j) r.d[j] = x.d[j] / (2.0 * s);
+    return r;
+}
+template <int K> __device__ __forceinline__ DualV<K> dabs(DualV<K> x) { return x.v < 0 ? -x : x; }
+
 }  // namespace dev
 }  // namespace afx

@@ -64,6 +64,8 @@ struct Settings {
     // preconditioner of the Newton finish and of the implicit adjoint's
     // flexible GMRES: 0 one ILU(0) sweep, 1 a GMRES solve with the matrix
     int krylov_preconditioner = 1;
+    // input directions per vector-dual pass of the adjoint's face kernel
+    int adjoint_directions = 4;
 
     int viscosity_code() const;
     static int bc_code(const std::string& t);

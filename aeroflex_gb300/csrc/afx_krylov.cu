@@ -67,6 +67,12 @@ __global__ void __launch_bounds__(KV_T) k_kv_sub(const long long n, const int k,
     }
 }
 
+// out = x .* y (out may alias either)
+__global__ void __launch_bounds__(KV_T) k_kv_mul(const long long n, const double* x, const double* y, double* out) {
+    for (long long j = (long long)blockIdx.x * KV_T + threadIdx.x; j < n; j += (long long)gridDim.x * KV_T)
+        out[j] = x[j] * y[j];
+}
+
 // out = a x + b y (out may alias y)
 __global__ void __launch_bounds__(KV_T) k_kv_axpby(const long long n, const double a, const double* __restrict__ x,
                                                    const double b, const double* y, double* out) {
@@ -124,6 +130,10 @@ double kv_dot(const KrylovSpace& ks, const double* x, const double* y, cudaStrea
 void kv_axpby(const KrylovSpace& ks, double a, const double* x, double b, const double* y, double* out,
               cudaStream_t s) {
     dev::k_kv_axpby<<<dev::KV_BLOCKS, dev::KV_T, 0, s>>>(ks.n, a, x, b, y, out);
+}
+
+void kv_mul(const KrylovSpace& ks, const double* x, const double* y, double* out, cudaStream_t s) {
+    dev::k_kv_mul<<<dev::KV_BLOCKS, dev::KV_T, 0, s>>>(ks.n, x, y, out);
 }
 
 // w -= sum_i h[i] V_i

@@ -38,6 +38,9 @@ double kv_dot(const KrylovSpace& ks, const double* x, const double* y, cudaStrea
 void kv_axpby(const KrylovSpace& ks, double a, const double* x, double b, const double* y, double* out,
               cudaStream_t s);
 
+// out = x .* y
+void kv_mul(const KrylovSpace& ks, const double* x, const double* y, double* out, cudaStream_t s);
+
 // Solves A x = b to ||b - A x|| <= rtol ||b|| or max_it Arnoldi steps, x
 // starting from its content (x_zero: from 0, x is overwritten).
 FgmresResult fgmres(KrylovSpace& ks, const double* b, double* x, bool x_zero, double rtol, int max_it,

@@ -186,6 +186,7 @@ struct AdjArgs {
     void* lt = nullptr;       // int4 [2N] limiter max/min target cells
     void* u = nullptr;        // d4 [N] result
     void* bqbar = nullptr;    // d4 [B] result (boundary states)
+    int dirs_per_pass = 4;    // face kernel: input directions per vector-dual pass (1, 2 or 4)
 };
 // gradients and limiter of state p (and the local time step when with_dt)
 void enqueue_adjoint_prep(const StepArgs& a, int p, bool with_dt, cudaStream_t s);

@@ -95,11 +95,11 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def _setup_gpu(precision, m, q0, variant="auto", block=0):
+def _setup_gpu(precision, m, q0, variant="auto", block=0, adjoint_directions=4):
     from aeroflex_gb300 import rans
     st = rans.Settings()
     st.set("solver", "explicit").set("precision", precision).set("start_cfl", 1.0).set("relaxation", 0.9)
-    st.set("kernel_variant", variant).set("block_size", block)
+    st.set("kernel_variant", variant).set("block_size", block).set("adjoint_directions", adjoint_directions)
     st.set_bc("farfield", "farfield", 1.0, MACH, 0.0, 1.0).set_bc("wall", "slip-wall")
     g = rans.Solver(m, st)
     g.init()
@@ -239,16 +239,20 @@ def run_lean(args):
             del g
         return
     if args.adjoint:
-        # transpose-Jacobian products of the FP64 residual (afx_residual_vjp)
-        g = _setup_gpu("fp64", m, q0, "face", args.block)
+        # transpose-Jacobian products of the FP64 residual (afx_residual_vjp),
+        # for each number of input directions per pass of the face kernel
         v = np.random.default_rng(1).standard_normal(4 * m.nRealCells)
-        for _ in range(args.warmup):
-            g.residual_vjp(v)
-        t = time.perf_counter()
-        for _ in range(args.steps):
-            g.residual_vjp(v)
-        print(json.dumps({"adjoint_vjp": True, "cells": m.nRealCells, "steps": args.steps,
-                          "ms_per_vjp_host": (time.perf_counter() - t) / args.steps * 1e3}))
+        for k in [int(x) for x in args.adjoint_directions.split(",")]:
+            g = _setup_gpu("fp64", m, q0, "face", args.block, k)
+            for _ in range(args.warmup):
+                g.residual_vjp(v)
+            t = time.perf_counter()
+            for _ in range(args.steps):
+                g.residual_vjp(v)
+            print(json.dumps({"adjoint_vjp": True, "directions_per_pass": k, "cells": m.nRealCells,
+                              "steps": args.steps,
+                              "ms_per_vjp_host": (time.perf_counter() - t) / args.steps * 1e3}))
+            del g
         return
     for precision in args.precision.split(","):
         g = _setup_gpu(precision, m, q0, args.variant, args.block)
@@ -997,6 +1001,8 @@ def main():
     ap.add_argument("--variant", default="auto", help="--lean: residual kernel variant (auto|gather|face|tile)")
     ap.add_argument("--block", type=int, default=0, help="--lean: threads per block (0: the library's default)")
     ap.add_argument("--adjoint", action="store_true", help="--lean: FP64 residual vJP calls instead of iterations")
+    ap.add_argument("--adjoint-directions", default="4",
+                    help="--lean --adjoint: comma-separated input directions per pass of the face kernel (1, 2, 4)")
     ap.add_argument("--implicit", action="store_true",
                     help="--lean: implicit iterations on the 128x128 airfoil O-mesh (--steps of them)")
     ap.add_argument("--implicit-batch", type=int, default=0,

@@ -92,7 +92,9 @@ int afx_config_from_ini_string(const char* text, afx_config* out);
  * loops, 0 = the same kernels driven from a host loop, for profilers) and
  * krylov_preconditioner (the flexible GMRES of afx_newton_solve and of the
  * implicit adjoint: 1 = a GMRES solve with the implicit matrix, 0 = one
- * ILU(0) sweep with it). */
+ * ILU(0) sweep with it) and adjoint_directions (input directions per pass
+ * of the vJP's face kernel, 1, 2 or 4: vector dual numbers that share the
+ * value's work; every choice gives the same bits). */
 int afx_config_set_double(afx_config c, const char* key, double v);
 int afx_config_get_double(afx_config c, const char* key, double* v);
 /* String fields: solver ("explicit"/"implicit"), gradient ("green-gauss"/
@@ -152,11 +154,13 @@ int afx_run_to_convergence(afx_solver s, double tol, int max_it, int* iters, dou
  * Jacobian-vector products (one-sided differences of the right-hand side),
  * flexible GMRES to lin_tol relative (<= 0: 1e-3; at most max_krylov steps
  * per Newton step, <= 0: 300) preconditioned by the solver's own linear
- * solve with its matrix at `cfl` (<= 0: max_cfl), backtracking on ||RHS||.
- * Stops at err = ||RHS|| / err_0 <= tol (<= 0: the settings' tolerance;
- * err_0 the norm of the freestream state's face fluxes, the
- * normalisation of afx_run_to_convergence without its last-update term) or
- * after max_newton steps (<= 0: 20).
+ * solve with its matrix at `cfl` (<= 0: max_cfl).  Rows are scaled by the
+ * cell perimeter (flux imbalance per unit face length: the wall's thin
+ * cells weigh as much as the far field's large ones), and each step
+ * backtracks on that scaled norm.  Stops at err <= tol (<= 0: the
+ * settings' tolerance), err = ||RHS / perimeter|| over the same norm of the
+ * freestream state's face fluxes, or after max_newton steps (<= 0: 20).
+ * Leaves qW (the last-update term of afx_run_to_convergence's err_0) at 0.
  * A step that finds no decrease after 8 halvings (the round-off floor of
  * the right-hand side) ends the solve at its start; compare err with tol.
  * record (record_cap rows of 4, may be NULL): per Newton step err after it,
