@@ -776,7 +776,7 @@ def c5_adjoint_coupling(n_fd_dirs=4):
     return out
 
 
-def c5_full(iterations=5, n_fd_dirs=2):
+def c5_full(iterations=5, n_fd_dirs=2, smooth=True):
     """Config 5 at its stated size: config 2's hybrid mesh (201k cells),
     Euler, first order, M 0.15, AoA 10 deg.  The primal on an FP32-mixed
     implicit solver (its right-hand side, update and Newton finish are FP64,
@@ -787,14 +787,13 @@ def c5_full(iterations=5, n_fd_dirs=2):
     state; gradients of C_L and C_D along 16 random unit normal-displacement
     directions (seed 3).  Central differences of converged solutions check
     them two ways: along the first ``n_fd_dirs`` random directions with
-    step 1e-5 (the largest that leaves the boundary layer's first cells,
-    1e-6 chord high, uninverted under node-to-node random displacements; the
-    residual's round-off floor, ~1e-11 of its freestream value, is then
-    reached after about two orders of reduction of what the step perturbs,
-    so this difference is short by up to ~1e-2), and along two smooth
+    steps 1e-6 and 3e-7 (node-to-node random displacements of a step of
+    1e-5 already reach 40% of the boundary layer's first cell height, 1e-6
+    chord, and the cell metrics' curvature then puts ~1e-3 of truncation
+    error in the difference), and (``smooth``) along two smooth
     vertical-displacement directions (random sine series over the chord,
-    unit norm) with steps 1e-3 and 3e-4, where it is accurate; then
-    ``iterations`` coupling iterations with the 50-element beam."""
+    unit norm) with steps 1e-3 and 3e-4; then ``iterations`` coupling
+    iterations with the 50-element beam."""
     import math as _m
 
     import numpy as np
@@ -858,20 +857,22 @@ def c5_full(iterations=5, n_fd_dirs=2):
 
     rnd = []
     for j in range(n_fd_dirs):
-        r = central(lambda g, t_: g.deform_patch(t_ * D[j], "wall"), 1e-5)
-        rnd.append({o: {"adjoint": float(grads[o][j]), "fd_step_1e-5": r[o],
-                        "rel_diff": abs(grads[o][j] - r[o]) / abs(r[o])} for o in r})
-    smooth = []
-    for j in range(2):
+        r6 = central(lambda g, t_: g.deform_patch(t_ * D[j], "wall"), 1e-6)
+        r7 = central(lambda g, t_: g.deform_patch(t_ * D[j], "wall"), 3e-7)
+        rnd.append({o: {"adjoint": float(grads[o][j]), "fd_step_1e-6": r6[o], "fd_step_3e-7": r7[o],
+                        "rel_diff_vs_fd_1e-6": abs(grads[o][j] - r6[o]) / abs(r6[o]),
+                        "rel_fd_step_disagreement": abs(r6[o] - r7[o]) / abs(r6[o])} for o in r6})
+    sm = []
+    for j in range(2 if smooth else 0):
         r3 = central(lambda g, t_: g.deform_patch_xy(0 * S[j, :, 0], t_ * S[j, :, 1], "wall"), 1e-3)
         r4 = central(lambda g, t_: g.deform_patch_xy(0 * S[j, :, 0], t_ * S[j, :, 1], "wall"), 3e-4)
-        smooth.append({o: {"adjoint": float(gsm[o][j]), "fd_step_1e-3": r3[o], "fd_step_3e-4": r4[o],
+        sm.append({o: {"adjoint": float(gsm[o][j]), "fd_step_1e-3": r3[o], "fd_step_3e-4": r4[o],
                            "rel_diff_vs_fd_3e-4": abs(gsm[o][j] - r4[o]) / abs(r4[o]),
                            "rel_fd_step_disagreement": abs(r3[o] - r4[o]) / abs(r4[o])} for o in r3})
     for g in (s32, s64):
         g.deform_patch(np.zeros(len(ids)), "wall")
     converge()
-    out["gradient_vs_fd"] = {"random_normal_directions": rnd, "smooth_vertical_directions": smooth}
+    out["gradient_vs_fd"] = {"random_normal_directions": rnd, "smooth_vertical_directions": sm}
     if iterations <= 0:
         out["wall_s"] = time.time() - t0
         return out
@@ -999,6 +1000,8 @@ def main():
                     help="run config 5 at its stated size (201k cells; about 10 minutes) alone and print it")
     ap.add_argument("--c5-full-iterations", type=int, default=5,
                     help="--c5-full: coupling iterations (0: the gradients and their checks only)")
+    ap.add_argument("--c5-full-no-smooth", action="store_true",
+                    help="--c5-full: skip the differences along smooth directions")
     ap.add_argument("--nx", type=int, default=NX)
     ap.add_argument("--ny", type=int, default=NY)
     ap.add_argument("--lean", action="store_true", help="warm-up + timed iterations only (for ncu)")
@@ -1031,7 +1034,7 @@ def main():
         print(json.dumps({"c5_adjoint_coupling": c5_adjoint_coupling()}))
         return
     if args.c5_full:
-        print(json.dumps({"c5_full": c5_full(args.c5_full_iterations)}))
+        print(json.dumps({"c5_full": c5_full(args.c5_full_iterations, smooth=not args.c5_full_no_smooth)}))
         return
     # replicas only: each rank runs the full workload on its own GPU
     if world > 1:
