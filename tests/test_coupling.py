@@ -2,8 +2,9 @@
 aeroelastic coupling they drive (aeroflex_gb300/coupling.py).
 
 - CPU: the beam against the closed-form cantilever, the load-vector size
-  rule of set_Load_Vector_From_Vector (model.hpp:94-100), and the
-  rank-one Newton update against a dense solve.
+  rule of set_Load_Vector_From_Vector (model.hpp:94-100), the rank-one
+  Newton update against a dense solve, and the loads' wall-face geometry
+  against the library's metrics of the deflected wall.
 - GPU, the config 2 generator at 8k cells (Euler, first order, M 0.15,
   AoA 10 deg, implicit solver then its Newton-Krylov finish to 3e-12,
   just above the round-off floor of the right-hand side's norm there):
@@ -72,6 +73,35 @@ def test_rank_one_newton_solves_the_linearised_beam():
     A = b.K_final - np.outer(b.apply_spc(s), g)
     want = np.linalg.solve(A, b.apply_spc(F - s * (g @ u)))
     np.testing.assert_allclose(x, want, rtol=1e-10, atol=1e-14)
+
+
+def test_coupling_wall_faces_are_the_mesh_metrics_of_the_deflected_wall(afx):
+    # the loads' face geometry for a deflected wall equals the metrics the
+    # library forms for those node positions (order, normals into the body,
+    # lengths, centres); host code only
+    m = _small_mesh()
+    M = afx.mesh.from_arrays(m)
+    names = M.boundary_names()
+    be = M.get_int("boundary_edges")
+    wall = np.array([n == "wall" for n in names])
+    ids = np.unique(M.get_int("edges_nodes").reshape(-1, 2)[be[wall]].ravel())
+
+    class Patch:  # the node list a solver's afx_patch_nodes returns
+        def patch_nodes(self, patch):
+            return ids, np.zeros(len(ids)), np.ones(len(ids))
+
+    beam = coupling.Beam(50, 1e4)
+    cpl = coupling.Coupling(Patch(), M, m, beam, 1000.0)
+    u = np.zeros(beam.n_dof)
+    u[0::2] = 3e-4 * beam.xn ** 2  # 0.3 mm at the trailing edge: no cell of the first layer inverts
+    a = cpl.surface_displacement(u)
+    xc, nx, ny, L = cpl.wall_faces(a)
+    y = np.array(m["y"], np.float64)
+    y[ids] += a
+    M2 = afx.mesh.from_arrays(dict(m, y=y))
+    e = be[wall]
+    for got, key in ((xc, "ex"), (nx, "nx"), (ny, "ny"), (L, "L")):
+        np.testing.assert_allclose(got, M2.get(key)[e], rtol=0, atol=1e-15)
 
 
 def _small_mesh():
