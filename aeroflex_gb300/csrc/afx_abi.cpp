@@ -836,6 +836,8 @@ int afx_mesh_get(afx_mesh mp, const char* what, double* out, long long cap, long
         else if (w == "ny") v = &m.edgesNormalsY;
         else if (w == "L") v = &m.edgesLengths;
         else if (w == "wall_dist") v = &m.wall_dist;
+        else if (w == "node_x") v = &m.nodesX;
+        else if (w == "node_y") v = &m.nodesY;
         if (!v) throw Error(AFX_ERR_ARG, "unknown mesh array '" + w + "'");
         if (n) *n = (long long)v->size();
         if (out) std::memcpy(out, v->data(), std::min<long long>(cap, (long long)v->size()) * sizeof(double));

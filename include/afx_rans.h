@@ -59,7 +59,8 @@ int afx_mesh_from_arrays(int n_nodes, const double* x, const double* y, int n_ce
  * (mesh.h:209-246 sizes; nRealCells, mesh.h:869). */
 int afx_mesh_counts(afx_mesh m, long long counts[5]);
 /* Copies one FP64 metric in reference order: "cx","cy","area" (all cells incl.
- * ghosts), "ex","ey","nx","ny","L" (edges), "wall_dist" (cells), mesh.h:378-453. */
+ * ghosts), "ex","ey","nx","ny","L" (edges), "wall_dist" (cells), mesh.h:378-453;
+ * "node_x","node_y" (the node coordinates, nodesX/nodesY, mesh.h:209-210). */
 int afx_mesh_get(afx_mesh m, const char* what, double* out, long long cap, long long* n);
 /* Integer topology: "edges_cells" (2/edge), "edges_nodes" (2/edge),
  * "boundary_edges" (edge id per boundary edge), "cell_order" (device

@@ -3,8 +3,9 @@ aeroelastic coupling they drive (aeroflex_gb300/coupling.py).
 
 - CPU: the beam against the closed-form cantilever, the load-vector size
   rule of set_Load_Vector_From_Vector (model.hpp:94-100), the rank-one
-  Newton update against a dense solve, and the loads' wall-face geometry
-  against the library's metrics of the deflected wall.
+  Newton update against a dense solve, the loads' wall-face geometry
+  against the library's metrics of the deflected wall, and the C++ beam
+  (include/afx_coupling.hpp) against this one.
 - GPU, the config 2 generator at 8k cells (Euler, first order, M 0.15,
   AoA 10 deg, implicit solver then its Newton-Krylov finish to 3e-12,
   just above the round-off floor of the right-hand side's norm there):
@@ -102,6 +103,32 @@ def test_coupling_wall_faces_are_the_mesh_metrics_of_the_deflected_wall(afx):
     e = be[wall]
     for got, key in ((xc, "ex"), (nx, "nx"), (ny, "ny"), (L, "L")):
         np.testing.assert_allclose(got, M2.get(key)[e], rtol=0, atol=1e-15)
+
+
+def test_cpp_beam_matches_the_python_beam(afx, tmp_path):
+    # include/afx_coupling.hpp's beam (dense LU) against coupling.Beam
+    # (numpy), and the whole header, coupling loop included, compiles and
+    # links against the library
+    import os
+    import subprocess
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    exe = str(tmp_path / "beam_coupling")
+    lib = os.path.dirname(afx.LIB_PATH)
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-Wall", "-I", os.path.join(root, "include"),
+                           os.path.join(root, "aeroflex_gb300", "cpp", "beam_coupling.cpp"), "-o", exe,
+                           "-L", lib, "-lafx_rans", "-Wl,-rpath," + lib])
+    out = subprocess.run([exe, "beam"], capture_output=True, text=True, check=True).stdout.split("\n")
+    uniform, tip = (np.array(list(map(float, l.split()))) for l in out[:2])
+    b = coupling.Beam(50, 1e4, 1.0)
+    xs = (np.arange(40000) + 0.5) / 40000
+    F = b.shape_matrix(xs).T @ np.full(xs.size, 1.0 / xs.size)
+    # two LU factorisations of a stiffness whose entries span 1 (the
+    # clamped rows) to 1.25e9 (EI/L_e^3), and loads summed in another order:
+    # they agree to ~1e-10, not to the last bit
+    np.testing.assert_allclose(uniform, b.solve(F), rtol=1e-9, atol=1e-20)
+    P = np.zeros(b.n_dof)
+    P[-2] = 3.0
+    np.testing.assert_allclose(tip, b.solve(P), rtol=1e-9, atol=1e-20)
 
 
 def _small_mesh():

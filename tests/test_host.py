@@ -213,6 +213,8 @@ def test_mesh_set_nodes_matches_a_fresh_mesh(afx):
     b = afx.mesh.from_arrays(dict(m0, x=x, y=y))
     for what in ("cx", "cy", "area", "ex", "ey", "nx", "ny", "L"):
         np.testing.assert_array_equal(a.get(what), b.get(what), err_msg=what)
+    np.testing.assert_array_equal(a.get("node_x"), x)
+    np.testing.assert_array_equal(a.get("node_y"), y)
     with pytest.raises(afx.AfxError):
         a.set_nodes(x[:-1], y[:-1])
 
