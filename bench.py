@@ -151,6 +151,21 @@ def algorithmic_bytes(kernel, n, f, precision):
     return 0
 
 
+def kernel_rooflines(prof, n, f, precision, peak):
+    """Each profiled kernel's algorithmic bytes per launch over its mean
+    CUDA-event launch time, against the HBM peak (the kernels the launch
+    list shows beside the dominant one)."""
+    out = {}
+    for k, (ms, launches) in prof.items():
+        ab = algorithmic_bytes(k, n, f, precision)
+        if ab <= 0 or launches <= 0 or ms <= 0:
+            continue
+        gbs = ab / (ms / launches * 1e-3) / 1e9
+        out[k] = dict(algorithmic_bytes_per_launch=ab, launch_ms=ms / launches, achieved=gbs, unit="GB/s",
+                      frac=gbs / peak)
+    return out
+
+
 def measured_traffic(kernel, precision, n, f):
     """DRAM bytes per launch of ``kernel`` from the committed ncu summary
     (profiles/traffic.json: measured on a smaller channel, per cell and per
@@ -310,6 +325,10 @@ def run_gpu(args):
                                    traffic=measured_traffic(kname, precision, N, F),
                                    algorithmic_bytes_per_launch=ab, launch_ms=per_launch_s * 1e3),
                      gpu_launches=int(round(launches_per_iter * K)))
+        try:
+            entry["roofline_kernels"] = kernel_rooflines(prof, N, F, precision, hbm_peak)
+        except Exception as ex:  # a report, never a reason to lose the line
+            entry["roofline_kernels"] = {"error": repr(ex)}
         if precision == "fp32-mixed":
             entry["clocks"] = ck
         # end-to-end through the C ABI, every step: the host state (pinned)
@@ -1064,6 +1083,7 @@ def main():
         "roofline": {k: f32["roofline"][k] for k in ("bound", "achieved", "peak", "unit", "frac", "traffic")},
         "roofline_kernel": f32["roofline"],
         "roofline_evaluation": f32["roofline_evaluation"],
+        "roofline_kernels": f32["roofline_kernels"],
         "kernels": f32["kernels"],
         "clocks": f32["clocks"],
         "e2e": f32["e2e"],
@@ -1073,7 +1093,8 @@ def main():
         "fp64": {"value": f64["value"], "unit": "cell-residual evals/s", "ms_per_step": f64["ms_per_step"],
                  "steps": f64["steps"], "dtype": "f64", "e2e": f64["e2e"], "tuned": f64["tuned"],
                  "fp64_ops": f64["fp64_ops"], "roofline_evaluation": f64["roofline_evaluation"],
-                 "roofline_kernel": f64["roofline"], "kernels": f64["kernels"], "gpu_launches": f64["gpu_launches"]},
+                 "roofline_kernel": f64["roofline"], "roofline_kernels": f64["roofline_kernels"],
+                 "kernels": f64["kernels"], "gpu_launches": f64["gpu_launches"]},
         "setup_s": r["setup_s"],
     }
     if not args.no_cpu:
