@@ -1624,6 +1624,7 @@ static double newton_run(afx_solver_s* s, double tol, int max_newton, double cfl
     AFX_CUDA(cudaEventRecord(s->ev0, s->stream));
     s->imp_rhs(p);
     double e = scaled_norm(s->imp_b);
+    bool have_q0 = false;  // q0 holds the current step's start (restored if the step fails)
     try {
         while (e / err0 > tol && nn < max_newton) {
             if (!(e == e)) throw Error(AFX_ERR_NONFINITE, "newton: residual norm is not finite");
@@ -1631,6 +1632,7 @@ static double newton_run(afx_solver_s* s, double tol, int max_newton, double cfl
             m.cfl = cfl;
             implicit_fill(s->imp, m, p, s->stream);
             AFX_CUDA(cudaMemcpyAsync(q0.p, qm, N * 32, cudaMemcpyDeviceToDevice, s->stream));
+            have_q0 = true;
             // the scaled system (W J) dq = W RHS, W = 1 / perimeter
             kv_mul(ks, W, (const double*)s->imp_b, (double*)b.p, s->stream);
             const double qrms = std::sqrt(kv_dot(ks, (const double*)q0.p, (const double*)q0.p, s->stream) / n4);
@@ -1681,9 +1683,11 @@ static double newton_run(afx_solver_s* s, double tol, int max_newton, double cfl
             }
             e = en;
             ++nn;
+            have_q0 = false;  // the step is taken (or undone): nothing to restore
             if (stalled) break;
         }
     } catch (...) {
+        if (have_q0) cudaMemcpyAsync(qm, q0.p, N * 32, cudaMemcpyDeviceToDevice, s->stream);
         s->imp_sync();
         throw;
     }

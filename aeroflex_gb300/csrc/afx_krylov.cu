@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(KV_T) k_kv_axpby(const long long n, const doub
 namespace {
 
 void kchk(cudaError_t r, const char* what) {
-    if (r != cudaSuccess) throw Error(7, std::string("krylov: ") + what + ": " + cudaGetErrorString(r));
+    if (r != cudaSuccess) throw Error(AFX_ERR_CUDA, std::string("krylov: ") + what + ": " + cudaGetErrorString(r));
 }
 
 }  // namespace
